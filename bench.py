@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""CT ADMM-TV benchmark: iterations/s of the 512x512 / 360-view / 725-bin
+ADMM-TV reconstruction (lambda 0.005, rho 2, 100 iterations, CG <= 10).
+
+A step is one complete 100-iteration ADMM-TV solve from x0 = 0 of a seeded
+synthetic sinogram (20-ellipse phantom, 0.5%-of-peak Gaussian noise).
+
+  value     iterations/s with the sinogram resident on the device: the fused
+            native solver (ct_admm_tv_solve, each iteration one CUDA graph),
+            CUDA events around each step, L2 flushed (256 MB write) before
+            every step outside the events.
+  e2e       the same metric through the public API (scico_gb300.optimize.ADMM
+            with SquaredL2Loss / XRayTransform2D / FiniteDifference / L21Norm),
+            with the sinogram copied from pinned host memory and the
+            reconstruction copied back inside the timed region.
+  roofline  the forward projector (dominant kernel) timed live with CUDA
+            events: algorithmic bytes = 4 B per pixel-view interaction +
+            the sinogram write, against the measured HBM copy bandwidth.
+  cpu_baseline  the C/OpenMP restatement of scico's path (reference float32
+            policy) timed on the host cores on a bounded sample.
+
+``--impl reference`` times that CPU restatement alone as the reference arm
+(scico itself runs on JAX, which is not installable on these machines).
+Multi-GPU (``--gpus N`` under torchrun): independent replicas, no collective
+on the data path; value = all ranks' iterations / max time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "CT ADMM-TV iters/s"
+UNIT = "iter/s"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM = 6800.0
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--cpu-iters", type=int, default=1, help="ADMM iterations per CPU-baseline sample")
+    return ap.parse_args()
+
+
+def _workload(name):
+    from scico_gb300 import workloads
+
+    return {"c1": workloads.C1, "c2": workloads.C2}[name]
+
+
+def _config_json(c, name):
+    return {
+        "workload": f"ct_admm_tv_2d_{c.n}x{c.n}_{c.n_views}v_{c.det_count}b",
+        "config": name,
+        "image": c.n,
+        "views": c.n_views,
+        "det_count": c.det_count,
+        "admm_iters_per_step": c.maxiter,
+        "cg_maxiter": c.cg_maxiter,
+        "lambda": c.lam,
+        "rho": c.rho,
+        "l2_flush": "256 MB write before every step",
+        "parallelism": "replicas",
+    }
+
+
+def _hbm_peak():
+    try:
+        return float(json.loads(PEAKS.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={','.join(self.FIELDS)}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.result = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return False
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[2:]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if sm:
+            self.result = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                           "samples": len(sm)}
+        return False
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement (baseline and reference arm)
+# ---------------------------------------------------------------------------
+
+
+def cpu_sample(c, iters: int, threads: int):
+    """Time `iters` ADMM-TV iterations of workload `c` on the CPU restatement."""
+    from oracle import ctref_c
+    from scico_gb300 import workloads
+
+    G = ctref_c.Geometry((c.n, c.n), c.angles, det_count=c.det_count)
+    used = ctref_c.set_threads(threads)
+    x_gt = c.phantom()
+    y = workloads.noisy(G.project(x_gt), c.noise, c.noise_seed)
+    t0 = time.perf_counter()
+    G.admm_tv(y, c.lam, c.rho, iters, cg_maxiter=c.cg_maxiter, cg_tol=c.cg_tol)
+    dt = time.perf_counter() - t0
+    return iters / dt, used, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import ctref_c
+
+    c = _workload(args.config)
+    threads = ctref_c.default_threads()
+    for _ in range(args.warmup):
+        cpu_sample(c, args.cpu_iters, threads)
+    total_it, total_t, used = 0, 0.0, threads
+    for _ in range(args.steps):
+        _, used, dt = cpu_sample(c, args.cpu_iters, threads)
+        total_it += args.cpu_iters
+        total_t += dt
+    value = total_it / total_t
+    sample = (f"{args.cpu_iters} ADMM-TV iteration(s) per step of the {c.n}x{c.n}/{c.n_views}/{c.det_count} "
+              f"workload; C/OpenMP restatement of scico's float32 path (scico runs on JAX, not installable here)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded 20-ellipse phantom, 0.5% Gaussian noise)",
+        "config": _config_json(c, args.config),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+
+def run_gpu(args):
+    import ctypes
+
+    import torch
+
+    from scico_gb300 import _device, _lib, functional, linop, loss, workloads
+    from scico_gb300.optimize import ADMM, LinearSubproblemSolver
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    c = _workload(args.config)
+
+    # ---- workload (device) -------------------------------------------------
+    A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+    x_gt = torch.from_numpy(c.phantom()).to(dev)
+    y_clean = A(x_gt).cpu().numpy()
+    y_host_np = workloads.noisy(y_clean, c.noise, c.noise_seed)
+    y_host = torch.from_numpy(y_host_np).pin_memory()
+    y_dev = y_host.to(dev)
+    g = A.geometry()
+    desc = _lib.AdmmTvDesc(g, c.maxiter, c.cg_maxiter, c.cg_tol, 0.0, c.lam, 0.0, c.rho, 0.5, 1.0, 1)
+    nbytes = _lib.c_size_t()
+    _lib.call("ct_admm_tv_workspace", ctypes.addressof(desc), ctypes.addressof(nbytes))
+    ws = _device.workspace(nbytes.value)
+    x = torch.zeros((c.n, c.n), device=dev)
+    itstat = torch.zeros((c.maxiter, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def solve():
+        x.zero_()
+        _lib.call("ct_admm_tv_solve", ctypes.addressof(desc), y_dev.data_ptr(), x.data_ptr(), itstat.data_ptr(),
+                  0, ws.data_ptr(), ws.numel(), stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        solve()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- timed: device-resident --------------------------------------------
+    barrier()
+    times = []
+    with ClockSampler(dev.index) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solve()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    barrier()
+    t_local = sum(times)
+    t_max = t_local
+    if dist is not None:
+        tt = torch.tensor([t_local], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    iters_total = c.maxiter * args.steps * world
+    value = iters_total / t_max
+    objective = float(itstat[c.maxiter - 1, _lib.CT_ITSTAT_OBJECTIVE])
+    x_dev = x.clone()
+
+    # ---- timed: end to end through the public API ----------------------------
+    def e2e_step():
+        yd = torch.empty((c.n_views, c.det_count), device=dev)
+        yd.copy_(y_host, non_blocking=True)
+        f = loss.SquaredL2Loss(y=yd, A=A)
+        C = linop.FiniteDifference((c.n, c.n), append=0)
+        s = ADMM(f=f, g_list=[c.lam * functional.L21Norm()], C_list=[C], rho_list=[c.rho], maxiter=c.maxiter,
+                 subproblem_solver=LinearSubproblemSolver(cg_kwargs={"tol": c.cg_tol, "maxiter": c.cg_maxiter}))
+        xr = s.solve()
+        return xr.cpu()
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xr = e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    barrier()
+    e2e_t = sum(e2e_times)
+    if dist is not None:
+        tt = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    e2e_value = c.maxiter * args.steps * world / e2e_t
+    e2e_dev_diff = float((xr.to(dev) - x_dev).norm() / x_dev.norm())
+
+    # ---- roofline: the forward projector, live CUDA events ---------------------
+    fwd_bytes, _ = A.workspace_bytes(1)
+    pws = _device.workspace(fwd_bytes)
+    sino = torch.empty((c.n_views, c.det_count), device=dev)
+    img = x_dev.clone()
+    bp = torch.empty_like(img)
+
+    def time_launches(fn, reps=20):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return statistics.median(ts)
+
+    t_fwd = time_launches(lambda: _lib.call("ct_proj2d_fwd", ctypes.addressof(g), img.data_ptr(), sino.data_ptr(),
+                                            1, pws.data_ptr(), pws.numel(), stream.cuda_stream))
+    t_adj = time_launches(lambda: _lib.call("ct_proj2d_adj", ctypes.addressof(g), sino.data_ptr(), bp.data_ptr(),
+                                            1, pws.data_ptr(), pws.numel(), stream.cuda_stream))
+    inter = c.interactions
+    alg_fwd = 4.0 * inter + 4.0 * c.n_views * c.det_count
+    alg_adj = 4.0 * inter + 4.0 * c.n * c.n
+    peak, peak_kind = _hbm_peak()
+    achieved = alg_fwd / t_fwd / 1e9
+    traffic = None
+    prof = ROOT / "profiles" / "ncu_traffic.json"
+    if prof.exists():
+        try:
+            traffic = json.loads(prof.read_text()).get("proj2d_fwd_c2_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # ---- CPU baseline (rank 0, N = 1) -----------------------------------------
+    cpu = None
+    if rank == 0 and world == 1:
+        try:
+            from oracle import ctref_c
+
+            v, used, dt = cpu_sample(c, args.cpu_iters, ctref_c.default_threads())
+            cpu = {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+                   "sample": f"{args.cpu_iters} ADMM-TV iteration(s) (CG<=10, itstat on) of the same workload, "
+                             f"C/OpenMP restatement of scico's float32 path, {dt:.1f} s"}
+        except Exception as exc:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+
+    K = c.cg_maxiter
+    launches_per_step = 4 + c.maxiter * (8 + 7 * K) + 5
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 20-ellipse phantom, 0.5% Gaussian noise)",
+            "config": _config_json(c, args.config),
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(c.n_views * c.det_count * 4),
+                    "d2h_bytes_per_step": int(c.n * c.n * 4),
+                    "api": "scico_gb300.optimize.ADMM(...).solve()", "rel_diff_vs_value_path": e2e_dev_diff},
+            "roofline": {"bound": "hbm", "kernel": "ct_proj2d_fwd", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes": alg_fwd, "launch_s": t_fwd,
+                         "interactions_per_s": inter / t_fwd,
+                         "adjoint": {"launch_s": t_adj, "achieved": alg_adj / t_adj / 1e9,
+                                     "frac": alg_adj / t_adj / 1e9 / peak}},
+            "cpu_baseline": cpu,
+            "clocks": clk.result,
+            "gpu_launches": launches_per_step * args.steps,
+            "final_objective": objective,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

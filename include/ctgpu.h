@@ -1,0 +1,272 @@
+/*
+ * ctgpu.h -- C ABI of the GB300 (sm_103a) CT reconstruction hot path.
+ *
+ * The library replaces the array kernels behind scico's parallel-beam CT
+ * ADMM-TV path.  Every entry point takes plain pointers and sizes, enqueues
+ * its work on the caller's CUDA stream and returns a ct_status; none of them
+ * allocates device memory.  Scratch memory, where an operation needs it, is
+ * a caller-provided workspace whose size is reported by a *_workspace query
+ * (the way an XLA FFI handler gets a scratch buffer from XLA, or a torch
+ * binding gets one from the caching allocator).
+ *
+ * Interfaces replaced (scico, path within the scico source tree):
+ *   ct_proj2d_*   scico/linop/xray/_xray2d.py  XRayTransform2D
+ *   ct_proj3d_*   scico/linop/xray/_xray3d.py  XRayTransform3D
+ *   ct_fd_*       scico/linop/_diff.py         FiniteDifference (+ its adjoint)
+ *   ct_l21_*      scico/functional/_norm.py    L21Norm, L1Norm
+ *   ct_cg_ and ct_dot scico/solver.py          cg
+ *   ct_admm_tv_*  scico/optimize/_admm.py + _admmaux.py  ADMM with
+ *                 LinearSubproblemSolver on 0.5||Ax-y||^2 + sum_i lam_i g_i(Dx)
+ *
+ * Conventions: all arrays are C-order float32 on the device unless noted;
+ * "batch" stacks independent problems that share one geometry along a new
+ * leading axis.  Results are deterministic: no kernel uses floating-point
+ * atomics, every reduction runs in a fixed order.
+ */
+#ifndef CTGPU_H
+#define CTGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A cudaStream_t, passed through unchanged (0 = legacy default stream). */
+typedef void* ct_stream_t;
+
+typedef enum ct_status {
+  CT_OK = 0,
+  CT_ERR_INVALID_ARG = 1, /* null pointer, bad enum, non-positive size     */
+  CT_ERR_SHAPE = 2,       /* sizes that do not conform                     */
+  CT_ERR_UNSUPPORTED = 3, /* valid request outside what the library covers */
+  CT_ERR_CUDA = 4,        /* a CUDA runtime call or launch failed          */
+  CT_ERR_TIMEOUT = 5,     /* a bounded device wait ran out                 */
+  CT_ERR_NONFINITE = 6,   /* NaN/Inf met where the caller asked to stop    */
+  CT_ERR_WORKSPACE = 7,   /* workspace missing, misaligned or too small    */
+  CT_ERR_NO_DEVICE = 8    /* no usable CUDA device                         */
+} ct_status;
+
+/* Library identification and error text. */
+const char* ct_version(void);
+const char* ct_status_string(ct_status s);
+/* Message of the last failing call on the calling host thread ("" if none). */
+const char* ct_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* 2D parallel-beam projector (XRayTransform2D)                             */
+/* ------------------------------------------------------------------------ */
+
+/* Floats per view in the per-view geometry table. */
+#define CT_VIEW2D_STRIDE 8
+
+/*
+ * Fill the per-view geometry table on the HOST, in float32 arithmetic and in
+ * the order of XRayTransform2D._calc_weights (scico/linop/xray/_xray2d.py:
+ * 326-347): u = (cos a, sin a); Px0 = x0[0]u0 + x0[1]u1 - y0;
+ * Pdx = (dx0 u0, dx1 u1); Pxmin = min of the 4 pixel-corner projections;
+ * width = (max(|Pdx0+Pdx1|,|Pdx0-Pdx1|) + min(...)) / 2.
+ * Row v of views_out = {Pxmin, Pdx0, Pdx1, width, 1/width, 0, 0, 0}.
+ * Also returns (optional, may be NULL) the largest projected pixel width,
+ * the quantity XRayTransform2D.__init__ warns about when > 1 (:96-106).
+ */
+ct_status ct_proj2d_views(const float* angles, int32_t n_views, float x0_0,
+                          float x0_1, float dx0, float dx1, float y0,
+                          float* views_out, float* max_width_out);
+
+typedef struct ct_geom2d {
+  int32_t rows;      /* image axis 0                                   */
+  int32_t cols;      /* image axis 1                                   */
+  int32_t n_views;   /* number of angles                               */
+  int32_t det_count; /* detector bins                                  */
+  const float* views; /* DEVICE pointer to the n_views x 8 view table  */
+  float max_width;   /* max_width_out of ct_proj2d_views for the table */
+} ct_geom2d;
+
+/* Workspace bytes that ct_proj2d_fwd / ct_proj2d_adj need for `batch`. */
+ct_status ct_proj2d_workspace(const ct_geom2d* g, int32_t batch,
+                              size_t* fwd_bytes, size_t* adj_bytes);
+
+/*
+ * sino[b, v, :] = A img[b]   (XRayTransform2D.project, _xray2d.py:138-146,
+ * _project :223-265).  img: batch x rows x cols, sino: batch x n_views x
+ * det_count.  Tile-owned pixel-driven sweep: each CTA owns an image tile
+ * and a run of views, bins of one tile are reduced in shared memory and the
+ * per-tile partial bins are summed in a fixed order by a second pass.
+ */
+ct_status ct_proj2d_fwd(const ct_geom2d* g, const float* img, float* sino,
+                        int32_t batch, void* workspace, size_t workspace_bytes,
+                        ct_stream_t stream);
+
+/*
+ * img[b] = A^T sino[b]  (XRayTransform2D.back_project, :148-156,
+ * _back_project :267-306).  Pixel-driven gather with the forward's weights,
+ * views summed in a fixed order, no atomics.
+ */
+ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
+                        int32_t batch, void* workspace, size_t workspace_bytes,
+                        ct_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Finite differences (FiniteDifference / SingleAxisFiniteDifference)       */
+/* ------------------------------------------------------------------------ */
+
+/* prepend/append: -1 = None, 0 or 1 as in scico/linop/_diff.py:157-225.  */
+typedef struct ct_fd_desc {
+  int32_t ndim;      /* 1, 2 or 3                                        */
+  int32_t shape[3];  /* input shape (first ndim entries)                 */
+  int32_t naxes;     /* number of differenced axes                       */
+  int32_t axes[3];   /* the axes, in output-block order                  */
+  int32_t prepend;   /* -1, 0, 1                                         */
+  int32_t append;    /* -1, 0, 1                                         */
+  int32_t circular;  /* 0 / 1 (then prepend = append = -1)               */
+} ct_fd_desc;
+
+/* Number of output elements: the blocks of every axis, concatenated in axis
+ * order (when all blocks share one shape this is the (naxes, *shape) stack of
+ * VerticalStack, scico/operator/_stack.py:87-88,126-129). */
+ct_status ct_fd_out_count(const ct_fd_desc* d, int64_t* count);
+
+/* out = D x   (SingleAxisFiniteDifference._eval, _diff.py:236-272). */
+ct_status ct_fd_fwd(const ct_fd_desc* d, const float* x, float* out,
+                    int32_t batch, ct_stream_t stream);
+
+/* x = D^T out = sum_k D_k^T out_k  (adjoint of the above; the reference
+ * derives it with jax.linear_transpose, scico/_core.py:140-153, summed per
+ * block in scico/linop/_stack.py:71-72). */
+ct_status ct_fd_adj(const ct_fd_desc* d, const float* dx, float* x,
+                    int32_t batch, ct_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Proximal operators and norms (scico/functional/_norm.py)                 */
+/* ------------------------------------------------------------------------ */
+
+/* out = prox_{lam ||.||_{2,1}}(v), l2 over the leading axis of ncomp
+ * components each of n elements (L21Norm._prox with l2_axis=0, :254-263,
+ * no_nan_divide scico/numpy/util.py:302-315). out may alias v. */
+ct_status ct_l21_prox(const float* v, float* out, int32_t ncomp, int64_t n,
+                      float lam, ct_stream_t stream);
+
+/* out = sign(v) max(|v| - lam, 0)  (L1Norm.prox, _norm.py:84-117). */
+ct_status ct_l1_prox(const float* v, float* out, int64_t n, float lam,
+                     ct_stream_t stream);
+
+/* *out_dev (float64, device) = sum_n sqrt(sum_c v[c,n]^2) (L21Norm.__call__,
+ * :246-250) -- or, when ncomp == 0, sum |v| over n (L1Norm.__call__). */
+ct_status ct_l21_norm(const float* v, int32_t ncomp, int64_t n,
+                      double* out_dev, void* workspace, size_t workspace_bytes,
+                      ct_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Reductions and CG vector steps (scico/solver.py:326-405)                 */
+/* ------------------------------------------------------------------------ */
+
+/* Workspace bytes for one reduction (ct_dot, ct_l21_norm, ct_cg_*).  The
+ * workspace must be zero-filled before its first use; every reduction leaves
+ * it zero-filled again.  Reductions that share one workspace must not
+ * overlap in time (issue them on one stream). */
+size_t ct_reduce_workspace(void);
+
+/* *out_dev (float64, device) = sum a[i] b[i], products and sums in float64,
+ * fixed summation order. */
+ct_status ct_dot(const float* a, const float* b, int64_t n, double* out_dev,
+                 void* workspace, size_t workspace_bytes, ct_stream_t stream);
+
+/* Device-resident CG scalars (float64), indices into a double[16]. */
+#define CT_CG_NUM 0       /* <r, r>                                  */
+#define CT_CG_PAP 1       /* <p, A p>                                */
+#define CT_CG_ALPHA 2
+#define CT_CG_BETA 3
+#define CT_CG_BNORM 4     /* ||b||                                   */
+#define CT_CG_TOL2 5      /* max(tol ||b||, atol)^2                  */
+#define CT_CG_ITERS 6     /* iterations taken                        */
+#define CT_CG_DONE 7      /* 1 once num <= TOL2 or ITERS == maxiter  */
+#define CT_CG_MAXITER 8
+#define CT_CG_RAN 9       /* 1 between an update that ran and its direction step */
+#define CT_CG_NSCALARS 16
+
+/*
+ * CG x/r step: alpha = num / pAp; x += alpha p; r -= alpha Ap;
+ * num' = <r, r>; beta = num'/num; ITERS += 1; DONE when num' <= TOL2 or
+ * ITERS reaches MAXITER.  Skips all work if DONE is already set, so a fixed
+ * number of launches (e.g. captured in a CUDA graph) reproduces the
+ * reference's early exit.  scalars: device double[CT_CG_NSCALARS].
+ */
+ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap,
+                       int64_t n, double* scalars, void* workspace,
+                       size_t workspace_bytes, ct_stream_t stream);
+
+/* p = r + beta p (skipped once DONE was set before the preceding update). */
+ct_status ct_cg_direction(float* p, const float* r, int64_t n,
+                          double* scalars, ct_stream_t stream);
+
+/* CG start: r = b - Ax; p = r; NUM = <r,r>; BNORM = ||b||;
+ * TOL2 = max(tol BNORM, atol)^2; ITERS = 0; DONE = (NUM <= TOL2) || maxiter==0. */
+ct_status ct_cg_init(const float* b, const float* Ax, float* r, float* p,
+                     int64_t n, double tol, double atol, int32_t maxiter,
+                     double* scalars, void* workspace, size_t workspace_bytes,
+                     ct_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Fused ADMM-TV solver (2D)                                                */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * ADMM for  min_x 0.5 ||A x - y||^2 + lam_l21 ||D x||_{2,1} + lam_l1 ||D x||_1
+ * with D = FiniteDifference(append=0) over both image axes, one g_i per
+ * non-zero lam (L21 then L1, sharing D and rho), the x-update solved by CG
+ * on (A^T A + rho_sum D^T D) x = A^T y + sum_i rho_i D^T (z_i - u_i)
+ * (LinearSubproblemSolver, scico/optimize/_admmaux.py:205-269), and the
+ * z/u updates of ADMM.step (scico/optimize/_admm.py:334-378).
+ * Iteration statistics per outer iteration (ADMM itstat fields,
+ * _admm.py:171-198): objective f(x)+sum g_i(z_i), primal residual,
+ * dual residual, CG iterations, CG relative residual.
+ */
+typedef struct ct_admm_tv_desc {
+  ct_geom2d geom;
+  int32_t maxiter;      /* ADMM outer iterations                         */
+  int32_t cg_maxiter;   /* CG cap per x-update                           */
+  double cg_tol;        /* CG relative tolerance                         */
+  double cg_atol;       /* CG absolute tolerance                         */
+  double lam_l21;       /* weight of ||Dx||_{2,1} (0 = term absent)      */
+  double lam_l1;        /* weight of ||Dx||_1     (0 = term absent)      */
+  double rho;           /* ADMM penalty, same for every g_i              */
+  double loss_scale;    /* SquaredL2Loss scale (0.5)                     */
+  double alpha;         /* ADMM relaxation (1.0 = none)                  */
+  int32_t use_graph;    /* 1 = replay the iteration as a CUDA graph      */
+} ct_admm_tv_desc;
+
+/* Fields of one itstat record (double each). */
+#define CT_ITSTAT_OBJECTIVE 0
+#define CT_ITSTAT_PRIMAL 1
+#define CT_ITSTAT_DUAL 2
+#define CT_ITSTAT_CG_ITERS 3
+#define CT_ITSTAT_CG_RELRES 4
+#define CT_ITSTAT_FIELDS 8
+
+ct_status ct_admm_tv_workspace(const ct_admm_tv_desc* d, size_t* bytes);
+
+/* Byte offsets, inside the solver workspace, of the ADMM state arrays
+ * z_list and u_list (ADMM._state_variable_names, _admm.py:200-205): each is
+ * n_terms x 2 x rows x cols float32, term order L2,1 then L1.  n_terms may
+ * be NULL. */
+ct_status ct_admm_tv_state(const ct_admm_tv_desc* d, size_t* z_offset,
+                           size_t* u_offset, int32_t* n_terms);
+
+/*
+ * Run d->maxiter ADMM iterations.  y: sinogram (n_views x det_count);
+ * x: in = x0, out = final x (rows x cols); itstat_dev: device
+ * double[maxiter * CT_ITSTAT_FIELDS] (may be NULL).  z/u state lives in the
+ * workspace; call with iter0 == 0 to initialise z = D x0, u = 0 (ADMM.z_init /
+ * u_init, _admm.py:297-332), or iter0 > 0 to continue from the workspace.
+ */
+ct_status ct_admm_tv_solve(const ct_admm_tv_desc* d, const float* y, float* x,
+                           double* itstat_dev, int32_t iter0, void* workspace,
+                           size_t workspace_bytes, ct_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CTGPU_H */

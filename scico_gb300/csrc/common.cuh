@@ -1,0 +1,112 @@
+// Shared helpers of the ctgpu library: status/error recording, launch checks,
+// exact float32 arithmetic helpers and the deterministic block reduction.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ctgpu.h"
+
+namespace ct {
+
+// Record `s` with a printf-style message for ct_last_error() and return it.
+ct_status fail(ct_status s, const char* fmt, ...);
+// Map a CUDA error to CT_ERR_CUDA (recording `what`), or CT_OK.
+ct_status cuda_check(cudaError_t e, const char* what);
+// cudaGetLastError() after a launch.
+ct_status launch_check(const char* what);
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+inline cudaStream_t as_stream(ct_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+__host__ __device__ inline bool aligned(const void* p, size_t a) {
+  return (reinterpret_cast<uintptr_t>(p) % a) == 0;
+}
+
+inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---------------------------------------------------------------------------
+// Exact float32 arithmetic.  The projector weights must be computed with the
+// same IEEE operations, in the same order, as the reference's float32
+// expressions, so the compiler may not contract a*b+c into an FMA there.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+
+// Detector position of pixel (i, j) for one view:
+// (Pxmin + Pdx0*i) + Pdx1*j, each operation rounded to float32
+// (scico/linop/xray/_xray2d.py:331-335).
+__device__ __forceinline__ float px2d(float pxmin, float pd0, float pd1, int i, int j) {
+  return fadd(fadd(pxmin, fmul(pd0, (float)i)), fmul(pd1, (float)j));
+}
+
+// Boxcar weight of the lower of the two bins a pixel lands in:
+// w = min(1 - (Px - floor(Px)), width) / width (:348-349).  `inv_width` is
+// 1/width rounded to float32; the product differs from the quotient by at
+// most one ulp, and w == 1 exactly whenever the footprint fits the bin.
+__device__ __forceinline__ void boxcar2d(float px, float width, float inv_width,
+                                         int& key, float& w) {
+  const float fl = floorf(px);
+  key = (int)fl;
+  const float dist = fsub(1.0f, fsub(px, fl));
+  w = dist < width ? fmul(dist, inv_width) : 1.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Deterministic float64 reduction: every block writes one partial to
+// `partials[blockIdx.x]`; the last block to finish (integer ticket, so the
+// choice of block does not affect the value) sums the partials in index
+// order.  The ticket is reset by that block, so the sequence can be replayed
+// (e.g. inside a CUDA graph) without host involvement.
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* red /*[NT/32]*/) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < NT / 32; ++k) s += red[k];
+  }
+  return s;  // valid in thread 0 only
+}
+
+// Returns true in thread 0 of the last block; `total` then holds the sum.
+template <int NT>
+__device__ __forceinline__ bool grid_sum_last(double block_total, double* partials,
+                                              unsigned int* ticket, double& total) {
+  __shared__ bool is_last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = block_total;
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    is_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    double s = 0.0;
+    volatile double* vp = partials;
+    for (unsigned int b = 0; b < gridDim.x; ++b) s += vp[b];
+    total = s;
+    *ticket = 0u;
+    return true;
+  }
+  return false;
+}
+
+// Fixed grid size for reductions (independent of the device, so results are
+// reproducible across GPUs).
+constexpr int kReduceBlocks = 304;
+constexpr int kReduceThreads = 256;
+// Workspace layout of one reduction: ticket (256 B aligned) + partials for
+// up to four simultaneous sums.
+constexpr int kReduceMaxSums = 4;
+constexpr size_t kReduceWorkspace = 256 + sizeof(double) * kReduceMaxSums * kReduceBlocks;
+
+}  // namespace ct

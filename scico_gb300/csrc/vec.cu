@@ -1,0 +1,228 @@
+// Deterministic float64 reductions and the CG vector steps of
+// scico.solver.cg (scico/solver.py:378-400), with the stopping test kept on
+// the device so that a fixed launch sequence reproduces the early exit.
+#include "common.cuh"
+
+namespace {
+
+struct RedWs {
+  unsigned int* ticket;
+  double* partials;
+};
+
+ct_status red_ws(void* ws, size_t bytes, const char* who, RedWs& r) {
+  if (!ws || bytes < ct::kReduceWorkspace || !ct::aligned(ws, 256))
+    return ct::fail(CT_ERR_WORKSPACE, "%s: reduction workspace needs %zu bytes (256-B aligned)",
+                    who, ct::kReduceWorkspace);
+  r.ticket = static_cast<unsigned int*>(ws);
+  r.partials = reinterpret_cast<double*>(static_cast<char*>(ws) + 256);
+  return CT_OK;
+}
+
+// Two simultaneous float64 grid sums; the last block gets both totals.
+template <int NT>
+__device__ __forceinline__ bool grid_sum2_last(double a, double b, double* partials,
+                                               unsigned int* ticket, double& ta, double& tb) {
+  __shared__ double red[2][NT / 32];
+  __shared__ bool is_last;
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = a;
+    red[1][warp] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int k = 0; k < NT / 32; ++k) {
+      sa += red[0][k];
+      sb += red[1][k];
+    }
+    partials[2 * blockIdx.x] = sa;
+    partials[2 * blockIdx.x + 1] = sb;
+    __threadfence();
+    is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!is_last || threadIdx.x != 0) return false;
+  __threadfence();
+  volatile double* vp = partials;
+  double sa = 0.0, sb = 0.0;
+  for (unsigned int k = 0; k < gridDim.x; ++k) {
+    sa += vp[2 * k];
+    sb += vp[2 * k + 1];
+  }
+  ta = sa;
+  tb = sb;
+  *ticket = 0u;
+  return true;
+}
+
+constexpr int NT = ct::kReduceThreads;
+
+__global__ void __launch_bounds__(NT)
+    k_dot(const float* __restrict__ a, const float* __restrict__ b, size_t n,
+          double* __restrict__ out, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+  double acc = 0.0;
+  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+    acc += (double)a[e] * (double)b[e];
+  double t0, t1;
+  if (grid_sum2_last<NT>(acc, 0.0, partials, ticket, t0, t1)) *out = t0;
+}
+
+__global__ void __launch_bounds__(NT)
+    k_cg_init(const float* __restrict__ b, const float* __restrict__ Ax, float* __restrict__ r,
+              float* __restrict__ p, size_t n, double tol, double atol, int maxiter,
+              double* __restrict__ s, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+  double rr = 0.0, bb = 0.0;
+  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+    const float be = b[e];
+    const float re = ct::fsub(be, Ax[e]);
+    r[e] = re;
+    p[e] = re;
+    rr += (double)re * (double)re;
+    bb += (double)be * (double)be;
+  }
+  double trr, tbb;
+  if (grid_sum2_last<NT>(rr, bb, partials, ticket, trr, tbb)) {
+    const double bn = sqrt(tbb);
+    const double thr = fmax(tol * bn, atol);
+    s[CT_CG_NUM] = trr;
+    s[CT_CG_PAP] = 0.0;
+    s[CT_CG_ALPHA] = 0.0;
+    s[CT_CG_BETA] = 0.0;
+    s[CT_CG_BNORM] = bn;
+    s[CT_CG_TOL2] = thr * thr;
+    s[CT_CG_ITERS] = 0.0;
+    s[CT_CG_MAXITER] = (double)maxiter;
+    s[CT_CG_RAN] = 0.0;
+    s[CT_CG_DONE] = (maxiter <= 0 || !(trr > thr * thr)) ? 1.0 : 0.0;
+  }
+}
+
+// alpha = num/pAp; x += alpha p; r -= alpha Ap; num' = <r,r>.
+__global__ void __launch_bounds__(NT)
+    k_cg_update(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+                const float* __restrict__ Ap, size_t n, double* __restrict__ s,
+                double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+  if (s[CT_CG_DONE] != 0.0) return;  // uniform over the grid
+  const double alpha = s[CT_CG_NUM] / s[CT_CG_PAP];
+  const float af = (float)alpha;
+  double rr = 0.0;
+  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+    const float pe = p[e];
+    x[e] = ct::fadd(x[e], ct::fmul(af, pe));
+    const float re = ct::fsub(r[e], ct::fmul(af, Ap[e]));
+    r[e] = re;
+    rr += (double)re * (double)re;
+  }
+  double trr, t1;
+  if (grid_sum2_last<NT>(rr, 0.0, partials, ticket, trr, t1)) {
+    const double num_old = s[CT_CG_NUM];
+    s[CT_CG_ALPHA] = alpha;
+    s[CT_CG_NUM] = trr;
+    s[CT_CG_BETA] = trr / num_old;
+    const double it = s[CT_CG_ITERS] + 1.0;
+    s[CT_CG_ITERS] = it;
+    // The direction update still runs for this iteration (reference order);
+    // DONE takes effect from the next update on.
+    s[CT_CG_RAN] = 1.0;
+    if (!(trr > s[CT_CG_TOL2]) || it >= s[CT_CG_MAXITER]) s[CT_CG_DONE] = 1.0;
+  }
+}
+
+// p = r + beta p, only when the preceding update ran.
+__global__ void k_cg_direction(float* __restrict__ p, const float* __restrict__ r, size_t n,
+                               double* __restrict__ s) {
+  if (s[CT_CG_RAN] == 0.0) return;
+  const float bf = (float)s[CT_CG_BETA];
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x)
+    p[e] = ct::fadd(r[e], ct::fmul(bf, p[e]));
+}
+
+// Clears the "update ran" marker once every block of k_cg_direction is done
+// (launched right after it, single thread).
+__global__ void k_cg_direction_done(double* __restrict__ s) { s[CT_CG_RAN] = 0.0; }
+
+}  // namespace
+
+extern "C" {
+
+ct_status ct_dot(const float* a, const float* b, int64_t n, double* out_dev, void* workspace,
+                 size_t workspace_bytes, ct_stream_t stream) {
+  if (!a || !b || !out_dev) return ct::fail(CT_ERR_INVALID_ARG, "ct_dot: null pointer");
+  if (n < 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_dot: n=%lld", (long long)n);
+  RedWs w;
+  ct_status st = red_ws(workspace, workspace_bytes, "ct_dot", w);
+  if (st != CT_OK) return st;
+  k_dot<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(a, b, (size_t)n, out_dev, w.partials,
+                                                            w.ticket);
+  return ct::launch_check("k_dot");
+}
+
+ct_status ct_cg_init(const float* b, const float* Ax, float* r, float* p, int64_t n, double tol,
+                     double atol, int32_t maxiter, double* scalars, void* workspace,
+                     size_t workspace_bytes, ct_stream_t stream) {
+  if (!b || !Ax || !r || !p || !scalars)
+    return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_init: null pointer");
+  if (n < 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_init: n=%lld", (long long)n);
+  RedWs w;
+  ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_init", w);
+  if (st != CT_OK) return st;
+  k_cg_init<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(
+      b, Ax, r, p, (size_t)n, tol, atol, maxiter, scalars, w.partials, w.ticket);
+  return ct::launch_check("k_cg_init");
+}
+
+ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap, int64_t n,
+                       double* scalars, void* workspace, size_t workspace_bytes,
+                       ct_stream_t stream) {
+  if (!x || !r || !p || !Ap || !scalars)
+    return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_update: null pointer");
+  RedWs w;
+  ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_update", w);
+  if (st != CT_OK) return st;
+  k_cg_update<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(x, r, p, Ap, (size_t)n, scalars,
+                                                                  w.partials, w.ticket);
+  return ct::launch_check("k_cg_update");
+}
+
+ct_status ct_cg_direction(float* p, const float* r, int64_t n, double* scalars,
+                          ct_stream_t stream) {
+  if (!p || !r || !scalars) return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_direction: null pointer");
+  cudaStream_t s = ct::as_stream(stream);
+  double* sc = scalars;
+  k_cg_direction<<<ct::kReduceBlocks, NT, 0, s>>>(p, r, (size_t)n, sc);
+  ct_status st = ct::launch_check("k_cg_direction");
+  if (st != CT_OK) return st;
+  k_cg_direction_done<<<1, 1, 0, s>>>(sc);
+  return ct::launch_check("k_cg_direction_done");
+}
+
+}  // extern "C"
+
+#include "kernels.cuh"
+
+namespace ct {
+
+ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, size_t n,
+                           double* scalars, void* red_ws, cudaStream_t s) {
+  unsigned int* ticket = static_cast<unsigned int*>(red_ws);
+  double* partials = reinterpret_cast<double*>(static_cast<char*>(red_ws) + 256);
+  k_cg_update<<<kReduceBlocks, NT, 0, s>>>(x, r, p, Ap, n, scalars, partials, ticket);
+  return launch_check("k_cg_update");
+}
+
+ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, cudaStream_t s) {
+  k_cg_direction<<<kReduceBlocks, NT, 0, s>>>(p, r, n, scalars);
+  ct_status st = launch_check("k_cg_direction");
+  if (st != CT_OK) return st;
+  k_cg_direction_done<<<1, 1, 0, s>>>(scalars);
+  return launch_check("k_cg_direction_done");
+}
+
+}  // namespace ct

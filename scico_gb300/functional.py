@@ -1,0 +1,148 @@
+"""Functionals of the CT ADMM-TV path, mirroring scico.functional.
+
+* :class:`Functional`, :class:`ScaledFunctional` --
+  scico/functional/_functional.py:24-198 (``lam * F`` scales the prox
+  parameter, :198).
+* :class:`L21Norm` -- scico/functional/_norm.py:208-296.
+* :class:`L1Norm` -- scico/functional/_norm.py:65-117.
+
+Values are returned as Python floats accumulated in float64 on the device;
+proxes run in the ctgpu kernels.
+"""
+
+from __future__ import annotations
+
+from typing import Tuple, Union
+
+import numpy as np
+import torch
+
+from . import _device, _lib
+
+
+class Functional:
+    """Base class (scico/functional/_functional.py:24)."""
+
+    has_eval = False
+    has_prox = False
+
+    def __call__(self, x) -> float:
+        raise NotImplementedError(f"Functional {type(self)} cannot be evaluated")
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        raise NotImplementedError(f"Functional {type(self)} has no prox")
+
+    def __mul__(self, other):
+        if np.isscalar(other) or (isinstance(other, np.ndarray) and other.ndim == 0):
+            return ScaledFunctional(self, float(other))
+        return NotImplemented
+
+    __rmul__ = __mul__
+
+    def __repr__(self):
+        return f"{type(self).__module__}.{type(self).__qualname__}"
+
+
+class ScaledFunctional(Functional):
+    """``scale * functional`` (scico/functional/_functional.py:131-198)."""
+
+    def __init__(self, functional: Functional, scale: float):
+        self.functional = functional
+        self.scale = float(scale)
+        self.has_eval = functional.has_eval
+        self.has_prox = functional.has_prox
+
+    def __call__(self, x) -> float:
+        return self.scale * self.functional(x)
+
+    def __mul__(self, other):
+        if np.isscalar(other):
+            return ScaledFunctional(self.functional, float(other) * self.scale)
+        return NotImplemented
+
+    __rmul__ = __mul__
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        return self.functional.prox(v, lam * self.scale, **kwargs)
+
+
+def _l2_layout(x: torch.Tensor, l2_axis) -> Tuple[torch.Tensor, int, int, tuple]:
+    """Move the l2 axes to the front; return (contiguous (ncomp, n) view, ncomp, n, perm)."""
+    nd = x.ndim
+    if l2_axis is None:
+        ax = tuple(range(nd))
+    elif isinstance(l2_axis, (int, np.integer)):
+        ax = (int(l2_axis) % nd,)
+    else:
+        ax = tuple(int(a) % nd for a in l2_axis)
+    rest = tuple(a for a in range(nd) if a not in ax)
+    perm = ax + rest
+    ncomp = int(np.prod([x.shape[a] for a in ax])) if ax else 1
+    n = int(np.prod([x.shape[a] for a in rest])) if rest else 1
+    xp = x if perm == tuple(range(nd)) else x.permute(perm)
+    return xp.contiguous().reshape(ncomp, n), ncomp, n, perm
+
+
+class L21Norm(Functional):
+    r"""The :math:`\ell_{2,1}` norm: l2 over `l2_axis`, then sum (scico/functional/_norm.py:208)."""
+
+    has_eval = True
+    has_prox = True
+
+    def __init__(self, l2_axis: Union[None, int, Tuple] = 0):
+        self.l2_axis = l2_axis
+
+    def __call__(self, x) -> float:
+        if isinstance(x, tuple):
+            if self.l2_axis is not None:
+                raise ValueError("Initializer argument 'l2_axis' must be None for BlockArray input.")
+            return float(sum(L21Norm(None)(b) for b in x))
+        t = _device.to_device(x)
+        v, ncomp, n, _ = _l2_layout(t, self.l2_axis)
+        out = _device.zeros((1,), dtype=torch.float64)
+        ws = _device.reduce_workspace()
+        _lib.call("ct_l21_norm", v.data_ptr(), ncomp, n, out.data_ptr(), ws.data_ptr(), ws.numel(),
+                  _device.stream())
+        return float(out.item())
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        if isinstance(v, tuple):
+            if self.l2_axis is not None:
+                raise ValueError("Initializer argument 'l2_axis' must be None for BlockArray input.")
+            return tuple(L21Norm(None).prox(b, lam) for b in v)
+        t = _device.to_device(v)
+        vv, ncomp, n, perm = _l2_layout(t, self.l2_axis)
+        out = torch.empty_like(vv)
+        _lib.call("ct_l21_prox", vv.data_ptr(), out.data_ptr(), ncomp, n, float(np.float32(lam)),
+                  _device.stream())
+        if perm == tuple(range(t.ndim)):
+            return out.reshape(t.shape)
+        shp = tuple(t.shape[a] for a in perm)
+        inv = tuple(np.argsort(perm))
+        return out.reshape(shp).permute(inv).contiguous()
+
+
+class L1Norm(Functional):
+    r"""The :math:`\ell_1` norm (scico/functional/_norm.py:65-117)."""
+
+    has_eval = True
+    has_prox = True
+
+    def __call__(self, x) -> float:
+        if isinstance(x, tuple):
+            return float(sum(self(b) for b in x))
+        t = _device.to_device(x).reshape(-1)
+        out = _device.zeros((1,), dtype=torch.float64)
+        ws = _device.reduce_workspace()
+        _lib.call("ct_l21_norm", t.data_ptr(), 0, t.numel(), out.data_ptr(), ws.data_ptr(), ws.numel(),
+                  _device.stream())
+        return float(out.item())
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        if isinstance(v, tuple):
+            return tuple(self.prox(b, lam) for b in v)
+        t = _device.to_device(v)
+        out = torch.empty_like(t)
+        _lib.call("ct_l1_prox", t.data_ptr(), out.data_ptr(), t.numel(), float(np.float32(lam)),
+                  _device.stream())
+        return out

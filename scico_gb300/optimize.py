@@ -1,0 +1,336 @@
+"""ADMM with LinearSubproblemSolver, mirroring scico.optimize.
+
+* :class:`ADMM` -- scico/optimize/_admm.py:34-378 with the solve loop,
+  nanstop, iteration statistics and save/load of scico/optimize/_common.py:
+  86-320.
+* :class:`LinearSubproblemSolver` -- scico/optimize/_admmaux.py:118-269.
+
+Two execution paths, same results (within float32 rounding):
+
+* generic: ``ADMM.step`` composes the operators exactly as the reference
+  does (every operator application is a ctgpu kernel launch);
+* fused: when the problem is the CT TV pattern -- ``f = SquaredL2Loss(y,
+  A=XRayTransform2D)``, every ``C_i`` a 2D ``FiniteDifference(append=0)``,
+  ``g_i`` a scaled ``L21Norm()`` and/or ``L1Norm()``, equal ``rho_i``,
+  ``LinearSubproblemSolver`` -- ``solve()`` runs ``ct_admm_tv_solve``: the
+  whole outer iteration (x-update CG with device-side stopping test, z/u
+  updates, iteration statistics) replayed as one CUDA graph.
+"""
+
+from __future__ import annotations
+
+import collections
+import math
+import time
+from typing import Any, Callable, List, Optional
+
+import numpy as np
+import torch
+
+from . import _device, _lib, linop
+from .functional import Functional, L1Norm, L21Norm, ScaledFunctional
+from .loss import SquaredL2Loss, _sqnorm
+from .solver import cg as scico_cg
+
+ITSTAT_FIELDS = ("Iter", "Time", "Objective", "Prml_Rsdl", "Dual_Rsdl", "CG_It", "CG_Res")
+IterationRecord = collections.namedtuple("IterationRecord", ITSTAT_FIELDS)
+
+
+class LinearSubproblemSolver:
+    """x-update by CG on ``(A^T W A + sum_i rho_i C_i^T C_i) x = rhs``."""
+
+    def __init__(self, cg_kwargs: Optional[dict] = None, cg_function: str = "scico", device=None):
+        default = {"tol": 1e-4, "maxiter": 100}  # _admmaux.py:189
+        if cg_kwargs:
+            default.update(cg_kwargs)
+        self.cg_kwargs = default
+        if cg_function != "scico":
+            raise ValueError(f"Argument 'cg_function' must be 'scico' here; got {cg_function}.")
+        self.cg_function = cg_function
+        self.cg = scico_cg
+        self.info = None
+        self.device = device
+
+    def internal_init(self, admm: "ADMM"):
+        if not isinstance(admm.f, SquaredL2Loss):
+            raise TypeError(f"LinearSubproblemSolver requires f to be a SquaredL2Loss; got {type(admm.f)}.")
+        if not isinstance(admm.f.A, linop.LinearOperator):
+            raise TypeError(f"LinearSubproblemSolver requires f.A to be a LinearOperator; got {type(admm.f.A)}.")
+        self.admm = admm
+        lhs = None
+        for rho, C in zip(admm.rho_list, admm.C_list):  # :222-224
+            t = rho * C.gram_op
+            lhs = t if lhs is None else lhs + t
+        self.lhs_op = lhs + admm.f.hessian  # :225-227
+
+    def compute_rhs(self):
+        """``2 scale A^T y + sum_i rho_i C_i^T (z_i - u_i)`` (:231-256)."""
+        admm = self.admm
+        C0 = admm.C_list[0]
+        rhs = _device.zeros(C0.input_shape)
+        rhs = rhs + 2.0 * admm.f.scale * admm.f.A.adj(admm.f.y)
+        for rho, C, z, u in zip(admm.rho_list, admm.C_list, admm.z_list, admm.u_list):
+            rhs = rhs + rho * C.adj(_sub(z, u))
+        return rhs
+
+    def solve(self, x0):
+        rhs = self.compute_rhs()
+        x, self.info = self.cg(self.lhs_op, rhs, x0, **self.cg_kwargs)
+        return x
+
+
+def _sub(a, b):
+    if isinstance(a, tuple):
+        return tuple(u - v for u, v in zip(a, b))
+    return a - b
+
+
+def _g_kind(g: Functional):
+    """('l21' | 'l1', weight) of a supported regulariser, else None."""
+    scale = 1.0
+    base = g
+    if isinstance(g, ScaledFunctional):
+        scale, base = g.scale, g.functional
+    if isinstance(base, L21Norm) and base.l2_axis == 0:
+        return "l21", scale
+    if isinstance(base, L1Norm):
+        return "l1", scale
+    return None
+
+
+class ADMM:
+    """Alternating direction method of multipliers (scico/optimize/_admm.py:34)."""
+
+    def __init__(self, f: Functional, g_list: List[Functional], C_list: List[linop.LinearOperator],
+                 rho_list: List[float], alpha: float = 1.0, x0=None, subproblem_solver=None, **kwargs):
+        N = len(g_list)
+        if len(C_list) != N:
+            raise ValueError(f"len(C_list)={len(C_list)} not equal to len(g_list)={N}.")
+        if len(rho_list) != N:
+            raise ValueError(f"len(rho_list)={len(rho_list)} not equal to len(g_list)={N}.")
+        self.f, self.g_list, self.C_list = f, g_list, C_list
+        self.rho_list = [float(r) for r in rho_list]
+        self.alpha = float(alpha)
+        if subproblem_solver is None:
+            raise NotImplementedError("only LinearSubproblemSolver is implemented on the device path")
+        self.subproblem_solver = subproblem_solver
+        self.subproblem_solver.internal_init(self)
+        if x0 is None:
+            x0 = _device.zeros(C_list[0].input_shape)
+        self.x = _device.to_device(x0, shape=C_list[0].input_shape, name="x0").clone()
+        self.z_list = [C(self.x) for C in C_list]  # z_init (:297-315)
+        self.z_list_old = list(self.z_list)
+        self.u_list = [_zeros_like(z) for z in self.z_list]  # u_init (:317-332)
+        # Optimizer.__init__ (_common.py:117-135)
+        self.itnum = kwargs.pop("iter0", 0)
+        self.maxiter = kwargs.pop("maxiter", 100)
+        self.nanstop = kwargs.pop("nanstop", False)
+        itstat_options = kwargs.pop("itstat_options", None) or {}
+        self.fused = kwargs.pop("fused", "auto")
+        if kwargs:
+            raise TypeError(f"Unrecognized keyword argument(s) {', '.join(kwargs)}")
+        self.itstat_display = bool(itstat_options.get("display", False))
+        self.itstat_period = int(itstat_options.get("period", 1))
+        self.iterations: List[IterationRecord] = []
+        self._fused_state = None
+        self._elapsed = 0.0
+
+    # -- reference quantities (_admm.py:210-295) ------------------------------
+    def objective(self, x=None, z_list=None) -> float:
+        if (x is None) != (z_list is None):
+            raise ValueError("Both or neither of arguments 'x' and 'z_list' must be supplied.")
+        if x is None:
+            x, z_list = self.x, self.z_list
+        out = self.f(x)
+        for g, z in zip(self.g_list, z_list):
+            out += g(z)
+        return out
+
+    def norm_primal_residual(self, x=None) -> float:
+        x = self.x if x is None else x
+        s = 0.0
+        for rho, C, z in zip(self.rho_list, self.C_list, self.z_list):
+            s += rho * _sqnorm(_flat(_sub(C(x), z)))
+        return math.sqrt(s)
+
+    def norm_dual_residual(self) -> float:
+        acc = None
+        for rho, z, zo, C in zip(self.rho_list, self.z_list, self.z_list_old, self.C_list):
+            t = rho * C.adj(_sub(z, zo))
+            acc = t if acc is None else acc + t
+        return math.sqrt(_sqnorm(acc))
+
+    def minimizer(self):
+        return self.x
+
+    # -- generic step (:334-378) ---------------------------------------------
+    def step(self):
+        self.x = self.subproblem_solver.solve(self.x)
+        self.z_list_old = list(self.z_list)
+        for i, (rho, g, C, z, u) in enumerate(zip(self.rho_list, self.g_list, self.C_list, self.z_list,
+                                                  self.u_list)):
+            Cx = C(self.x)
+            if self.alpha != 1.0:
+                Cx = _lin(self.alpha, Cx, 1.0 - self.alpha, z)
+            z = g.prox(_add(Cx, u), 1.0 / rho, v0=z)
+            u = _sub(_add(u, Cx), z)
+            self.z_list[i] = z
+            self.u_list[i] = u
+
+    def _working_vars_finite(self) -> bool:
+        for v in [self.x] + list(self.z_list) + list(self.u_list):
+            for t in (v if isinstance(v, tuple) else (v,)):
+                if not bool(torch.isfinite(t).all()):
+                    return False
+        return True
+
+    def _record(self, rec: IterationRecord):
+        self.iterations.append(rec)
+        if self.itstat_display and (rec.Iter % self.itstat_period == 0):
+            print("  ".join(f"{k}={v:.4g}" if isinstance(v, float) else f"{k}={v}" for k, v in rec._asdict().items()))
+
+    def solve(self, callback: Optional[Callable] = None):
+        """Run ``maxiter`` iterations (Optimizer.solve, _common.py:287-320)."""
+        use_fused = self.fused is True or (self.fused == "auto" and callback is None and self._fused_plan() is not None)
+        if self.fused is True and self._fused_plan() is None:
+            raise ValueError("fused=True but the problem is not the fused ADMM-TV pattern")
+        if use_fused:
+            self._solve_fused()
+        else:
+            t0 = time.perf_counter()
+            for self.itnum in range(self.itnum, self.itnum + self.maxiter):
+                self.step()
+                if self.nanstop and not self._working_vars_finite():
+                    raise ValueError(f"NaN or Inf value encountered in working variable in iteration {self.itnum}.")
+                info = self.subproblem_solver.info or {}
+                self._record(IterationRecord(self.itnum, self._elapsed + time.perf_counter() - t0,
+                                             self.objective(), self.norm_primal_residual(),
+                                             self.norm_dual_residual(), info.get("num_iter", 0),
+                                             info.get("rel_res", float("nan"))))
+                if callback:
+                    callback(self)
+            self._elapsed += time.perf_counter() - t0
+            self.itnum += 1
+        return self.minimizer()
+
+    def history(self, transpose: bool = False):
+        if transpose:
+            return IterationRecord(*[list(col) for col in zip(*self.iterations)]) if self.iterations else \
+                IterationRecord(*[[] for _ in ITSTAT_FIELDS])
+        return list(self.iterations)
+
+    # -- fused native path ------------------------------------------------------
+    def _fused_plan(self):
+        f = self.f
+        if not isinstance(f, SquaredL2Loss) or not isinstance(f.A, linop.XRayTransform2D):
+            return None
+        if not isinstance(self.subproblem_solver, LinearSubproblemSolver):
+            return None
+        if len(set(self.rho_list)) != 1 or not (1 <= len(self.g_list) <= 2):
+            return None
+        shape = f.A.input_shape
+        for C in self.C_list:
+            if not isinstance(C, linop.FiniteDifference) or C.input_shape != shape:
+                return None
+            if C.axes != (0, 1) or C.append != 0 or C.prepend is not None or C.circular:
+                return None
+        kinds = [_g_kind(g) for g in self.g_list]
+        if any(k is None for k in kinds) or len({k[0] for k in kinds}) != len(kinds):
+            return None
+        lam = {k: w for k, w in kinds}
+        if any(w == 0 for w in lam.values()):
+            return None
+        order = [0 if k == "l21" else 1 for k, _ in kinds]
+        return dict(lam21=lam.get("l21", 0.0), lam1=lam.get("l1", 0.0), order=order)
+
+    def _solve_fused(self):
+        plan = self._fused_plan()
+        A = self.f.A
+        cgk = self.subproblem_solver.cg_kwargs
+        g = A.geometry()
+        desc = _lib.AdmmTvDesc(g, int(self.maxiter), int(cgk.get("maxiter", 100)), float(cgk.get("tol", 1e-4)),
+                               float(cgk.get("atol", 0.0)), float(plan["lam21"]), float(plan["lam1"]),
+                               float(self.rho_list[0]), float(self.f.scale), float(self.alpha), 1)
+        st = self._fused_state
+        first = st is None
+        if first:
+            nbytes = _lib.c_size_t()
+            _lib.call("ct_admm_tv_workspace", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(nbytes))
+            ws = _device.workspace(nbytes.value)
+            zoff, uoff, nt = _lib.c_size_t(), _lib.c_size_t(), _lib.c_int32()
+            _lib.call("ct_admm_tv_state", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(zoff),
+                      _lib.ctypes.addressof(uoff), _lib.ctypes.addressof(nt))
+            st = self._fused_state = dict(ws=ws, zoff=zoff.value, uoff=uoff.value, nt=nt.value, y=self.f.y)
+        itstat = _device.zeros((max(1, self.maxiter), _lib.CT_ITSTAT_FIELDS), dtype=torch.float64)
+        x = self.x.contiguous()
+        t0 = time.perf_counter()
+        _lib.call("ct_admm_tv_solve", _lib.ctypes.addressof(desc), st["y"].data_ptr(), x.data_ptr(),
+                  itstat.data_ptr(), 0 if first else 1, st["ws"].data_ptr(), st["ws"].numel(), _device.stream())
+        torch.cuda.current_stream().synchronize()
+        dt = time.perf_counter() - t0
+        self.x = x
+        # expose z_list / u_list as views of the solver state (in g_list order)
+        N = int(np.prod(A.input_shape))
+        ws = st["ws"]
+        zs = ws[st["zoff"]:st["zoff"] + st["nt"] * 2 * N * 4].view(torch.float32).view(st["nt"], 2, *A.input_shape)
+        us = ws[st["uoff"]:st["uoff"] + st["nt"] * 2 * N * 4].view(torch.float32).view(st["nt"], 2, *A.input_shape)
+        self.z_list = [zs[k] for k in plan["order"]]
+        self.u_list = [us[k] for k in plan["order"]]
+        rec = itstat.cpu().numpy()
+        for k in range(self.maxiter):
+            r = rec[k]
+            self._record(IterationRecord(self.itnum + k, self._elapsed + dt * (k + 1) / self.maxiter,
+                                         float(r[_lib.CT_ITSTAT_OBJECTIVE]), float(r[_lib.CT_ITSTAT_PRIMAL]),
+                                         float(r[_lib.CT_ITSTAT_DUAL]), int(r[_lib.CT_ITSTAT_CG_ITERS]),
+                                         float(r[_lib.CT_ITSTAT_CG_RELRES])))
+        self._elapsed += dt
+        self.itnum += self.maxiter
+        if self.nanstop and not self._working_vars_finite():
+            raise ValueError("NaN or Inf value encountered in a working variable during the fused solve.")
+
+    # -- state (_common.py:222-258) --------------------------------------------
+    def save_state(self, path: str):
+        def host(v):
+            return np.stack([t.cpu().numpy() for t in v]) if isinstance(v, (list, tuple)) else v.cpu().numpy()
+
+        np.savez(path, opt_class=np.array(type(self).__name__), itnum=self.itnum, x=host(self.x),
+                 z_list=host(self.z_list), z_list_old=host(self.z_list_old), u_list=host(self.u_list),
+                 history=np.array([tuple(r) for r in self.iterations], dtype=np.float64))
+
+    def load_state(self, path: str):
+        npz = np.load(path, allow_pickle=False)
+        if str(npz["opt_class"]) != type(self).__name__:
+            raise TypeError(f"Cannot load state for {npz['opt_class']} into optimizer of type {type(self)}.")
+        self.itnum = int(npz["itnum"])
+        self.x = _device.to_device(npz["x"])
+        self.z_list = [_device.to_device(z) for z in npz["z_list"]]
+        self.z_list_old = [_device.to_device(z) for z in npz["z_list_old"]]
+        self.u_list = [_device.to_device(u) for u in npz["u_list"]]
+        self.iterations = [IterationRecord(int(r[0]), *[float(v) for v in r[1:5]], int(r[5]), float(r[6]))
+                           for r in npz["history"]]
+        self._fused_state = None
+        self.fused = False  # the fused solver state lives in its workspace; continue generically
+
+
+def _zeros_like(z):
+    if isinstance(z, tuple):
+        return tuple(torch.zeros_like(t) for t in z)
+    return torch.zeros_like(z)
+
+
+def _add(a, b):
+    if isinstance(a, tuple):
+        return tuple(u + v for u, v in zip(a, b))
+    return a + b
+
+
+def _lin(a, x, b, y):
+    if isinstance(x, tuple):
+        return tuple(a * u + b * v for u, v in zip(x, y))
+    return a * x + b * y
+
+
+def _flat(v):
+    if isinstance(v, tuple):
+        return torch.cat([t.reshape(-1) for t in v])
+    return v.reshape(-1)

@@ -1,0 +1,121 @@
+"""Seeded synthetic CT workloads (the five benchmark configurations).
+
+scico's CT examples build phantoms with xdesign (not a dependency here);
+these configurations instead use seeded random-ellipse phantoms of the
+stated sizes and value ranges.  Generation order per ellipse: centre,
+semi-axes, rotation angle, intensity, all from
+``numpy.random.default_rng(seed)``; pixel centres lie on [-1, 1]^2
+(axis 0 = y, axis 1 = x); ellipses add and the image is clipped to [0, 1].
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Optional
+
+import numpy as np
+
+
+def random_ellipses(n: int, count: int, seed: int, semi=(0.05, 0.4), rng=None) -> np.ndarray:
+    """(n, n) float32 phantom of `count` random ellipses."""
+    rng = np.random.default_rng(seed) if rng is None else rng
+    c = ((np.arange(n) + 0.5) / n * 2.0 - 1.0).astype(np.float64)
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    img = np.zeros((n, n), dtype=np.float64)
+    for _ in range(count):
+        cx, cy = rng.uniform(-0.6, 0.6, size=2)
+        a, b = rng.uniform(semi[0], semi[1], size=2)
+        th = rng.uniform(0.0, math.pi)
+        val = rng.uniform(-0.5, 1.0)
+        ct, st = math.cos(th), math.sin(th)
+        xr = (X - cx) * ct + (Y - cy) * st
+        yr = -(X - cx) * st + (Y - cy) * ct
+        img[(xr / a) ** 2 + (yr / b) ** 2 <= 1.0] += val
+    return np.clip(img, 0.0, 1.0).astype(np.float32)
+
+
+def random_ellipsoids(n: int, count: int, seed: int, semi=(0.05, 0.35)) -> np.ndarray:
+    """(n, n, n) float32 phantom of `count` randomly rotated ellipsoids."""
+    rng = np.random.default_rng(seed)
+    c = ((np.arange(n) + 0.5) / n * 2.0 - 1.0).astype(np.float32)
+    vol = np.zeros((n, n, n), dtype=np.float32)
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    P = np.stack([X.ravel(), Y.ravel(), Z.ravel()])
+    del X, Y, Z
+    for _ in range(count):
+        ctr = rng.uniform(-0.6, 0.6, size=3).astype(np.float32)
+        ax = rng.uniform(semi[0], semi[1], size=3).astype(np.float32)
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        Rm = np.array(
+            [
+                [1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)],
+            ],
+            dtype=np.float32,
+        )
+        val = np.float32(rng.uniform(-0.5, 1.0))
+        L = Rm.T @ (P - ctr[:, None])
+        inside = ((L / ax[:, None]) ** 2).sum(axis=0) <= 1.0
+        vol.reshape(-1)[inside] += val
+    return np.clip(vol, 0.0, 1.0)
+
+
+def noisy(y: np.ndarray, rel_sigma: float, seed: int) -> np.ndarray:
+    """y + N(0, (rel_sigma * max|y|)^2), float32."""
+    rng = np.random.default_rng(seed)
+    sigma = rel_sigma * float(np.max(np.abs(y)))
+    return (y + rng.normal(0.0, sigma, size=y.shape)).astype(np.float32)
+
+
+@dataclasses.dataclass
+class Slice2D:
+    """One 2D parallel-beam ADMM-TV problem."""
+
+    n: int
+    n_views: int
+    det_count: int
+    lam: float
+    rho: float
+    maxiter: int
+    cg_maxiter: int
+    cg_tol: float
+    phantom_seed: int
+    n_ellipses: int
+    noise: float
+    noise_seed: int
+
+    @property
+    def angles(self) -> np.ndarray:
+        return np.linspace(0, np.pi, self.n_views, endpoint=False)
+
+    @property
+    def interactions(self) -> int:
+        return self.n * self.n * self.n_views
+
+    def phantom(self) -> np.ndarray:
+        return random_ellipses(self.n, self.n_ellipses, self.phantom_seed)
+
+
+# C1: 256x256, 180 views, 363 bins (default det_count), lambda 0.01, rho 1, 50 it, CG <= 10
+C1 = Slice2D(256, 180, 363, 0.01, 1.0, 50, 10, 1e-4, 0, 10, 0.01, 1)
+# C2: 512x512, 360 views, 725 bins, lambda 0.005, rho 2, 100 it, CG <= 10
+C2 = Slice2D(512, 360, 725, 0.005, 2.0, 100, 10, 1e-4, 2, 20, 0.005, 3)
+
+
+def batched_configs(count: int = 64, seed: int = 3) -> List[Slice2D]:
+    """C3: `count` scans with N from {128..768}, views from {90..720}, det = ceil(sqrt2 N)+1."""
+    rng = np.random.default_rng(seed)
+    out = []
+    sizes = [128, 192, 256, 384, 512, 768]
+    views = [90, 180, 360, 720]
+    for k in range(count):
+        n = int(rng.choice(sizes))
+        v = int(rng.choice(views))
+        lam = float(rng.uniform(0.002, 0.02))
+        out.append(Slice2D(n, v, int(math.ceil(math.sqrt(2.0) * n)) + 1, lam, 1.0, 50, 10, 1e-4,
+                           1000 + k, 10, 0.01, 2000 + k))
+    return out

@@ -1,0 +1,163 @@
+"""The CPU oracle against the reference's own known-answer tests and the
+analytic properties its tests check (no GPU)."""
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import ctref
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+KAT = json.loads((GOLDEN / "reference_kat.json").read_text())
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_xray3d_scaling_kat(case):
+    """scico/test/linop/xray/test_xray_3d.py:29-60 (test_scaling)."""
+    c = KAT["xray3d_scaling"]["cases"][case]
+    x = np.zeros((4, 4, 1), dtype=np.float32)
+    x[1:3, 1:3, 0] = 1.0
+    M = ctref.xray3d_matrices_from_euler_angles(x.shape, x.shape[:2], "X", [[0.0]],
+                                                voxel_spacing=c["voxel_spacing"])
+    for dt in (np.float32, np.float64):
+        y = ctref.xray3d_project(x, M.astype(dt), x.shape[:2], dt)
+        np.testing.assert_allclose(y, np.array(c["truth"]), rtol=1e-7, atol=0)
+
+
+def test_fd_eval_kat():
+    """scico/test/linop/test_diff.py:11-31 (test_eval, append=1)."""
+    k = KAT["fd_eval_append1"]
+    x = np.array(k["x"], dtype=np.float32)
+    blocks = ctref.fd_eval(x, append=1)
+    np.testing.assert_array_equal(blocks[0], np.array(k["axis0"]))
+    np.testing.assert_array_equal(blocks[1], np.array(k["axis1"]))
+    np.testing.assert_array_equal(2.0 * blocks[0], 2.0 * np.array(k["axis0"]))
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_fd_1d_kat(case):
+    """scico/test/linop/test_diff.py:50-65 (prepend / append values)."""
+    c = KAT["fd_1d"]["cases"][case]
+    x = np.array(KAT["fd_1d"]["x"], dtype=np.float32)
+    y = ctref.fd_single(x, 0, c["prepend"], c["append"])
+    np.testing.assert_array_equal(y, np.array(c["truth"]))
+
+
+@pytest.mark.parametrize("axis", [0, 1, (0, 2)])
+def test_l21_analytic(axis):
+    """scico/test/functional/test_norm.py:9-28."""
+    x = np.ones((3, 4, 5), dtype=np.float32)
+    l2axis = (axis,) if isinstance(axis, int) else axis
+    l2shape = [x.shape[k] for k in l2axis]
+    l1shape = [x.shape[k] for k in set(range(3)) - set(l2axis)]
+    ana = np.sqrt(np.prod(l2shape)) * np.prod(l1shape)
+    np.testing.assert_allclose(ctref.l21_norm(x, l2axis), ana, rtol=1e-5)
+    l2 = np.sqrt(np.prod(l2shape))
+    np.testing.assert_allclose(ctref.l21_prox(x, 1.0, l2axis), (l2 - 1.0) / l2 * x, rtol=1e-5)
+
+
+@pytest.mark.parametrize("shape", [(16,), (16, 24), (5, 6, 7)])
+@pytest.mark.parametrize("mode", ["none", "pre0", "pre1", "app0", "app1", "both01", "circ"])
+def test_fd_adjoint_dot(shape, mode):
+    """Dot test of the FD adjoint (test_diff.py:68-78), float64."""
+    kw = dict(none={}, pre0=dict(prepend=0), pre1=dict(prepend=1), app0=dict(append=0),
+              app1=dict(append=1), both01=dict(prepend=0, append=1), circ=dict(circular=True))[mode]
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(shape)
+    for ax in range(len(shape)):
+        d = ctref.fd_single(x, ax, kw.get("prepend"), kw.get("append"), kw.get("circular", False))
+        r = rng.standard_normal(d.shape)
+        back = ctref.fd_single_adj(r, shape[ax], ax, kw.get("prepend"), kw.get("append"), kw.get("circular", False))
+        np.testing.assert_allclose(np.sum(d * r), np.sum(x * back), rtol=1e-12)
+
+
+def test_xray2d_angle0_sums_rows():
+    """Angle 0 sums image rows (_xray2d.py:66-70): exact with unit pixels."""
+    rng = np.random.default_rng(1)
+    im = rng.integers(0, 9, size=(12, 12)).astype(np.float32)
+    g = ctref.xray2d_defaults(im.shape, np.array([0.0]), dx=1.0, det_count=12)
+    y = ctref.xray2d_project(im, g, np.float32)
+    np.testing.assert_array_equal(y[0], im.sum(axis=1))
+
+
+def test_xray2d_angle90_sums_columns():
+    rng = np.random.default_rng(2)
+    im = rng.random((10, 10)).astype(np.float32)
+    g = ctref.xray2d_defaults(im.shape, np.array([np.pi / 2]), dx=1.0, det_count=10)
+    y = ctref.xray2d_project(im, g, np.float64)
+    np.testing.assert_allclose(y[0], im.sum(axis=0), rtol=1e-5, atol=1e-5)
+
+
+def test_xray2d_mass_and_adjoint():
+    """Every pixel splits w + (1-w) = 1 over two bins; matched adjoint
+    (test_xray_2d.py:52-85)."""
+    rng = np.random.default_rng(3)
+    im = rng.random((12, 13)).astype(np.float32)
+    ang = np.linspace(0, np.pi, 10, endpoint=False)
+    g = ctref.xray2d_defaults(im.shape, ang)
+    y = ctref.xray2d_project(im, g, np.float64)
+    np.testing.assert_allclose(y.sum(axis=1), np.full(10, im.astype(np.float64).sum()), rtol=1e-12)
+    yr = rng.standard_normal(y.shape)
+    bp = ctref.xray2d_back_project(yr, g, np.float64)
+    np.testing.assert_allclose(np.sum(y * yr), np.sum(im * bp), rtol=1e-12)
+    # narrow detector, N=16, det=int(16*1.05/sqrt2), dx=1/sqrt2 (:77-85)
+    g2 = ctref.xray2d_defaults((16, 16), np.linspace(0, np.pi, 3, endpoint=False), dx=1 / np.sqrt(2),
+                               det_count=int(16 * 1.05 / np.sqrt(2.0)))
+    x = rng.standard_normal((16, 16)).astype(np.float32)
+    y2 = ctref.xray2d_project(x, g2, np.float32)
+    yr2 = rng.standard_normal(y2.shape).astype(np.float32)
+    bp2 = ctref.xray2d_back_project(yr2, g2, np.float32)
+    a, b = float(np.sum(y2.astype(np.float64) * yr2)), float(np.sum(x.astype(np.float64) * bp2))
+    assert abs(a - b) / max(abs(a), abs(b)) < 1e-5
+
+
+def test_xray2d_f32_vs_f64():
+    rng = np.random.default_rng(4)
+    im = rng.random((20, 20)).astype(np.float32)
+    g = ctref.xray2d_defaults(im.shape, np.linspace(0, np.pi, 9, endpoint=False))
+    y32 = ctref.xray2d_project(im, g, np.float32)
+    y64 = ctref.xray2d_project(im, g, np.float64)
+    assert ctref.rel_l2(y32, y64) < 1e-6
+
+
+def test_xray3d_adjoint_dot():
+    """test_xray_3d.py:9-26 (matched adjoint, 3 views about 'X')."""
+    N = 16
+    det = int(N * 1.05 / np.sqrt(2.0))
+    M = ctref.xray3d_matrices_from_euler_angles((N, N, N), (det, det), "X",
+                                                np.linspace(0, np.pi, 3, endpoint=False)[:, None])
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((N, N, N))
+    y = ctref.xray3d_project(x, M, (det, det), np.float64)
+    r = rng.standard_normal(y.shape)
+    bp = ctref.xray3d_back_project(r, M, (N, N, N), np.float64)
+    np.testing.assert_allclose(np.sum(y * r), np.sum(x * bp), rtol=1e-12)
+
+
+def test_cg_spd():
+    """scico/test/test_solver.py:28-60: CG on an SPD system."""
+    rng = np.random.default_rng(6)
+    n = 64
+    A = rng.standard_normal((n, n))
+    A = A.T @ A + n * np.eye(n)
+    b = rng.standard_normal(n)
+    x, info = ctref.cg(lambda v: A @ v, b, np.zeros(n), tol=1e-12, maxiter=200)
+    assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) < 1e-6
+    assert info["num_iter"] <= 200
+
+
+def test_admm_tv_oracle_decreases():
+    from scico_gb300 import workloads
+
+    x_gt = workloads.random_ellipses(24, 3, 5)
+    ang = np.linspace(0, np.pi, 20, endpoint=False)
+    g = ctref.xray2d_defaults(x_gt.shape, ang)
+    y = ctref.xray2d_project(x_gt, g, np.float64)
+    fwd = lambda v: ctref.xray2d_project(v, g, np.float64)
+    adj = lambda v: ctref.xray2d_back_project(v, g, np.float64)
+    x, hist, _, _ = ctref.admm_tv(fwd, adj, y, x_gt.shape, lam_l21=0.01, rho=1.0, maxiter=8, dtype=np.float64)
+    obj = [h["Objective"] for h in hist]
+    assert obj[-1] < obj[0]
+    assert ctref.snr(x_gt, x) > 10
