@@ -197,9 +197,11 @@ ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap,
                        int64_t n, double* scalars, void* workspace,
                        size_t workspace_bytes, ct_stream_t stream);
 
-/* p = r + beta p (skipped once DONE was set before the preceding update). */
+/* p = r + beta p (skipped once DONE was set before the preceding update).
+ * Uses the reduction workspace of the preceding ct_cg_update. */
 ct_status ct_cg_direction(float* p, const float* r, int64_t n,
-                          double* scalars, ct_stream_t stream);
+                          double* scalars, void* workspace,
+                          size_t workspace_bytes, ct_stream_t stream);
 
 /* CG start: r = b - Ax; p = r; NUM = <r,r>; BNORM = ||b||;
  * TOL2 = max(tol BNORM, atol)^2; ITERS = 0; DONE = (NUM <= TOL2) || maxiter==0. */

@@ -135,7 +135,7 @@ _SIGNATURES = {
     "ct_dot": (ctypes.c_int, [P, P, c_int64, P, P, c_size_t, P]),
     "ct_cg_init": (ctypes.c_int, [P, P, P, P, c_int64, c_double, c_double, c_int32, P, P, c_size_t, P]),
     "ct_cg_update": (ctypes.c_int, [P, P, P, P, c_int64, P, P, c_size_t, P]),
-    "ct_cg_direction": (ctypes.c_int, [P, P, c_int64, P, P]),
+    "ct_cg_direction": (ctypes.c_int, [P, P, c_int64, P, P, c_size_t, P]),
     "ct_admm_tv_workspace": (ctypes.c_int, [P, P]),
     "ct_admm_tv_state": (ctypes.c_int, [P, P, P, P]),
     "ct_admm_tv_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),

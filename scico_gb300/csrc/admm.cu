@@ -430,7 +430,7 @@ ct_status enqueue_iteration(const Ctx& c, cudaStream_t s) {
                                           c.cg(), 0.0, 0.0, K, c.partials(), c.ticket());
     CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
     CT_TRY(ct::cg_update_launch(c.x, r, p, ap, c.L.N, c.cg(), c.ws + c.L.off_red, s));
-    CT_TRY(ct::cg_direction_launch(p, r, c.L.N, c.cg(), s));
+    CT_TRY(ct::cg_direction_launch(p, r, c.L.N, c.cg(), c.ws + c.L.off_red, s));
   }
   k_zu<<<NB, NT, 0, s>>>(c.x, z, u, dz, R, C, c.tp, c.slots(), c.partials(), c.ticket());
   return ct::launch_check("k_zu");

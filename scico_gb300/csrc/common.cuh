@@ -55,49 +55,65 @@ __device__ __forceinline__ void boxcar2d(float px, float width, float inv_width,
 }
 
 // ---------------------------------------------------------------------------
-// Deterministic float64 reduction: every block writes one partial to
-// `partials[blockIdx.x]`; the last block to finish (integer ticket, so the
-// choice of block does not affect the value) sums the partials in index
-// order.  The ticket is reset by that block, so the sequence can be replayed
-// (e.g. inside a CUDA graph) without host involvement.
+// Deterministic float64 grid reduction of K simultaneous sums.  Every block
+// reduces its threads' values (fixed shuffle tree, warps in order) and
+// writes K partials to partials[K*blockIdx.x + k]; the last block to finish
+// (integer ticket, so which block it is does not affect the value) sums the
+// partials with all its threads in a fixed pattern.  The ticket is reset by
+// that block, so the sequence can be replayed (e.g. inside a CUDA graph)
+// without host involvement.  Returns true in thread 0 of the last block,
+// with `out` holding the K totals.
 // ---------------------------------------------------------------------------
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* red /*[NT/32]*/) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+template <int NT, int K>
+__device__ __forceinline__ void block_reduce(double (&v)[K], double (*red)[NT / 32]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < NT / 32; ++k) s += red[k];
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k][warp] = v[k];
   }
-  return s;  // valid in thread 0 only
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < NT / 32; ++w) s += red[k][w];
+      v[k] = s;
+    }
+  }
+  __syncthreads();
 }
 
-// Returns true in thread 0 of the last block; `total` then holds the sum.
-template <int NT>
-__device__ __forceinline__ bool grid_sum_last(double block_total, double* partials,
-                                              unsigned int* ticket, double& total) {
+template <int NT, int K>
+__device__ __forceinline__ bool grid_reduce_last(double (&v)[K], double* partials, unsigned int* ticket,
+                                                 double (&out)[K]) {
+  __shared__ double red[K][NT / 32];
   __shared__ bool is_last;
+  block_reduce<NT, K>(v, red);
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = block_total;
+#pragma unroll
+    for (int k = 0; k < K; ++k) partials[(size_t)K * blockIdx.x + k] = v[k];
     __threadfence();
-    const unsigned int t = atomicAdd(ticket, 1u);
-    is_last = (t == gridDim.x - 1);
+    is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
   }
   __syncthreads();
   if (!is_last) return false;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    double s = 0.0;
-    volatile double* vp = partials;
-    for (unsigned int b = 0; b < gridDim.x; ++b) s += vp[b];
-    total = s;
-    *ticket = 0u;
-    return true;
+  __threadfence();
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (unsigned int b = threadIdx.x; b < gridDim.x; b += NT) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] += __ldcg(partials + (size_t)K * b + k);
   }
-  return false;
+  block_reduce<NT, K>(acc, red);
+  if (threadIdx.x != 0) return false;
+#pragma unroll
+  for (int k = 0; k < K; ++k) out[k] = acc[k];
+  *ticket = 0u;
+  return true;
 }
 
 // Fixed grid size for reductions (independent of the device, so results are

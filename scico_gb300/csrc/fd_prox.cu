@@ -201,7 +201,6 @@ __global__ void k_l1_prox(const float* __restrict__ v, float* __restrict__ out, 
 __global__ void __launch_bounds__(ct::kReduceThreads)
     k_l21_norm(const float* __restrict__ v, int ncomp, size_t n, double* __restrict__ out,
                double* __restrict__ partials, unsigned int* __restrict__ ticket) {
-  __shared__ double red[ct::kReduceThreads / 32];
   double acc = 0.0;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -217,9 +216,8 @@ __global__ void __launch_bounds__(ct::kReduceThreads)
       acc += (double)__fsqrt_rn(ss);
     }
   }
-  const double bs = ct::block_sum<ct::kReduceThreads>(acc, red);
-  double total;
-  if (ct::grid_sum_last<ct::kReduceThreads>(bs, partials, ticket, total)) *out = total;
+  double part[1] = {acc}, tot[1];
+  if (ct::grid_reduce_last<ct::kReduceThreads, 1>(part, partials, ticket, tot)) *out = tot[0];
 }
 
 }  // namespace

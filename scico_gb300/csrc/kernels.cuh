@@ -7,10 +7,13 @@ namespace ct {
 
 // ---- 2D projector (proj2d.cu) ---------------------------------------------
 struct Proj2dPlan {
-  int tiles_i, tiles_j, n_tiles, L, LS, view_groups;
+  // forward: 32-row x 256-column strips, views per CTA, bins per tile / strip
+  int tiles_i, n_chunks, n_strips, L, LS, cspan, vpc, fwd_groups;
   size_t fwd_bytes, fwd_smem;
-  int adj_gx, adj_gy, nsplit, per_split;
+  // adjoint: 16x64 tiles, view splits, staged window length
+  int adj_gx, adj_gy, nsplit, per_split, W;
   size_t adj_bytes;  // split partial images (0 when nsplit == 1)
+  size_t adj_smem;
 };
 
 ct_status proj2d_check(const ct_geom2d* g, const char* who);
@@ -32,48 +35,14 @@ ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
 // ---- CG vector steps (vec.cu) ----------------------------------------------
 ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, size_t n,
                            double* scalars, void* red_ws, cudaStream_t s);
-ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, cudaStream_t s);
+ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, void* red_ws,
+                              cudaStream_t s);
 
-// ---- generic N-way float64 grid sum ------------------------------------------
-// All threads call with their K partial values; returns true in thread 0 of
-// the last block to finish, with `out` holding the K grid totals (block
-// partials summed in block order).
+// ---- generic N-way float64 grid sum (see grid_reduce_last in common.cuh) ----
 template <int NT, int K>
-__device__ __forceinline__ bool grid_sumk_last(double (&v)[K], double* partials,
-                                               unsigned int* ticket, double (&out)[K]) {
-  __shared__ double red[K][NT / 32];
-  __shared__ bool is_last;
-#pragma unroll
-  for (int k = 0; k < K; ++k)
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) red[k][warp] = v[k];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double s = 0.0;
-      for (int w = 0; w < NT / 32; ++w) s += red[k][w];
-      partials[(size_t)K * blockIdx.x + k] = s;
-    }
-    __threadfence();
-    is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!is_last || threadIdx.x != 0) return false;
-  __threadfence();
-  volatile double* vp = partials;
-#pragma unroll
-  for (int k = 0; k < K; ++k) out[k] = 0.0;
-  for (unsigned int b = 0; b < gridDim.x; ++b) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) out[k] += vp[(size_t)K * b + k];
-  }
-  *ticket = 0u;
-  return true;
+__device__ __forceinline__ bool grid_sumk_last(double (&v)[K], double* partials, unsigned int* ticket,
+                                               double (&out)[K]) {
+  return grid_reduce_last<NT, K>(v, partials, ticket, out);
 }
 
 }  // namespace ct

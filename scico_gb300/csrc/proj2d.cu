@@ -5,31 +5,51 @@
 // w = min(1 - (Px - k), width)/width it adds w*x to bin k and (1-w)*x to bin
 // k+1 (bins outside [0, det) dropped).
 //
-// Forward (A):  tile-owned pixel-driven sweep.  A CTA owns a 32x32 image
-//   tile and a run of views; lane r of a warp holds tile row r in registers
-//   and walks its 32 pixels in the direction in which k is non-decreasing,
-//   carrying the running sums of the current bin and the next one in
-//   registers.  Each row's bin sums go to the warp's shared-memory partial
-//   rows, which are then summed over the 32 rows in a fixed order.  The
-//   per-(tile, view) partial bins are written to the workspace and a second
-//   kernel sums the tiles covering each bin in tile order.  No atomics; the
-//   result is bit-reproducible.
-// Adjoint (A^T): pixel-driven gather over all views with the same weights,
-//   views summed in a fixed order (optionally in fixed view splits reduced
-//   by a second kernel), no atomics.
+// Forward (A), tile-owned pixel-driven sweep, two kernels:
+//   k_proj2d_fwd_strips  A CTA owns a strip of 32 image rows x 256 columns,
+//     copied once into padded shared memory with bulk (TMA) copies, and a run
+//     of views.  For each view the 8 warps take the strip's 8 32x32 tiles;
+//     lane r holds tile row r in registers and walks its 32 pixels in the
+//     direction in which k never decreases, carrying the running sums of the
+//     current bin and the next in registers and storing finished bins in its
+//     shared-memory partial row.  The 32 partial rows are summed in row
+//     order, the 8 tiles in tile order, giving the strip's bins for the view.
+//   k_proj2d_fwd_gather  sums, per detector bin, the strips that cover it in
+//     strip order.
+//   No atomics: the result is bit-reproducible.
+// Adjoint (A^T), k_proj2d_adj: pixel-driven gather with the same weights.  A
+//   CTA owns a 16x64 pixel tile; per run of 32 views it stages the tile's
+//   detector windows in shared memory as (y[k], y[k+1]) pairs (zero outside
+//   the detector), then each thread accumulates its 4 pixels over the views
+//   in view order.  Small images split the views into a fixed number of
+//   runs whose partial images are summed in run order.
+//
+// floor(Px) is taken with one round-down float add of 1.5*2^23 (exact for
+// |Px| < 2^22, checked per tile and view, with a floorf path otherwise):
+// full-rate FP32 operations instead of conversion instructions.
 #include <algorithm>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace {
 
-constexpr int kTile = 32;       // forward tile edge (rows = lanes, cols = registers)
-constexpr int kFwdWarps = 8;    // views processed concurrently by one forward CTA
-constexpr int kFwdViewsPerCta = 24;
-constexpr int kAdjRows = 8;     // adjoint CTA: 8 rows x (32*kAdjPx) cols
-constexpr int kAdjPx = 2;
+constexpr int kT = 32;          // forward tile edge: rows = lanes, columns = registers
+constexpr int kCW = 256;        // forward strip width (8 tiles)
+constexpr int kFW = 8;          // warps of a forward CTA (one tile each)
+constexpr int kRS = kCW + 4;    // strip row stride in floats: 16-B rows, conflict-free LDS.128
+constexpr int kFwdTargetCtas = 1824;
+constexpr int kAI = 16;         // adjoint tile rows
+constexpr int kAJ = 64;         // adjoint tile columns
+constexpr int kAPX = 4;         // pixels per adjoint thread
+constexpr int kAVC = 32;        // views staged per adjoint run
 constexpr int kAdjTargetCtas = 304;
 constexpr int kAdjMinViewsPerSplit = 16;
+constexpr uint32_t kMaxPolls = 1u << 24;
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+constexpr float kFastLimit = 2097152.0f;  // 2^21
 
 struct ViewParams {
   float pxmin, pd0, pd1, width, inv_width;
@@ -41,209 +61,353 @@ __device__ __forceinline__ ViewParams load_view(const float* __restrict__ views,
   return ViewParams{a.x, a.y, a.z, a.w, b.x};
 }
 
-// Bin range [base, top] of the pixel keys of the 32x32 tile at (i0, j0).
-// Px is monotone in i and in j separately (every operation of px2d is a
-// monotone rounding), so the extremes are at the tile corners.
-__device__ __forceinline__ void tile_keys(const ViewParams& p, int i0, int j0, int& base, int& top) {
+// Extreme Px over the pixel rectangle [i0, i1] x [j0, j1]: px2d is monotone
+// in i and in j separately (each operation is a monotone rounding), so the
+// extremes are at the corners.
+__device__ __forceinline__ void rect_px(const ViewParams& p, int i0, int i1, int j0, int j1, float& lo,
+                                        float& hi) {
   const float a = ct::px2d(p.pxmin, p.pd0, p.pd1, i0, j0);
-  const float b = ct::px2d(p.pxmin, p.pd0, p.pd1, i0 + kTile - 1, j0);
-  const float c = ct::px2d(p.pxmin, p.pd0, p.pd1, i0, j0 + kTile - 1);
-  const float d = ct::px2d(p.pxmin, p.pd0, p.pd1, i0 + kTile - 1, j0 + kTile - 1);
-  base = (int)floorf(fminf(fminf(a, b), fminf(c, d)));
-  top = (int)floorf(fmaxf(fmaxf(a, b), fmaxf(c, d)));
+  const float b = ct::px2d(p.pxmin, p.pd0, p.pd1, i1, j0);
+  const float c = ct::px2d(p.pxmin, p.pd0, p.pd1, i0, j1);
+  const float d = ct::px2d(p.pxmin, p.pd0, p.pd1, i1, j1);
+  lo = fminf(fminf(a, b), fminf(c, d));
+  hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
 }
+
+// key = floor(px) - kbias and w = min(1 - (px - floor(px)), width) * inv_width.
+template <bool FAST>
+__device__ __forceinline__ void weight(float px, float width, float inv_width, int kbias, int& key,
+                                       float& w) {
+  float fl;
+  if (FAST) {
+    const float t = __fadd_rd(px, kMagic);  // kMagic + floor(px), exactly
+    key = __float_as_int(t) - (kMagicBits + kbias);
+    fl = ct::fsub(t, kMagic);
+  } else {
+    fl = floorf(px);
+    key = (int)fl - kbias;
+  }
+  const float dist = ct::fsub(1.0f, ct::fsub(px, fl));
+  w = ct::fmul(fminf(dist, width), inv_width);
+}
+
+// ---------------------------------------------------------------------------
+// Forward
+// ---------------------------------------------------------------------------
 
 // Walk one tile row for one view.  REV walks j downwards (Pdx1 < 0) so that
 // the bin key never decreases.  mp: this lane's partial row, indexed by
-// key - base.  Bin b receives, in j order, the (1-w) x of the pixels with
+// key - base.  Bin b receives, in walk order, the (1-w) x of the pixels with
 // key b-1 followed by the w x of the pixels with key b.
-template <bool REV>
-__device__ __forceinline__ void walk_row(const float (&xr)[kTile], float* __restrict__ mp,
-                                         const ViewParams& p, float R, int j0, int base) {
+template <bool REV, bool FAST>
+__device__ __forceinline__ void walk_row(const float (&xr)[kT], float* __restrict__ mp, const ViewParams& p,
+                                         float R, float fj0, int base) {
   int cur = 0;
   float A = 0.0f, B = 0.0f;
 #pragma unroll
-  for (int t = 0; t < kTile; ++t) {
-    const int jj = REV ? kTile - 1 - t : t;
-    const float px = ct::fadd(R, ct::fmul(p.pd1, (float)(j0 + jj)));
+  for (int t = 0; t < kT; ++t) {
+    const int jj = REV ? kT - 1 - t : t;
+    const float px = ct::fadd(R, ct::fmul(p.pd1, fj0 + (float)jj));
     int key;
     float w;
-    ct::boxcar2d(px, p.width, p.inv_width, key, w);
+    weight<FAST>(px, p.width, p.inv_width, base, key, w);
     const float omw = ct::fsub(1.0f, w);
     if (t == 0) cur = key;
     const int d = key - cur;
-    if (d >= 2) mp[cur + 1 - base] = B;  // bin cur+1 complete, bins between stay 0
+    if (d >= 2) mp[cur + 1] = B;  // bin cur+1 complete; bins between stay 0
     const float a0 = d == 0 ? A : (d == 1 ? B : 0.0f);
     const float b0 = d == 0 ? B : 0.0f;
     A = fmaf(w, xr[jj], a0);
     B = fmaf(omw, xr[jj], b0);
     cur = key;
-    mp[cur - base] = A;
+    mp[cur] = A;
   }
-  mp[cur + 1 - base] = B;
+  mp[cur + 1] = B;
 }
 
-// Forward pass 1.  grid = (n_tiles, view groups, batch), block = 256.
-// part layout: [batch][tile][view][L].
-__global__ void __launch_bounds__(kFwdWarps * 32)
-    k_proj2d_fwd_tiles(const float* __restrict__ img, float* __restrict__ part,
-                       const float* __restrict__ views, int rows, int cols, int nv, int L,
-                       int LS, int tiles_j, int n_tiles, int* __restrict__ errflag,
-                       const double* __restrict__ skip) {
-  if (skip && *skip != 0.0) return;
-  extern __shared__ float smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int tile = blockIdx.x;
-  const int ti = tile / tiles_j, tj = tile - ti * tiles_j;
-  const int b = blockIdx.z;
-  const int i0 = ti * kTile, j0 = tj * kTile;
-  const int i = i0 + lane;
+struct FwdArgs {
+  const float* img;
+  float* part;          // [batch][strip][view][cspan]
+  const float* views;
+  int rows, cols, nv;
+  int L, LS, cspan;
+  int n_chunks, vpc;
+  int bulk;             // 1 = strip rows by cp.async.bulk
+  int* errflag;
+  const double* skip;
+};
 
-  float xr[kTile];
-  {
-    const float* im = img + (size_t)b * rows * cols;
-    if (i < rows) {
-      const float* rp = im + (size_t)i * cols + j0;
-      const bool vec = ((cols & 3) == 0) && (j0 + kTile <= cols) && ct::aligned(rp, 16);
-      if (vec) {
+// grid = (n_strips, view groups, batch), block = 256.
+__global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a) {
+  if (a.skip && *a.skip != 0.0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* strip = reinterpret_cast<float*>(smem_raw);                 // [32][kRS]
+  float* part = strip + kT * kRS;                                    // [kFW][32][LS]
+  float* slot = part + kFW * kT * a.LS;                              // [kFW][L]
+  int* sbase = reinterpret_cast<int*>(slot + kFW * a.L);             // [kFW]
+  int* sspan = sbase + kFW;                                          // [kFW]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sspan + kFW + 0) + 0;  // 8-B aligned below
+  bar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(bar) + 7) & ~uintptr_t(7));
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int s = blockIdx.x;
+  const int ti = s / a.n_chunks, ch = s - ti * a.n_chunks;
+  const int i0 = ti * kT, c0 = ch * kCW;
+  const int b = blockIdx.z;
+  const float* im = a.img + (size_t)b * a.rows * a.cols;
+
+  // ---- stage the 32 x 256 strip (zero outside the image) -------------------
+  const int vrows = min(kT, a.rows - i0);
+  const int vcols = min(kCW, a.cols - c0);
+  if (a.bulk) {
+    if (tid == 0) {
+      ct::mbar_init(bar, 1);
+      ct::fence_barrier_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const uint32_t row_bytes = (uint32_t)vcols * 4u;
+      ct::mbar_arrive_expect_tx(bar, row_bytes * (uint32_t)vrows);
+      for (int r = 0; r < vrows; ++r)
+        ct::bulk_g2s(strip + r * kRS, im + (size_t)(i0 + r) * a.cols + c0, row_bytes, bar);
+    }
+    // zero what the copies do not cover (disjoint addresses)
+    for (int e = tid; e < kT * kRS; e += kFW * 32) {
+      const int r = e / kRS, c = e - r * kRS;
+      if (r >= vrows || c >= vcols) strip[e] = 0.0f;
+    }
+    if (!ct::mbar_wait_bounded(bar, 0, kMaxPolls)) {
+      if (tid == 0) atomicOr(a.errflag, 2);
+      ct::mbar_wait_bounded(bar, 0, kMaxPolls);
+    }
+  } else {
+    for (int e = tid; e < kT * kRS; e += kFW * 32) {
+      const int r = e / kRS, c = e - r * kRS;
+      strip[e] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
+    }
+  }
+  // zero every partial row once; after each tile the reduction re-zeroes
+  // exactly what the walk wrote, so rows stay zero outside a tile's bins
+  for (int e = tid; e < kFW * kT * a.LS; e += kFW * 32) part[e] = 0.0f;
+  __syncthreads();
+
+  const int tj = ch * (kCW / kT) + warp;  // this warp's tile column
+  const int j0 = tj * kT;
+  const bool tile_live = (j0 < a.cols) && (i0 < a.rows);
+  float* wpart = part + warp * kT * a.LS;
+  float* mp = wpart + lane * a.LS;
+  const float fi = (float)(i0 + lane);
+  const float fj0 = (float)j0;
+  const int vbeg = blockIdx.y * a.vpc;
+  const int vend = min(a.nv, vbeg + a.vpc);
+
+  for (int v = vbeg; v < vend; ++v) {
+    const ViewParams p = load_view(a.views, v);
+    // ---- this warp's tile --------------------------------------------------
+    int base = 0, span = 0;
+    if (tile_live) {
+      float lo, hi;
+      rect_px(p, i0, i0 + kT - 1, j0, j0 + kT - 1, lo, hi);
+      base = (int)floorf(lo);
+      span = (int)floorf(hi) - base + 2;
+      const bool fast = fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit;
+      if (span > a.L) {  // cannot happen for a table from ct_proj2d_views
+        if (lane == 0) atomicOr(a.errflag, 1);
+        span = 0;
+      } else {
+        float xr[kT];
+        const float* row = strip + lane * kRS + warp * kT;
 #pragma unroll
-        for (int q = 0; q < kTile / 4; ++q) {
-          const float4 f = __ldg(reinterpret_cast<const float4*>(rp) + q);
+        for (int q = 0; q < kT / 4; ++q) {
+          const float4 f = *reinterpret_cast<const float4*>(row + 4 * q);
           xr[4 * q] = f.x;
           xr[4 * q + 1] = f.y;
           xr[4 * q + 2] = f.z;
           xr[4 * q + 3] = f.w;
         }
-      } else {
-#pragma unroll
-        for (int jj = 0; jj < kTile; ++jj) xr[jj] = (j0 + jj < cols) ? __ldg(rp + jj) : 0.0f;
-      }
-    } else {
-#pragma unroll
-      for (int jj = 0; jj < kTile; ++jj) xr[jj] = 0.0f;
-    }
-  }
-
-  float* wpart = smem + (size_t)warp * kTile * LS;
-  float* mp = wpart + (size_t)lane * LS;
-  const int vbeg = blockIdx.y * kFwdViewsPerCta;
-  const int vend = min(nv, vbeg + kFwdViewsPerCta);
-  for (int v = vbeg + warp; v < vend; v += kFwdWarps) {
-    const ViewParams p = load_view(views, v);
-    int base, top;
-    tile_keys(p, i0, j0, base, top);
-    float* po = part + (((size_t)b * n_tiles + tile) * nv + v) * L;
-    if (top - base + 2 > L) {  // cannot happen for a table from ct_proj2d_views
-      if (lane == 0) atomicOr(errflag, 1);
-      for (int k = lane; k < L; k += 32) po[k] = 0.0f;
-      continue;
-    }
-    for (int k = 0; k < L; ++k) mp[k] = 0.0f;
-    const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, (float)i));
-    if (p.pd1 >= 0.0f)
-      walk_row<false>(xr, mp, p, R, j0, base);
-    else
-      walk_row<true>(xr, mp, p, R, j0, base);
-    __syncwarp();
-    for (int k = lane; k < L; k += 32) {
-      float s = 0.0f;
-      const float* q = wpart + k;
+        const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, fi));
+        if (fast) {
+          if (p.pd1 >= 0.0f)
+            walk_row<false, true>(xr, mp, p, R, fj0, base);
+          else
+            walk_row<true, true>(xr, mp, p, R, fj0, base);
+        } else {
+          if (p.pd1 >= 0.0f)
+            walk_row<false, false>(xr, mp, p, R, fj0, base);
+          else
+            walk_row<true, false>(xr, mp, p, R, fj0, base);
+        }
+        __syncwarp();
+        // rows summed in row order; the read entries are zeroed again
+        for (int k = lane; k < span; k += 32) {
+          float acc = 0.0f;
+          float* q = wpart + k;
 #pragma unroll 8
-      for (int r = 0; r < kTile; ++r) s += q[(size_t)r * LS];
-      po[k] = s;
+          for (int r = 0; r < kT; ++r) {
+            acc += q[r * a.LS];
+            q[r * a.LS] = 0.0f;
+          }
+          slot[warp * a.L + k] = acc;
+        }
+      }
     }
-    __syncwarp();
+    if (lane == 0) {
+      sbase[warp] = base;
+      sspan[warp] = span;
+    }
+    __syncthreads();
+    // ---- combine the 8 tiles in tile order into the strip's bins ----------
+    float lo, hi;
+    rect_px(p, i0, i0 + kT - 1, c0, c0 + kCW - 1, lo, hi);
+    const int cb = (int)floorf(lo);
+    float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + v) * a.cspan;
+    for (int k = tid; k < a.cspan; k += kFW * 32) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int w = 0; w < kFW; ++w) {
+        const int off = cb + k - sbase[w];
+        if ((unsigned)off < (unsigned)sspan[w]) acc += slot[w * a.L + off];
+      }
+      po[k] = acc;
+    }
+    __syncthreads();
   }
 }
 
-// Forward pass 2: sino[b, v, bin] = sum over tiles (in tile order) of the
-// tile partials covering bin.  grid = (n_views, batch), block = 256,
-// dynamic smem = n_tiles ints.
+// sino[b, v, bin] = sum over strips (strip order) of the strip bins covering
+// bin.  grid = (n_views, batch), block = 256, dynamic smem = n_strips ints.
 __global__ void __launch_bounds__(256)
     k_proj2d_fwd_gather(const float* __restrict__ part, float* __restrict__ sino,
-                        const float* __restrict__ views, int nv, int det, int L, int tiles_j,
-                        int n_tiles, const double* __restrict__ skip) {
+                        const float* __restrict__ views, int nv, int det, int cspan, int n_chunks,
+                        int n_strips, const double* __restrict__ skip) {
   if (skip && *skip != 0.0) return;
-  extern __shared__ int sbase[];
+  extern __shared__ int sb[];
   const int v = blockIdx.x, b = blockIdx.y;
   const ViewParams p = load_view(views, v);
-  for (int t = threadIdx.x; t < n_tiles; t += blockDim.x) {
-    const int ti = t / tiles_j, tj = t - ti * tiles_j;
-    int base, top;
-    tile_keys(p, ti * kTile, tj * kTile, base, top);
-    sbase[t] = base;
+  for (int s = threadIdx.x; s < n_strips; s += blockDim.x) {
+    const int ti = s / n_chunks, ch = s - ti * n_chunks;
+    float lo, hi;
+    rect_px(p, ti * kT, ti * kT + kT - 1, ch * kCW, ch * kCW + kCW - 1, lo, hi);
+    sb[s] = (int)floorf(lo);
   }
   __syncthreads();
-  const float* pb = part + ((size_t)b * n_tiles * nv + v) * L;
-  const size_t tstride = (size_t)nv * L;
+  const float* pb = part + ((size_t)b * n_strips * nv + v) * cspan;
+  const size_t sstride = (size_t)nv * cspan;
   float* out = sino + ((size_t)b * nv + v) * det;
   for (int bin = threadIdx.x; bin < det; bin += blockDim.x) {
     float acc = 0.0f;
-    for (int t = 0; t < n_tiles; ++t) {
-      const int off = bin - sbase[t];
-      if ((unsigned)off < (unsigned)L) acc += __ldg(pb + t * tstride + off);
+    for (int s = 0; s < n_strips; ++s) {
+      const int off = bin - sb[s];
+      if ((unsigned)off < (unsigned)cspan) acc += __ldg(pb + s * sstride + off);
     }
     out[bin] = acc;
   }
 }
 
-// Adjoint.  grid = (ceil(cols/64), ceil(rows/8), batch*nsplit),
-// block = (32, 8).  With nsplit > 1, split s sums views
-// [s*per, (s+1)*per) into out + s*split_stride.
-__global__ void __launch_bounds__(256)
-    k_proj2d_adj(const float* __restrict__ sino, float* __restrict__ out,
-                 const float* __restrict__ views, int rows, int cols, int nv, int det,
-                 int nsplit, int per_split, size_t split_stride, const double* __restrict__ skip) {
-  if (skip && *skip != 0.0) return;
-  __shared__ float4 sv[256];
-  __shared__ float sinv[256];
-  const int z = blockIdx.z;
-  const int b = z / nsplit, s = z - b * nsplit;
-  const int vbeg = s * per_split, vend = min(nv, vbeg + per_split);
-  const int i = blockIdx.y * kAdjRows + threadIdx.y;
-  const int jb = blockIdx.x * 32 * kAdjPx + threadIdx.x;
-  const int tid = threadIdx.y * 32 + threadIdx.x;
-  const float* yb = sino + (size_t)b * nv * det;
-  float acc[kAdjPx];
-#pragma unroll
-  for (int q = 0; q < kAdjPx; ++q) acc[q] = 0.0f;
-  const float fi = (float)i;
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
 
-  for (int a0 = vbeg; a0 < vend; a0 += 256) {
-    const int n = min(256, vend - a0);
+struct AdjArgs {
+  const float* sino;
+  float* out;
+  const float* views;
+  int rows, cols, nv, det;
+  int nsplit, per_split;
+  size_t split_stride;
+  int W;  // window length (bins) per staged view
+  int* errflag;
+  const double* skip;
+};
+
+template <bool FAST>
+__device__ __forceinline__ void adj_view(const float4 pv, float width, int base, const float2* __restrict__ wy,
+                                         float fi, const float (&fj)[kAPX], float (&acc)[kAPX]) {
+  const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
+#pragma unroll
+  for (int q = 0; q < kAPX; ++q) {
+    const float px = ct::fadd(R, ct::fmul(pv.z, fj[q]));
+    int key;
+    float w;
+    weight<FAST>(px, width, pv.w, base, key, w);
+    const float2 y = wy[key];
+    acc[q] = fmaf(y.x, w, acc[q]);
+    acc[q] = fmaf(y.y, ct::fsub(1.0f, w), acc[q]);
+  }
+}
+
+// grid = (ceil(cols/64), ceil(rows/16), batch*nsplit), block = 256.
+__global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
+  if (a.skip && *a.skip != 0.0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* sy = reinterpret_cast<float2*>(smem_raw);          // [kAVC][W]
+  float4* sp = reinterpret_cast<float4*>(sy + kAVC * a.W);   // [kAVC] pxmin, pd0, pd1, 1/width
+  float* sw = reinterpret_cast<float*>(sp + kAVC);           // [kAVC] width
+  int* sb = reinterpret_cast<int*>(sw + kAVC);               // [kAVC] window base
+  int* sf = sb + kAVC;                                       // [kAVC] 1 = fast floor, -1 = skip
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int z = blockIdx.z;
+  const int b = z / a.nsplit, sidx = z - b * a.nsplit;
+  const int vbeg = sidx * a.per_split, vend = min(a.nv, vbeg + a.per_split);
+  const int i0 = blockIdx.y * kAI, j0 = blockIdx.x * kAJ;
+  const int ty = tid >> 4, tx = tid & 15;
+  const int i = i0 + ty;
+  const float fi = (float)i;
+  float fj[kAPX];
+#pragma unroll
+  for (int q = 0; q < kAPX; ++q) fj[q] = (float)(j0 + tx + 16 * q);
+  float acc[kAPX];
+#pragma unroll
+  for (int q = 0; q < kAPX; ++q) acc[q] = 0.0f;
+  const float* yb = a.sino + (size_t)b * a.nv * a.det;
+
+  for (int a0 = vbeg; a0 < vend; a0 += kAVC) {
+    const int n = min(kAVC, vend - a0);
     __syncthreads();
     if (tid < n) {
-      const ViewParams p = load_view(views, a0 + tid);
-      sv[tid] = make_float4(p.pxmin, p.pd0, p.pd1, p.width);
-      sinv[tid] = p.inv_width;
+      const ViewParams p = load_view(a.views, a0 + tid);
+      float lo, hi;
+      rect_px(p, i0, i0 + kAI - 1, j0, j0 + kAJ - 1, lo, hi);
+      const int base = (int)floorf(lo);
+      const int span = (int)floorf(hi) - base + 2;
+      sp[tid] = make_float4(p.pxmin, p.pd0, p.pd1, p.inv_width);
+      sw[tid] = p.width;
+      sb[tid] = base;
+      int f = fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit ? 1 : 0;
+      if (span > a.W) {  // cannot happen for a table from ct_proj2d_views
+        atomicOr(a.errflag, 4);
+        f = -1;
+      }
+      sf[tid] = f;
     }
     __syncthreads();
-    for (int k = 0; k < n; ++k) {
-      const float4 pv = sv[k];
-      const float invw = sinv[k];
-      const float* yr = yb + (size_t)(a0 + k) * det;
-      const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
-#pragma unroll
-      for (int q = 0; q < kAdjPx; ++q) {
-        const int j = jb + 32 * q;
-        const float px = ct::fadd(R, ct::fmul(pv.z, (float)j));
-        int key;
-        float w;
-        ct::boxcar2d(px, pv.w, invw, key, w);
-        const float omw = ct::fsub(1.0f, w);
-        const float y0 = ((unsigned)key < (unsigned)det) ? __ldg(yr + key) : 0.0f;
-        const float y1 = ((unsigned)(key + 1) < (unsigned)det) ? __ldg(yr + key + 1) : 0.0f;
-        acc[q] = fmaf(y0, w, acc[q]);
-        acc[q] = fmaf(y1, omw, acc[q]);
+    for (int v = warp; v < n; v += 8) {
+      const float* yr = yb + (size_t)(a0 + v) * a.det;
+      const int base = sb[v];
+      float2* wy = sy + v * a.W;
+      for (int k = lane; k < a.W; k += 32) {
+        const int bin = base + k;
+        const float y0 = ((unsigned)bin < (unsigned)a.det) ? __ldg(yr + bin) : 0.0f;
+        const float y1 = ((unsigned)(bin + 1) < (unsigned)a.det) ? __ldg(yr + bin + 1) : 0.0f;
+        wy[k] = make_float2(y0, y1);
       }
     }
+    __syncthreads();
+    for (int v = 0; v < n; ++v) {
+      const int f = sf[v];
+      if (f == 1)
+        adj_view<true>(sp[v], sw[v], sb[v], sy + v * a.W, fi, fj, acc);
+      else if (f == 0)
+        adj_view<false>(sp[v], sw[v], sb[v], sy + v * a.W, fi, fj, acc);
+    }
   }
-  if (i < rows) {
-    float* o = out + (size_t)s * split_stride + (size_t)b * rows * cols + (size_t)i * cols;
+  if (i < a.rows) {
+    float* o = a.out + (size_t)sidx * a.split_stride + (size_t)b * a.rows * a.cols + (size_t)i * a.cols;
 #pragma unroll
-    for (int q = 0; q < kAdjPx; ++q) {
-      const int j = jb + 32 * q;
-      if (j < cols) o[j] = acc[q];
+    for (int q = 0; q < kAPX; ++q) {
+      const int j = j0 + tx + 16 * q;
+      if (j < a.cols) o[j] = acc[q];
     }
   }
 }
@@ -259,8 +423,8 @@ __global__ void k_sum_splits(const float* __restrict__ part, float* __restrict__
   }
 }
 
-
-// Device error word for the forward's internal span check.
+// Device error word of the projector's internal checks (bit 0: forward tile
+// span, bit 1: strip copy wait, bit 2: adjoint window span).
 __device__ int g_proj2d_err = 0;
 
 int* errflag_ptr() {
@@ -273,6 +437,16 @@ int* errflag_ptr() {
     cached[dev] = p;
   }
   return cached[dev];
+}
+
+size_t fwd_smem_bytes(int L, int LS) {
+  return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L) +
+         sizeof(int) * 2 * kFW + 16;
+}
+
+size_t adj_smem_bytes(int W) {
+  return sizeof(float2) * (size_t)kAVC * W + sizeof(float4) * kAVC + sizeof(float) * kAVC +
+         2 * sizeof(int) * kAVC;
 }
 
 }  // namespace
@@ -288,31 +462,38 @@ ct_status proj2d_check(const ct_geom2d* g, const char* who) {
                 g->cols, g->n_views, g->det_count);
   if (!g->views) return fail(CT_ERR_INVALID_ARG, "%s: null view table", who);
   if (!aligned(g->views, 16)) return fail(CT_ERR_INVALID_ARG, "%s: view table not 16-B aligned", who);
-  if (!(g->max_width > 0.0f) || g->max_width > 64.0f)
-    return fail(CT_ERR_UNSUPPORTED, "%s: max projected pixel width %g outside (0, 64]", who,
+  if (!(g->max_width > 0.0f) || g->max_width > 16.0f)
+    return fail(CT_ERR_UNSUPPORTED, "%s: max projected pixel width %g outside (0, 16]", who,
                 (double)g->max_width);
   const Proj2dPlan p = proj2d_plan(g, 1);
-  if (p.fwd_smem > 200 * 1024)
-    return fail(CT_ERR_UNSUPPORTED, "%s: tile span of %d bins too large", who, p.L);
-  if ((size_t)p.n_tiles * sizeof(int) > 200 * 1024)
-    return fail(CT_ERR_UNSUPPORTED, "%s: %d image tiles too many", who, p.n_tiles);
+  if (p.fwd_smem > 200 * 1024 || p.adj_smem > 200 * 1024)
+    return fail(CT_ERR_UNSUPPORTED, "%s: tile spans of %d / %d bins too large", who, p.L, p.W);
+  if ((size_t)p.n_strips * sizeof(int) > 48 * 1024)
+    return fail(CT_ERR_UNSUPPORTED, "%s: %d image strips too many", who, p.n_strips);
   return CT_OK;
 }
 
 Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   Proj2dPlan p;
-  p.tiles_i = (g->rows + kTile - 1) / kTile;
-  p.tiles_j = (g->cols + kTile - 1) / kTile;
-  p.n_tiles = p.tiles_i * p.tiles_j;
-  // Keys inside a tile differ by at most 31*(|Pdx0|+|Pdx1|) + 1 (plus
-  // rounding); the tile needs bins [base, top + 1].
-  p.L = (int)floorf(31.0f * g->max_width * 1.0001f + 1.01f) + 3;
-  p.LS = p.L | 1;  // odd row stride: lanes of one column hit distinct banks
-  p.view_groups = (g->n_views + kFwdViewsPerCta - 1) / kFwdViewsPerCta;
-  p.fwd_bytes = round_up((size_t)batch * p.n_tiles * g->n_views * p.L * sizeof(float), 256);
-  p.fwd_smem = (size_t)kFwdWarps * kTile * p.LS * sizeof(float);
-  p.adj_gx = (g->cols + 32 * kAdjPx - 1) / (32 * kAdjPx);
-  p.adj_gy = (g->rows + kAdjRows - 1) / kAdjRows;
+  const float mw = g->max_width * 1.0001f;
+  // Keys inside an a x b pixel rectangle differ by at most
+  // (a-1)|Pdx0| + (b-1)|Pdx1| <= max(a-1, b-1) * max_width (plus rounding),
+  // and the rectangle needs the bins [base, top + 1].
+  p.tiles_i = (g->rows + kT - 1) / kT;
+  p.n_chunks = (g->cols + kCW - 1) / kCW;
+  p.n_strips = p.tiles_i * p.n_chunks;
+  p.L = (int)floorf((float)(kT - 1) * mw + 1.01f) + 3;
+  p.LS = p.L | 1;  // odd row stride: lanes hit distinct banks
+  p.cspan = (int)floorf((float)(kCW - 1) * mw + 1.01f) + 3;
+  const long work = (long)p.n_strips * g->n_views * batch;
+  p.vpc = (int)std::min<long>(16, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
+  p.fwd_groups = (g->n_views + p.vpc - 1) / p.vpc;
+  p.fwd_bytes = round_up((size_t)batch * p.n_strips * g->n_views * p.cspan * sizeof(float), 256);
+  p.fwd_smem = fwd_smem_bytes(p.L, p.LS);
+  p.W = (int)floorf((float)(kAJ - 1) * mw + 1.01f) + 3;
+  p.adj_smem = adj_smem_bytes(p.W);
+  p.adj_gx = (g->cols + kAJ - 1) / kAJ;
+  p.adj_gy = (g->rows + kAI - 1) / kAI;
   const long ctas = (long)p.adj_gx * p.adj_gy * batch;
   int ns = 1;
   if (ctas < kAdjTargetCtas) ns = (int)((kAdjTargetCtas + ctas - 1) / ctas);
@@ -326,48 +507,63 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
 
 ct_status proj2d_prepare(const Proj2dPlan& p) {
   if (!errflag_ptr()) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
-  if (p.fwd_smem > 48 * 1024) {
-    ct_status st = cuda_check(cudaFuncSetAttribute(k_proj2d_fwd_tiles,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)p.fwd_smem),
-                              "fwd smem attribute");
-    if (st != CT_OK) return st;
-  }
-  const size_t smem2 = (size_t)p.n_tiles * sizeof(int);
-  if (smem2 > 48 * 1024) {
-    ct_status st = cuda_check(cudaFuncSetAttribute(k_proj2d_fwd_gather,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem2),
-                              "gather smem attribute");
-    if (st != CT_OK) return st;
-  }
-  return CT_OK;
+  ct_status st = cuda_check(cudaFuncSetAttribute(k_proj2d_fwd_strips,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)p.fwd_smem),
+                            "fwd smem attribute");
+  if (st != CT_OK) return st;
+  return cuda_check(cudaFuncSetAttribute(k_proj2d_adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p.adj_smem),
+                    "adj smem attribute");
 }
 
 ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* img, float* sino,
                             int batch, float* part, cudaStream_t s, const double* skip) {
-  int* errflag = errflag_ptr();
-  if (!errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
-  dim3 g1(p.n_tiles, p.view_groups, batch);
-  k_proj2d_fwd_tiles<<<g1, kFwdWarps * 32, p.fwd_smem, s>>>(img, part, g->views, g->rows, g->cols,
-                                                            g->n_views, p.L, p.LS, p.tiles_j,
-                                                            p.n_tiles, errflag, skip);
-  ct_status st = launch_check("k_proj2d_fwd_tiles");
+  FwdArgs a;
+  a.img = img;
+  a.part = part;
+  a.views = g->views;
+  a.rows = g->rows;
+  a.cols = g->cols;
+  a.nv = g->n_views;
+  a.L = p.L;
+  a.LS = p.LS;
+  a.cspan = p.cspan;
+  a.n_chunks = p.n_chunks;
+  a.vpc = p.vpc;
+  a.bulk = ((g->cols & 3) == 0 && aligned(img, 16)) ? 1 : 0;
+  a.errflag = errflag_ptr();
+  a.skip = skip;
+  if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
+  dim3 g1(p.n_strips, p.fwd_groups, batch);
+  k_proj2d_fwd_strips<<<g1, kFW * 32, p.fwd_smem, s>>>(a);
+  ct_status st = launch_check("k_proj2d_fwd_strips");
   if (st != CT_OK) return st;
   dim3 g2(g->n_views, batch);
-  k_proj2d_fwd_gather<<<g2, 256, (size_t)p.n_tiles * sizeof(int), s>>>(
-      part, sino, g->views, g->n_views, g->det_count, p.L, p.tiles_j, p.n_tiles, skip);
+  k_proj2d_fwd_gather<<<g2, 256, (size_t)p.n_strips * sizeof(int), s>>>(
+      part, sino, g->views, g->n_views, g->det_count, p.cspan, p.n_chunks, p.n_strips, skip);
   return launch_check("k_proj2d_fwd_gather");
 }
 
 ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* sino, float* out,
                             float* part, int batch, cudaStream_t s, const double* skip) {
-  const size_t n = (size_t)batch * g->rows * g->cols;
+  AdjArgs a;
+  a.sino = sino;
+  a.out = p.nsplit > 1 ? part : out;
+  a.views = g->views;
+  a.rows = g->rows;
+  a.cols = g->cols;
+  a.nv = g->n_views;
+  a.det = g->det_count;
+  a.nsplit = p.nsplit;
+  a.per_split = p.per_split;
+  a.split_stride = p.nsplit > 1 ? (size_t)batch * g->rows * g->cols : 0;
+  a.W = p.W;
+  a.errflag = errflag_ptr();
+  a.skip = skip;
+  if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
   dim3 grid(p.adj_gx, p.adj_gy, batch * p.nsplit);
-  float* dst = p.nsplit > 1 ? part : out;
-  k_proj2d_adj<<<grid, dim3(32, kAdjRows), 0, s>>>(sino, dst, g->views, g->rows, g->cols,
-                                                   g->n_views, g->det_count, p.nsplit, p.per_split,
-                                                   p.nsplit > 1 ? n : 0, skip);
+  k_proj2d_adj<<<grid, 256, p.adj_smem, s>>>(a);
   return launch_check("k_proj2d_adj");
 }
 
@@ -415,6 +611,8 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img, int32
       return ct::fail(CT_ERR_WORKSPACE, "ct_proj2d_adj: need %zu bytes (256-B aligned), got %zu",
                       p.adj_bytes, workspace_bytes);
   }
+  st = ct::proj2d_prepare(p);
+  if (st != CT_OK) return st;
   float* part = static_cast<float*>(workspace);
   st = ct::proj2d_adj_launch(g, p, sino, img, part, batch, s, nullptr);
   if (st != CT_OK || p.nsplit == 1) return st;
@@ -424,7 +622,7 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img, int32
   return ct::launch_check("k_sum_splits");
 }
 
-// Diagnostic: returns (and clears) the forward's internal span-check word.
+// Diagnostic: returns (and clears) the projector's internal check word.
 int ct_proj2d_errflag(void) {
   int v = 0;
   if (cudaMemcpyFromSymbol(&v, g_proj2d_err, sizeof(int)) != cudaSuccess) return -1;

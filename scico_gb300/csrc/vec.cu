@@ -2,6 +2,7 @@
 // scico.solver.cg (scico/solver.py:378-400), with the stopping test kept on
 // the device so that a fixed launch sequence reproduces the early exit.
 #include "common.cuh"
+#include "kernels.cuh"
 
 namespace {
 
@@ -23,42 +24,13 @@ ct_status red_ws(void* ws, size_t bytes, const char* who, RedWs& r) {
 template <int NT>
 __device__ __forceinline__ bool grid_sum2_last(double a, double b, double* partials,
                                                unsigned int* ticket, double& ta, double& tb) {
-  __shared__ double red[2][NT / 32];
-  __shared__ bool is_last;
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
+  double v[2] = {a, b}, out[2];
+  const bool last = ct::grid_reduce_last<NT, 2>(v, partials, ticket, out);
+  if (last) {
+    ta = out[0];
+    tb = out[1];
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) {
-    red[0][warp] = a;
-    red[1][warp] = b;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double sa = 0.0, sb = 0.0;
-    for (int k = 0; k < NT / 32; ++k) {
-      sa += red[0][k];
-      sb += red[1][k];
-    }
-    partials[2 * blockIdx.x] = sa;
-    partials[2 * blockIdx.x + 1] = sb;
-    __threadfence();
-    is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!is_last || threadIdx.x != 0) return false;
-  __threadfence();
-  volatile double* vp = partials;
-  double sa = 0.0, sb = 0.0;
-  for (unsigned int k = 0; k < gridDim.x; ++k) {
-    sa += vp[2 * k];
-    sb += vp[2 * k + 1];
-  }
-  ta = sa;
-  tb = sb;
-  *ticket = 0u;
-  return true;
+  return last;
 }
 
 constexpr int NT = ct::kReduceThreads;
@@ -134,19 +106,25 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-// p = r + beta p, only when the preceding update ran.
+// p = r + beta p, only when the preceding update ran.  Every block reads
+// the marker when it starts; the last block to finish (ticket in the second
+// word of the reduction workspace) clears it, after all blocks have read it.
 __global__ void k_cg_direction(float* __restrict__ p, const float* __restrict__ r, size_t n,
-                               double* __restrict__ s) {
-  if (s[CT_CG_RAN] == 0.0) return;
+                               double* __restrict__ s, unsigned int* __restrict__ ticket) {
+  if (s[CT_CG_RAN] == 0.0) return;  // uniform over the grid
   const float bf = (float)s[CT_CG_BETA];
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
        e += (size_t)gridDim.x * blockDim.x)
     p[e] = ct::fadd(r[e], ct::fmul(bf, p[e]));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(ticket, 1u) == gridDim.x - 1) {
+      s[CT_CG_RAN] = 0.0;
+      *ticket = 0u;
+    }
+  }
 }
-
-// Clears the "update ran" marker once every block of k_cg_direction is done
-// (launched right after it, single thread).
-__global__ void k_cg_direction_done(double* __restrict__ s) { s[CT_CG_RAN] = 0.0; }
 
 }  // namespace
 
@@ -191,21 +169,17 @@ ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap, int6
   return ct::launch_check("k_cg_update");
 }
 
-ct_status ct_cg_direction(float* p, const float* r, int64_t n, double* scalars,
-                          ct_stream_t stream) {
+ct_status ct_cg_direction(float* p, const float* r, int64_t n, double* scalars, void* workspace,
+                          size_t workspace_bytes, ct_stream_t stream) {
   if (!p || !r || !scalars) return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_direction: null pointer");
-  cudaStream_t s = ct::as_stream(stream);
-  double* sc = scalars;
-  k_cg_direction<<<ct::kReduceBlocks, NT, 0, s>>>(p, r, (size_t)n, sc);
-  ct_status st = ct::launch_check("k_cg_direction");
+  RedWs w;
+  ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_direction", w);
   if (st != CT_OK) return st;
-  k_cg_direction_done<<<1, 1, 0, s>>>(sc);
-  return ct::launch_check("k_cg_direction_done");
+  return ct::cg_direction_launch(p, r, (size_t)n, scalars, workspace, ct::as_stream(stream));
 }
 
 }  // extern "C"
 
-#include "kernels.cuh"
 
 namespace ct {
 
@@ -217,12 +191,11 @@ ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, 
   return launch_check("k_cg_update");
 }
 
-ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, cudaStream_t s) {
-  k_cg_direction<<<kReduceBlocks, NT, 0, s>>>(p, r, n, scalars);
-  ct_status st = launch_check("k_cg_direction");
-  if (st != CT_OK) return st;
-  k_cg_direction_done<<<1, 1, 0, s>>>(scalars);
-  return launch_check("k_cg_direction_done");
+ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, void* red_ws,
+                              cudaStream_t s) {
+  unsigned int* ticket2 = static_cast<unsigned int*>(red_ws) + 1;
+  k_cg_direction<<<kReduceBlocks, NT, 0, s>>>(p, r, n, scalars, ticket2);
+  return launch_check("k_cg_direction");
 }
 
 }  // namespace ct

@@ -240,7 +240,9 @@ class ADMM:
         lam = {k: w for k, w in kinds}
         if any(w == 0 for w in lam.values()):
             return None
-        order = [0 if k == "l21" else 1 for k, _ in kinds]
+        # the native solver keeps its terms in the order L2,1 then L1
+        native = [k for k in ("l21", "l1") if k in lam]
+        order = [native.index(k) for k, _ in kinds]
         return dict(lam21=lam.get("l21", 0.0), lam1=lam.get("l1", 0.0), order=order)
 
     def _solve_fused(self):

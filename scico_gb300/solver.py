@@ -45,7 +45,7 @@ def cg(A: Callable, b, x0=None, *, tol: float = 1e-5, atol: float = 0.0, maxiter
         _lib.call("ct_dot", p.data_ptr(), Ap.data_ptr(), n, pap, ws.data_ptr(), ws.numel(), st)
         _lib.call("ct_cg_update", x.data_ptr(), r.data_ptr(), p.data_ptr(), Ap.data_ptr(), n, s.data_ptr(),
                   ws.data_ptr(), ws.numel(), st)
-        _lib.call("ct_cg_direction", p.data_ptr(), r.data_ptr(), n, s.data_ptr(), st)
+        _lib.call("ct_cg_direction", p.data_ptr(), r.data_ptr(), n, s.data_ptr(), ws.data_ptr(), ws.numel(), st)
     if not info:
         return x
     sc = s.cpu().numpy()

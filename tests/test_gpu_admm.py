@@ -11,9 +11,11 @@ Two regimes, because the x-update is a float32 CG:
   benchmark configurations).  There the iterates depend on float32 rounding:
   perturbing only the projector's rounding (float64 projector rounded to
   float32) moves x by 1e-3 .. 1e-2 after a few iterations, for any float32
-  implementation including the reference.  The bar is the measured floor:
-  rel l2 <= 2e-2 against the same-precision oracle (float32 vectors, float64
-  dots) and the objective to 5e-3.
+  implementation including the reference.  The bar is that floor, measured
+  in the test: the GPU result must lie within 3x the spread of the
+  same-precision oracle (float32 vectors, float64 dots) run with its float32
+  projector and with a float64 projector rounded to float32, for x and for
+  the objective.
 """
 
 from pathlib import Path
@@ -91,16 +93,28 @@ def test_admm_converged_vs_oracle(cuda, fused, terms):
         assert ctref.rel_l2(zk.cpu().numpy(), zo) <= 1e-3
 
 
+def _floor_oracle(y, shape, g, **kw):
+    """Same-precision oracle (float32 vectors, float64 dots) twice: with its
+    float32 projector and with a float64 projector rounded to float32.  Their
+    spread is the float32 rounding floor of the problem."""
+    xm, hm, _, _ = _oracle(y, shape, g, dtype=np.float32, dot_dtype=np.float64, **kw)
+    fwd = lambda v: ctref.xray2d_project(v, g, np.float64).astype(np.float32)
+    adj = lambda v: ctref.xray2d_back_project(v, g, np.float64).astype(np.float32)
+    xp, hp, _, _ = ctref.admm_tv(fwd, adj, y.astype(np.float32), shape, dtype=np.float32, dot_dtype=np.float64, **kw)
+    om, op = np.array([r["Objective"] for r in hm]), np.array([r["Objective"] for r in hp])
+    return xm, om, ctref.rel_l2(xp, xm), float(np.max(np.abs(op / om - 1)))
+
+
 @pytest.mark.parametrize("fused", [False, True])
 def test_admm_capped_vs_oracle(cuda, fused):
     x_gt, ang, g, y = _problem(n=32, nv=24)
     s = _solver(cuda, ang, y, x_gt.shape, lam21=0.02, rho=1.0, maxiter=6, cg_maxiter=10, cg_tol=1e-4,
                 fused=fused)
     x = s.solve().cpu().numpy()
-    xm, hm, _, _ = _oracle(y, x_gt.shape, g, dtype=np.float32, dot_dtype=np.float64, lam_l21=0.02, rho=1.0,
-                           maxiter=6, cg_maxiter=10, cg_tol=1e-4)
-    assert ctref.rel_l2(x, xm) <= 2e-2
-    np.testing.assert_allclose(s.history(transpose=True).Objective, [r["Objective"] for r in hm], rtol=5e-3)
+    xm, om, fx, fo = _floor_oracle(y, x_gt.shape, g, lam_l21=0.02, rho=1.0, maxiter=6, cg_maxiter=10, cg_tol=1e-4)
+    assert ctref.rel_l2(x, xm) <= 3 * fx + 1e-4, (ctref.rel_l2(x, xm), fx)
+    obj = np.array(s.history(transpose=True).Objective)
+    assert np.max(np.abs(obj / om - 1)) <= 3 * fo + 1e-4, (np.max(np.abs(obj / om - 1)), fo)
 
 
 def test_fused_matches_generic(cuda):

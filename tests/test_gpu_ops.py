@@ -105,7 +105,10 @@ def test_cg_spd(cuda):
 
 
 def test_cg_ct_normal_equations(cuda):
-    """CG on (A^T A + D^T D) x = A^T y vs the float64 oracle's CG."""
+    """CG on (A^T A + D^T D) x = A^T y, 15 steps, against the same-precision
+    oracle CG (float32 vectors, float64 dots), within the float32 rounding
+    floor of the problem (the spread between that oracle with its float32
+    projector and with a float64 projector rounded to float32)."""
     from scico_gb300 import workloads
 
     x_gt = workloads.random_ellipses(48, 5, 21)
@@ -117,10 +120,15 @@ def test_cg_ct_normal_equations(cuda):
     y = ctref.xray2d_project(x_gt, g, np.float64).astype(np.float32)
     b = H.adj(torch.from_numpy(y).to(cuda))
     x, info = solver.cg(lhs, b, torch.zeros_like(b), tol=1e-4, maxiter=15)
-    fwd = lambda v: ctref.xray2d_project(v, g, np.float64)
-    adj = lambda v: ctref.xray2d_back_project(v, g, np.float64)
-    l64 = lambda v: adj(fwd(v)) + ctref.fd_adj(ctref.fd_eval(v, append=0), x_gt.shape, append=0)
-    b64 = adj(y.astype(np.float64))
-    x64, info64 = ctref.cg(l64, b64, np.zeros_like(b64), tol=1e-4, maxiter=15)
-    assert info["num_iter"] == info64["num_iter"]
-    assert ctref.rel_l2(x.cpu().numpy(), x64) < 1e-5
+    D = lambda v: ctref.fd_adj(ctref.fd_eval(v, append=0), x_gt.shape, append=0)
+    runs = []
+    for pdt in (np.float32, np.float64):
+        fwd = lambda v: ctref.xray2d_project(v, g, pdt).astype(np.float32)
+        adj = lambda v: ctref.xray2d_back_project(v, g, pdt).astype(np.float32)
+        bb = b.cpu().numpy()
+        runs.append(ctref.cg(lambda v: adj(fwd(v)) + D(v), bb, np.zeros_like(bb), tol=1e-4, maxiter=15,
+                             dot_dtype=np.float64))
+    (xm, im), (xp, _) = runs
+    floor = ctref.rel_l2(xp, xm)
+    assert abs(info["num_iter"] - im["num_iter"]) <= 1
+    assert ctref.rel_l2(x.cpu().numpy(), xm) <= 3 * floor + 1e-5, (ctref.rel_l2(x.cpu().numpy(), xm), floor)
