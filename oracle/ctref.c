@@ -55,9 +55,62 @@ static inline void weight_of(const float* v, int i, int j, int* key, float* w) {
   *w = (dist < width ? dist : width) / width;
 }
 
+/* 1: accumulate the projector sums in float64 and round once (the same
+ * operator with different rounding: used to measure how sensitive a solve is
+ * to float32 summation order). */
+static int g_proj64 = 0;
+void ref_set_proj64(int on) { g_proj64 = on; }
+
+static void proj2d_fwd64(const ref_geom* g, const float* x, float* y) {
+  const int R = g->rows, C = g->cols, D = g->det;
+#pragma omp parallel
+  {
+    double* acc = (double*)malloc(sizeof(double) * (size_t)D);
+#pragma omp for schedule(dynamic, 1)
+    for (int a = 0; a < g->nv; ++a) {
+      const float* v = g->views + 8 * (size_t)a;
+      for (int b = 0; b < D; ++b) acc[b] = 0.0;
+      for (int i = 0; i < R; ++i)
+        for (int j = 0; j < C; ++j) {
+          int k;
+          float w;
+          weight_of(v, i, j, &k, &w);
+          const double xv = x[(size_t)i * C + j];
+          if (k >= 0 && k < D) acc[k] += xv * w;
+          if (k + 1 >= 0 && k + 1 < D) acc[k + 1] += xv * (1.0f - w);
+        }
+      for (int b = 0; b < D; ++b) y[(size_t)a * D + b] = (float)acc[b];
+    }
+    free(acc);
+  }
+}
+
+static void proj2d_adj64(const ref_geom* g, const float* y, float* x) {
+  const int R = g->rows, C = g->cols, D = g->det;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < R; ++i)
+    for (int j = 0; j < C; ++j) {
+      double s = 0.0;
+      for (int a = 0; a < g->nv; ++a) {
+        const float* v = g->views + 8 * (size_t)a;
+        int k;
+        float w;
+        weight_of(v, i, j, &k, &w);
+        const float* ya = y + (size_t)a * D;
+        if (k >= 0 && k < D) s += (double)ya[k] * w;
+        if (k + 1 >= 0 && k + 1 < D) s += (double)ya[k + 1] * (1.0f - w);
+      }
+      x[(size_t)i * C + j] = (float)s;
+    }
+}
+
 /* y = A x: the two scatter-adds per view, in update order (:254-263). */
 void ref_proj2d_fwd(const ref_geom* g, const float* x, float* y) {
   const int R = g->rows, C = g->cols, D = g->det;
+  if (g_proj64) {
+    proj2d_fwd64(g, x, y);
+    return;
+  }
 #pragma omp parallel for schedule(dynamic, 1)
   for (int a = 0; a < g->nv; ++a) {
     const float* v = g->views + 8 * (size_t)a;
@@ -79,6 +132,10 @@ void ref_proj2d_fwd(const ref_geom* g, const float* x, float* y) {
  * (:293-306). */
 void ref_proj2d_adj(const ref_geom* g, const float* y, float* x) {
   const int R = g->rows, C = g->cols, D = g->det;
+  if (g_proj64) {
+    proj2d_adj64(g, y, x);
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (int i = 0; i < R; ++i)
     for (int j = 0; j < C; ++j) {

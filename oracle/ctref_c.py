@@ -37,6 +37,7 @@ def lib():
                                      ctypes.c_int, ctypes.c_float, P, P, P, P]
         _lib.ref_admm_tv.restype = ctypes.c_int
         _lib.ref_set_dot64.argtypes = [ctypes.c_int]
+        _lib.ref_set_proj64.argtypes = [ctypes.c_int]
     return _lib
 
 
@@ -65,12 +66,15 @@ class Geometry:
         lib().ref_proj2d_adj(ctypes.addressof(self.cg), y.ctypes.data, x.ctypes.data)
         return x
 
-    def admm_tv(self, y, lam, rho, maxiter, cg_maxiter=10, cg_tol=1e-4, scale=0.5, state=None, dot64=False):
+    def admm_tv(self, y, lam, rho, maxiter, cg_maxiter=10, cg_tol=1e-4, scale=0.5, state=None, dot64=False,
+                proj64=False):
         """Run `maxiter` ADMM-TV iterations; returns (x, z, u, itstat (maxiter, 5)).
 
         dot64=False: float32 CG scalars as the reference; True: float64 dot
-        products (the GPU solver's precision policy)."""
+        products (the GPU solver's precision policy).  proj64: projector sums
+        accumulated in float64 and rounded once (rounding-sensitivity probe)."""
         lib().ref_set_dot64(1 if dot64 else 0)
+        lib().ref_set_proj64(1 if proj64 else 0)
         y = np.ascontiguousarray(y, dtype=np.float32)
         R, C = self.shape
         if state is None:

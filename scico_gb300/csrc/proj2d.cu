@@ -74,21 +74,35 @@ __device__ __forceinline__ void rect_px(const ViewParams& p, int i0, int i1, int
   hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
 }
 
-// key = floor(px) - kbias and w = min(1 - (px - floor(px)), width) * inv_width.
-template <bool FAST>
-__device__ __forceinline__ void weight(float px, float width, float inv_width, int kbias, int& key,
-                                       float& w) {
-  float fl;
-  if (FAST) {
-    const float t = __fadd_rd(px, kMagic);  // kMagic + floor(px), exactly
-    key = __float_as_int(t) - (kMagicBits + kbias);
-    fl = ct::fsub(t, kMagic);
-  } else {
-    fl = floorf(px);
-    key = (int)fl - kbias;
-  }
+// key = floor(px) - kbias and w = min(1 - (px - floor(px)), width) * inv_width
+// (the general path, used where |Px| may reach 2^21).
+__device__ __forceinline__ void weight_floor(float px, float width, float inv_width, int kbias, int& key,
+                                             float& w) {
+  const float fl = floorf(px);
+  key = (int)fl - kbias;
   const float dist = ct::fsub(1.0f, ct::fsub(px, fl));
   w = ct::fmul(fminf(dist, width), inv_width);
+}
+
+// Fast path for |px| < 2^22: t = kMagic + floor(px) exactly (one round-down
+// add), fl = floor(px), and w = sat((1 - (px - fl)) * inv_width), which is
+// min(1 - (px - fl), width) / width up to one rounding of the product.
+__device__ __forceinline__ void weight_fast(float px, float inv_width, int& tbits, float& fl, float& w) {
+  const float t = __fadd_rd(px, kMagic);
+  tbits = __float_as_int(t);
+  fl = ct::fsub(t, kMagic);
+  const float dist = ct::fsub(1.0f, ct::fsub(px, fl));
+  w = __saturatef(ct::fmul(dist, inv_width));
+}
+
+__device__ __forceinline__ void st_shared(uint32_t addr, float v) {
+  asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
+__device__ __forceinline__ float2 ld_shared2(uint32_t addr) {
+  float2 r;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(addr) : "memory");
+  return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -96,12 +110,44 @@ __device__ __forceinline__ void weight(float px, float width, float inv_width, i
 // ---------------------------------------------------------------------------
 
 // Walk one tile row for one view.  REV walks j downwards (Pdx1 < 0) so that
-// the bin key never decreases.  mp: this lane's partial row, indexed by
-// key - base.  Bin b receives, in walk order, the (1-w) x of the pixels with
-// key b-1 followed by the w x of the pixels with key b.
-template <bool REV, bool FAST>
-__device__ __forceinline__ void walk_row(const float (&xr)[kT], float* __restrict__ mp, const ViewParams& p,
-                                         float R, float fj0, int base) {
+// the bin key never decreases.  Bin b receives, in walk order, the (1-w) x of
+// the pixels with key b-1 followed by the w x of the pixels with key b.
+//
+// walk_row_fast: |Pdx1| < 0.999 and |Px| < 2^21, so consecutive keys differ
+// by 0 or 1 (d).  The carry select is done with exact 0/1 mask products on
+// the FMA pipe: a0 = A (1-d) + B d, b0 = B (1-d).  The partial row is
+// addressed directly from the float bits of kMagic + key:
+// row_addr = mp_addr - 4 (kMagicBits + base).
+template <bool REV>
+__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, const ViewParams& p,
+                                              float R, float fj0) {
+  float A = 0.0f, B = 0.0f, flp = 0.0f;
+  int tb = 0;
+#pragma unroll
+  for (int t = 0; t < kT; ++t) {
+    const int jj = REV ? kT - 1 - t : t;
+    const float px = ct::fadd(R, ct::fmul(p.pd1, fj0 + (float)jj));
+    float fl, w;
+    weight_fast(px, p.inv_width, tb, fl, w);
+    const float omw = ct::fsub(1.0f, w);
+    if (t == 0) flp = fl;
+    const float d = ct::fsub(fl, flp);
+    const float m0 = ct::fsub(1.0f, d);
+    const float a0 = fmaf(B, d, ct::fmul(A, m0));
+    const float b0 = ct::fmul(B, m0);
+    A = fmaf(w, xr[jj], a0);
+    B = fmaf(omw, xr[jj], b0);
+    flp = fl;
+    st_shared(row_addr + 4u * (uint32_t)tb, A);
+  }
+  st_shared(row_addr + 4u * (uint32_t)tb + 4u, B);
+}
+
+// General walk (any step, floorf when |Px| may be large): bins skipped when
+// the key advances by 2 or more keep their zero.
+template <bool REV>
+__device__ __forceinline__ void walk_row_gen(const float (&xr)[kT], float* __restrict__ mp, const ViewParams& p,
+                                             float R, float fj0, int base) {
   int cur = 0;
   float A = 0.0f, B = 0.0f;
 #pragma unroll
@@ -110,11 +156,11 @@ __device__ __forceinline__ void walk_row(const float (&xr)[kT], float* __restric
     const float px = ct::fadd(R, ct::fmul(p.pd1, fj0 + (float)jj));
     int key;
     float w;
-    weight<FAST>(px, p.width, p.inv_width, base, key, w);
+    weight_floor(px, p.width, p.inv_width, base, key, w);
     const float omw = ct::fsub(1.0f, w);
     if (t == 0) cur = key;
     const int d = key - cur;
-    if (d >= 2) mp[cur + 1] = B;  // bin cur+1 complete; bins between stay 0
+    if (d >= 2) mp[cur + 1] = B;
     const float a0 = d == 0 ? A : (d == 1 ? B : 0.0f);
     const float b0 = d == 0 ? B : 0.0f;
     A = fmaf(w, xr[jj], a0);
@@ -146,7 +192,8 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
   float* slot = part + kFW * kT * a.LS;                              // [kFW][L]
   int* sbase = reinterpret_cast<int*>(slot + kFW * a.L);             // [kFW]
   int* sspan = sbase + kFW;                                          // [kFW]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sspan + kFW + 0) + 0;  // 8-B aligned below
+  int* scb = sspan + kFW;                                            // strip base of the view
+  uint64_t* bar = reinterpret_cast<uint64_t*>(scb + 1);              // 8-B aligned below
   bar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(bar) + 7) & ~uintptr_t(7));
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -210,7 +257,7 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
       rect_px(p, i0, i0 + kT - 1, j0, j0 + kT - 1, lo, hi);
       base = (int)floorf(lo);
       span = (int)floorf(hi) - base + 2;
-      const bool fast = fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit;
+      const bool fast = fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit && fabsf(p.pd1) < 0.999f;
       if (span > a.L) {  // cannot happen for a table from ct_proj2d_views
         if (lane == 0) atomicOr(a.errflag, 1);
         span = 0;
@@ -227,15 +274,16 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
         }
         const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, fi));
         if (fast) {
+          const uint32_t row_addr = ct::smem_u32(mp) - 4u * (uint32_t)(kMagicBits + base);
           if (p.pd1 >= 0.0f)
-            walk_row<false, true>(xr, mp, p, R, fj0, base);
+            walk_row_fast<false>(xr, row_addr, p, R, fj0);
           else
-            walk_row<true, true>(xr, mp, p, R, fj0, base);
+            walk_row_fast<true>(xr, row_addr, p, R, fj0);
         } else {
           if (p.pd1 >= 0.0f)
-            walk_row<false, false>(xr, mp, p, R, fj0, base);
+            walk_row_gen<false>(xr, mp, p, R, fj0, base);
           else
-            walk_row<true, false>(xr, mp, p, R, fj0, base);
+            walk_row_gen<true>(xr, mp, p, R, fj0, base);
         }
         __syncwarp();
         // rows summed in row order; the read entries are zeroed again
@@ -255,11 +303,14 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
       sbase[warp] = base;
       sspan[warp] = span;
     }
+    if (tid == 32) {
+      float lo, hi;
+      rect_px(p, i0, i0 + kT - 1, c0, c0 + kCW - 1, lo, hi);
+      *scb = (int)floorf(lo);
+    }
     __syncthreads();
     // ---- combine the 8 tiles in tile order into the strip's bins ----------
-    float lo, hi;
-    rect_px(p, i0, i0 + kT - 1, c0, c0 + kCW - 1, lo, hi);
-    const int cb = (int)floorf(lo);
+    const int cb = *scb;
     float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + v) * a.cspan;
     for (int k = tid; k < a.cspan; k += kFW * 32) {
       float acc = 0.0f;
@@ -320,16 +371,33 @@ struct AdjArgs {
   const double* skip;
 };
 
-template <bool FAST>
-__device__ __forceinline__ void adj_view(const float4 pv, float width, int base, const float2* __restrict__ wy,
-                                         float fi, const float (&fj)[kAPX], float (&acc)[kAPX]) {
+// One view's contribution to this thread's pixels.  Fast path: the window
+// pair of key k lives at shared address off + 8 (kMagicBits + k) for the
+// float bits kMagicBits + k of kMagic + k.
+__device__ __forceinline__ void adj_view_fast(const float4 pv, uint32_t off, float fi, const float (&fj)[kAPX],
+                                              float (&acc)[kAPX]) {
+  const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
+#pragma unroll
+  for (int q = 0; q < kAPX; ++q) {
+    const float px = ct::fadd(R, ct::fmul(pv.z, fj[q]));
+    int tb;
+    float fl, w;
+    weight_fast(px, pv.w, tb, fl, w);
+    const float2 y = ld_shared2(off + 8u * (uint32_t)tb);
+    acc[q] = fmaf(y.x, w, acc[q]);
+    acc[q] = fmaf(y.y, ct::fsub(1.0f, w), acc[q]);
+  }
+}
+
+__device__ __forceinline__ void adj_view_gen(const float4 pv, float width, int base, const float2* __restrict__ wy,
+                                             float fi, const float (&fj)[kAPX], float (&acc)[kAPX]) {
   const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
 #pragma unroll
   for (int q = 0; q < kAPX; ++q) {
     const float px = ct::fadd(R, ct::fmul(pv.z, fj[q]));
     int key;
     float w;
-    weight<FAST>(px, width, pv.w, base, key, w);
+    weight_floor(px, width, pv.w, base, key, w);
     const float2 y = wy[key];
     acc[q] = fmaf(y.x, w, acc[q]);
     acc[q] = fmaf(y.y, ct::fsub(1.0f, w), acc[q]);
@@ -345,6 +413,7 @@ __global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
   float* sw = reinterpret_cast<float*>(sp + kAVC);           // [kAVC] width
   int* sb = reinterpret_cast<int*>(sw + kAVC);               // [kAVC] window base
   int* sf = sb + kAVC;                                       // [kAVC] 1 = fast floor, -1 = skip
+  uint32_t* so = reinterpret_cast<uint32_t*>(sf + kAVC);     // [kAVC] fast-path address offset
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int z = blockIdx.z;
@@ -380,6 +449,7 @@ __global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
         f = -1;
       }
       sf[tid] = f;
+      so[tid] = ct::smem_u32(sy + tid * a.W) - 8u * (uint32_t)(kMagicBits + base);
     }
     __syncthreads();
     for (int v = warp; v < n; v += 8) {
@@ -397,9 +467,9 @@ __global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
     for (int v = 0; v < n; ++v) {
       const int f = sf[v];
       if (f == 1)
-        adj_view<true>(sp[v], sw[v], sb[v], sy + v * a.W, fi, fj, acc);
+        adj_view_fast(sp[v], so[v], fi, fj, acc);
       else if (f == 0)
-        adj_view<false>(sp[v], sw[v], sb[v], sy + v * a.W, fi, fj, acc);
+        adj_view_gen(sp[v], sw[v], sb[v], sy + v * a.W, fi, fj, acc);
     }
   }
   if (i < a.rows) {
@@ -441,12 +511,12 @@ int* errflag_ptr() {
 
 size_t fwd_smem_bytes(int L, int LS) {
   return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L) +
-         sizeof(int) * 2 * kFW + 16;
+         sizeof(int) * (2 * kFW + 1) + 24;
 }
 
 size_t adj_smem_bytes(int W) {
   return sizeof(float2) * (size_t)kAVC * W + sizeof(float4) * kAVC + sizeof(float) * kAVC +
-         2 * sizeof(int) * kAVC;
+         3 * sizeof(int) * kAVC;
 }
 
 }  // namespace

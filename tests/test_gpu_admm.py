@@ -149,7 +149,9 @@ def test_fused_deterministic(cuda):
 
 def test_c1_admm_quality(cuda):
     """C1 geometry (256^2, 180 views, 363 bins), lambda 0.01, rho 1, CG <= 10:
-    3 iterations against the same-precision oracle (capped regime floor)."""
+    3 iterations against the same-precision C oracle, within 3x its rounding
+    floor (the spread between its float32-summed and float64-summed
+    projector) for x, the objective and the SNR to the phantom."""
     from oracle import ctref_c
 
     c = workloads.C1
@@ -161,6 +163,12 @@ def test_c1_admm_quality(cuda):
     x = s.solve().cpu().numpy()
     ctref_c.set_threads(ctref_c.default_threads())
     xm, _, _, it = G.admm_tv(y, c.lam, c.rho, 3, cg_maxiter=c.cg_maxiter, cg_tol=c.cg_tol, dot64=True)
-    assert ctref.rel_l2(x, xm) <= 2e-2
-    np.testing.assert_allclose(s.history(transpose=True).Objective, it[:, 0], rtol=5e-3)
-    assert abs(ctref.snr(x_gt, x) - ctref.snr(x_gt, xm)) < 0.1
+    xp, _, _, itp = G.admm_tv(y, c.lam, c.rho, 3, cg_maxiter=c.cg_maxiter, cg_tol=c.cg_tol, dot64=True,
+                              proj64=True)
+    fx = ctref.rel_l2(xp, xm)
+    fo = float(np.max(np.abs(itp[:, 0] / it[:, 0] - 1)))
+    fs = abs(ctref.snr(x_gt, xp) - ctref.snr(x_gt, xm))
+    assert ctref.rel_l2(x, xm) <= 3 * fx + 1e-4, (ctref.rel_l2(x, xm), fx)
+    obj = np.array(s.history(transpose=True).Objective)
+    assert np.max(np.abs(obj / it[:, 0] - 1)) <= 3 * fo + 1e-4, (np.max(np.abs(obj / it[:, 0] - 1)), fo)
+    assert abs(ctref.snr(x_gt, x) - ctref.snr(x_gt, xm)) <= 3 * fs + 0.02
