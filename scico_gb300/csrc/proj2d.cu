@@ -85,13 +85,15 @@ __device__ __forceinline__ void weight_floor(float px, float width, float inv_wi
 }
 
 // Fast path for |px| < 2^22: t = kMagic + floor(px) exactly (one round-down
-// add), fl = floor(px), and w = sat((1 - (px - fl)) * inv_width), which is
-// min(1 - (px - fl), width) / width up to one rounding of the product.
-__device__ __forceinline__ void weight_fast(float px, float inv_width, int& tbits, float& fl, float& w) {
+// add), dist = (floor(px) + 1) - px and w = sat(dist * inv_width), which is
+// min(1 - (px - floor(px)), width) / width up to one rounding of the product
+// (dist is the reference's 1 - (px - floor(px)) exactly for px >= 0; below
+// the detector's first bin it may differ by one rounding).
+__device__ __forceinline__ void weight_fast(float px, float inv_width, int& tbits, float& w) {
   const float t = __fadd_rd(px, kMagic);
   tbits = __float_as_int(t);
-  fl = ct::fsub(t, kMagic);
-  const float dist = ct::fsub(1.0f, ct::fsub(px, fl));
+  const float fl1 = ct::fsub(t, kMagic - 1.0f);
+  const float dist = ct::fsub(fl1, px);
   w = __saturatef(ct::fmul(dist, inv_width));
 }
 
@@ -119,28 +121,28 @@ __device__ __forceinline__ float2 ld_shared2(uint32_t addr) {
 // addressed directly from the float bits of kMagic + key:
 // row_addr = mp_addr - 4 (kMagicBits + base).
 template <bool REV>
-__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, const ViewParams& p,
-                                              float R, float fj0) {
-  float A = 0.0f, B = 0.0f, flp = 0.0f;
-  int tb = 0;
+__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, const float* __restrict__ pj,
+                                              float R, float inv_width) {
+  float A = 0.0f, B = 0.0f;
+  int tbp = 0;
 #pragma unroll
   for (int t = 0; t < kT; ++t) {
     const int jj = REV ? kT - 1 - t : t;
-    const float px = ct::fadd(R, ct::fmul(p.pd1, fj0 + (float)jj));
-    float fl, w;
-    weight_fast(px, p.inv_width, tb, fl, w);
+    const float px = ct::fadd(R, pj[jj]);  // pj[jj] = Pdx1 * (j0 + jj), shared by the warp
+    int tb;
+    float w;
+    weight_fast(px, inv_width, tb, w);
     const float omw = ct::fsub(1.0f, w);
-    if (t == 0) flp = fl;
-    const float d = ct::fsub(fl, flp);
-    const float m0 = ct::fsub(1.0f, d);
-    const float a0 = fmaf(B, d, ct::fmul(A, m0));
-    const float b0 = ct::fmul(B, m0);
+    if (t == 0) tbp = tb;
+    const bool next = tb != tbp;  // the key advanced by one bin
+    const float a0 = next ? B : A;
+    const float b0 = next ? 0.0f : B;
     A = fmaf(w, xr[jj], a0);
     B = fmaf(omw, xr[jj], b0);
-    flp = fl;
+    tbp = tb;
     st_shared(row_addr + 4u * (uint32_t)tb, A);
   }
-  st_shared(row_addr + 4u * (uint32_t)tb + 4u, B);
+  st_shared(row_addr + 4u * (uint32_t)tbp + 4u, B);
 }
 
 // General walk (any step, floorf when |Px| may be large): bins skipped when
@@ -190,7 +192,8 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
   float* strip = reinterpret_cast<float*>(smem_raw);                 // [32][kRS]
   float* part = strip + kT * kRS;                                    // [kFW][32][LS]
   float* slot = part + kFW * kT * a.LS;                              // [kFW][L]
-  int* sbase = reinterpret_cast<int*>(slot + kFW * a.L);             // [kFW]
+  float* pjt = slot + kFW * a.L;                                     // [kFW][32]
+  int* sbase = reinterpret_cast<int*>(pjt + kFW * kT);               // [kFW]
   int* sspan = sbase + kFW;                                          // [kFW]
   int* scb = sspan + kFW;                                            // strip base of the view
   uint64_t* bar = reinterpret_cast<uint64_t*>(scb + 1);              // 8-B aligned below
@@ -218,20 +221,19 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
       for (int r = 0; r < vrows; ++r)
         ct::bulk_g2s(strip + r * kRS, im + (size_t)(i0 + r) * a.cols + c0, row_bytes, bar);
     }
-    // zero what the copies do not cover (disjoint addresses)
-    for (int e = tid; e < kT * kRS; e += kFW * 32) {
-      const int r = e / kRS, c = e - r * kRS;
-      if (r >= vrows || c >= vcols) strip[e] = 0.0f;
-    }
+    // zero what the copies do not cover (disjoint addresses): warp w, rows
+    // w, w+8, ...
+    for (int r = warp; r < kT; r += kFW)
+      for (int c = lane; c < kRS; c += 32)
+        if (r >= vrows || c >= vcols) strip[r * kRS + c] = 0.0f;
     if (!ct::mbar_wait_bounded(bar, 0, kMaxPolls)) {
       if (tid == 0) atomicOr(a.errflag, 2);
       ct::mbar_wait_bounded(bar, 0, kMaxPolls);
     }
   } else {
-    for (int e = tid; e < kT * kRS; e += kFW * 32) {
-      const int r = e / kRS, c = e - r * kRS;
-      strip[e] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
-    }
+    for (int r = warp; r < kT; r += kFW)
+      for (int c = lane; c < kRS; c += 32)
+        strip[r * kRS + c] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
   }
   // zero every partial row once; after each tile the reduction re-zeroes
   // exactly what the walk wrote, so rows stay zero outside a tile's bins
@@ -274,11 +276,14 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
         }
         const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, fi));
         if (fast) {
+          float* pj = pjt + warp * kT;
+          pj[lane] = ct::fmul(p.pd1, fj0 + (float)lane);
+          __syncwarp();
           const uint32_t row_addr = ct::smem_u32(mp) - 4u * (uint32_t)(kMagicBits + base);
           if (p.pd1 >= 0.0f)
-            walk_row_fast<false>(xr, row_addr, p, R, fj0);
+            walk_row_fast<false>(xr, row_addr, pj, R, p.inv_width);
           else
-            walk_row_fast<true>(xr, row_addr, p, R, fj0);
+            walk_row_fast<true>(xr, row_addr, pj, R, p.inv_width);
         } else {
           if (p.pd1 >= 0.0f)
             walk_row_gen<false>(xr, mp, p, R, fj0, base);
@@ -381,8 +386,8 @@ __device__ __forceinline__ void adj_view_fast(const float4 pv, uint32_t off, flo
   for (int q = 0; q < kAPX; ++q) {
     const float px = ct::fadd(R, ct::fmul(pv.z, fj[q]));
     int tb;
-    float fl, w;
-    weight_fast(px, pv.w, tb, fl, w);
+    float w;
+    weight_fast(px, pv.w, tb, w);
     const float2 y = ld_shared2(off + 8u * (uint32_t)tb);
     acc[q] = fmaf(y.x, w, acc[q]);
     acc[q] = fmaf(y.y, ct::fsub(1.0f, w), acc[q]);
@@ -510,7 +515,7 @@ int* errflag_ptr() {
 }
 
 size_t fwd_smem_bytes(int L, int LS) {
-  return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L) +
+  return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L + (size_t)kFW * kT) +
          sizeof(int) * (2 * kFW + 1) + 24;
 }
 
