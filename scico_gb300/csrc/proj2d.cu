@@ -121,14 +121,14 @@ __device__ __forceinline__ float2 ld_shared2(uint32_t addr) {
 // addressed directly from the float bits of kMagic + key:
 // row_addr = mp_addr - 4 (kMagicBits + base).
 template <bool REV>
-__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, const float* __restrict__ pj,
+__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, float pd1, float fj0,
                                               float R, float inv_width) {
   float A = 0.0f, B = 0.0f;
   int tbp = 0;
 #pragma unroll
   for (int t = 0; t < kT; ++t) {
     const int jj = REV ? kT - 1 - t : t;
-    const float px = ct::fadd(R, pj[jj]);  // pj[jj] = Pdx1 * (j0 + jj), shared by the warp
+    const float px = ct::fadd(R, ct::fmul(pd1, fj0 + (float)jj));
     int tb;
     float w;
     weight_fast(px, inv_width, tb, w);
@@ -186,14 +186,13 @@ struct FwdArgs {
 };
 
 // grid = (n_strips, view groups, batch), block = 256.
-__global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a) {
+__global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs a) {
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* strip = reinterpret_cast<float*>(smem_raw);                 // [32][kRS]
   float* part = strip + kT * kRS;                                    // [kFW][32][LS]
   float* slot = part + kFW * kT * a.LS;                              // [kFW][L]
-  float* pjt = slot + kFW * a.L;                                     // [kFW][32]
-  int* sbase = reinterpret_cast<int*>(pjt + kFW * kT);               // [kFW]
+  int* sbase = reinterpret_cast<int*>(slot + kFW * a.L);             // [kFW]
   int* sspan = sbase + kFW;                                          // [kFW]
   int* scb = sspan + kFW;                                            // strip base of the view
   uint64_t* bar = reinterpret_cast<uint64_t*>(scb + 1);              // 8-B aligned below
@@ -249,6 +248,19 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
   const float fj0 = (float)j0;
   const int vbeg = blockIdx.y * a.vpc;
   const int vend = min(a.nv, vbeg + a.vpc);
+  // this lane's tile row, kept in registers for all the CTA's views
+  float xr[kT];
+  {
+    const float* row = strip + lane * kRS + warp * kT;
+#pragma unroll
+    for (int q = 0; q < kT / 4; ++q) {
+      const float4 f = *reinterpret_cast<const float4*>(row + 4 * q);
+      xr[4 * q] = f.x;
+      xr[4 * q + 1] = f.y;
+      xr[4 * q + 2] = f.z;
+      xr[4 * q + 3] = f.w;
+    }
+  }
 
   for (int v = vbeg; v < vend; ++v) {
     const ViewParams p = load_view(a.views, v);
@@ -264,26 +276,13 @@ __global__ void __launch_bounds__(kFW * 32) k_proj2d_fwd_strips(const FwdArgs a)
         if (lane == 0) atomicOr(a.errflag, 1);
         span = 0;
       } else {
-        float xr[kT];
-        const float* row = strip + lane * kRS + warp * kT;
-#pragma unroll
-        for (int q = 0; q < kT / 4; ++q) {
-          const float4 f = *reinterpret_cast<const float4*>(row + 4 * q);
-          xr[4 * q] = f.x;
-          xr[4 * q + 1] = f.y;
-          xr[4 * q + 2] = f.z;
-          xr[4 * q + 3] = f.w;
-        }
         const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, fi));
         if (fast) {
-          float* pj = pjt + warp * kT;
-          pj[lane] = ct::fmul(p.pd1, fj0 + (float)lane);
-          __syncwarp();
           const uint32_t row_addr = ct::smem_u32(mp) - 4u * (uint32_t)(kMagicBits + base);
           if (p.pd1 >= 0.0f)
-            walk_row_fast<false>(xr, row_addr, pj, R, p.inv_width);
+            walk_row_fast<false>(xr, row_addr, p.pd1, fj0, R, p.inv_width);
           else
-            walk_row_fast<true>(xr, row_addr, pj, R, p.inv_width);
+            walk_row_fast<true>(xr, row_addr, p.pd1, fj0, R, p.inv_width);
         } else {
           if (p.pd1 >= 0.0f)
             walk_row_gen<false>(xr, mp, p, R, fj0, base);
@@ -352,9 +351,12 @@ __global__ void __launch_bounds__(256)
   float* out = sino + ((size_t)b * nv + v) * det;
   for (int bin = threadIdx.x; bin < det; bin += blockDim.x) {
     float acc = 0.0f;
+#pragma unroll 8
     for (int s = 0; s < n_strips; ++s) {
       const int off = bin - sb[s];
-      if ((unsigned)off < (unsigned)cspan) acc += __ldg(pb + s * sstride + off);
+      const bool in = (unsigned)off < (unsigned)cspan;
+      const float v = __ldg(pb + s * sstride + (in ? off : 0));
+      acc += in ? v : 0.0f;
     }
     out[bin] = acc;
   }
@@ -515,7 +517,7 @@ int* errflag_ptr() {
 }
 
 size_t fwd_smem_bytes(int L, int LS) {
-  return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L + (size_t)kFW * kT) +
+  return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L) +
          sizeof(int) * (2 * kFW + 1) + 24;
 }
 
