@@ -16,10 +16,17 @@
 //   k_itstat      writes the previous iteration's itstat record
 //   A^T, k_lhs_finish<INIT>   lhs(x) = c A^T A x + rho D^T D x, r = rhs - lhs(x),
 //                 p = r, CG scalars (num, ||b||, tolerance) in float64
-//   CG x cg_maxiter: A p, A^T, k_lhs_finish<PAP> (Ap, <p,Ap>), CG update,
-//                 direction -- every launch is a no-op once CG has converged
+//   CG loop       A p, A^T, k_lhs_finish<PAP> (Ap, <p,Ap>), CG update,
+//                 direction.  In the graph the loop is a conditional WHILE
+//                 node whose condition the device sets (CG start and each
+//                 update), so it runs exactly the reference's number of CG
+//                 iterations; without a graph, cg_maxiter copies are launched
+//                 and become no-ops once CG has converged
 //   k_zu          Dx, z_i = prox(Dx + u_i), u_i += Dx - z_i, primal residual
 //                 and g_i(z_i) partial sums
+// lhs(x) and A x are kept from the last CG start while x is unchanged (no CG
+// step ran since): the deterministic kernels would recompute the same bits,
+// so the projections of x are skipped then.
 // The reference evaluates the itstat quantities with extra operator
 // applications after each step; here they are fused into the kernels that
 // already read the operands, and the x-dependent ones are taken from the
@@ -46,6 +53,7 @@ enum Slot {
   S_G1 = 4,       // ||z_l1||_1 of the last z/u update
   S_HAVE_PREV = 5,
   S_REC = 6,      // records written in this call
+  S_XCLEAN = 7,   // 1 while lhs(x) and A x in the workspace belong to the current x
   S_CG = 16,      // CT_CG_NSCALARS doubles
   S_COUNT = 32
 };
@@ -153,6 +161,7 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT)
     k_resid2(const float* __restrict__ sino, const float* __restrict__ y, size_t n,
              double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+  if (slots[S_XCLEAN] != 0.0) return;  // x unchanged: S_RESID2 is current
   double acc[1] = {0.0};
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
     const float d = ct::fsub(y[e], sino[e]);
@@ -186,24 +195,35 @@ __global__ void k_itstat(double* __restrict__ itstat, double* __restrict__ slots
 }
 
 // lhs(q) = sum_i rho D^T D q + c A^T A q, from the adjoint output (or its
-// view splits).  INIT: r = rhs - lhs(q), p = r and the CG start scalars.
-// PAP: Ap = lhs(q) and <q, Ap>.
+// view splits).  INIT (q = x): r = rhs - lhs(x), p = r and the CG start
+// scalars; lhs(x) is stored in lhsx, or read from it while x is unchanged
+// (slots[S_XCLEAN]).  PAP: Ap = lhs(q) and <q, Ap>.  In a graph with a
+// conditional CG loop, INIT sets the loop condition.
 template <bool INIT>
 __global__ void __launch_bounds__(NT)
     k_lhs_finish(const float* __restrict__ adj, int nsplit, const float* __restrict__ q, int R, int C,
                  TermParams tp, float* __restrict__ out, const float* __restrict__ rhs,
-                 float* __restrict__ p, double* __restrict__ cg, double tol, double atol, int maxiter,
-                 double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+                 float* __restrict__ p, float* __restrict__ lhsx, double* __restrict__ slots,
+                 double* __restrict__ cg, double tol, double atol, int maxiter,
+                 double* __restrict__ partials, unsigned int* __restrict__ ticket,
+                 cudaGraphConditionalHandle cond, int use_cond) {
   if (!INIT && cg[CT_CG_DONE] != 0.0) return;
+  const bool cached = INIT && slots[S_XCLEAN] != 0.0;
   const size_t N = (size_t)R * C;
   double acc[2] = {0.0, 0.0};
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-    float a = adj[e];
-    for (int k = 1; k < nsplit; ++k) a = ct::fadd(a, adj[(size_t)k * N + e]);
-    const float g = dtd_at(q, pix_i(e, C), (int)(e % C), R, C);
-    float v = ct::fmul(tp.rho, g);
-    for (int t = 1; t < tp.ng; ++t) v = ct::fadd(v, ct::fmul(tp.rho, g));
-    v = ct::fadd(v, ct::fmul(tp.c, a));
+    float v;
+    if (cached) {
+      v = lhsx[e];
+    } else {
+      float a = adj[e];
+      for (int k = 1; k < nsplit; ++k) a = ct::fadd(a, adj[(size_t)k * N + e]);
+      const float g = dtd_at(q, pix_i(e, C), (int)(e % C), R, C);
+      v = ct::fmul(tp.rho, g);
+      for (int t = 1; t < tp.ng; ++t) v = ct::fadd(v, ct::fmul(tp.rho, g));
+      v = ct::fadd(v, ct::fmul(tp.c, a));
+      if (INIT) lhsx[e] = v;
+    }
     if (INIT) {
       const float b = rhs[e];
       const float re = ct::fsub(b, v);
@@ -230,7 +250,10 @@ __global__ void __launch_bounds__(NT)
       cg[CT_CG_ITERS] = 0.0;
       cg[CT_CG_MAXITER] = (double)maxiter;
       cg[CT_CG_RAN] = 0.0;
-      cg[CT_CG_DONE] = (maxiter <= 0 || !(tot[0] > thr * thr)) ? 1.0 : 0.0;
+      const bool done = maxiter <= 0 || !(tot[0] > thr * thr);
+      cg[CT_CG_DONE] = done ? 1.0 : 0.0;
+      slots[S_XCLEAN] = 1.0;
+      if (use_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
     } else {
       cg[CT_CG_PAP] = tot[0];
     }
@@ -298,12 +321,14 @@ __global__ void __launch_bounds__(NT)
     slots[S_G21] = tot[1];
     slots[S_G1] = tot[2];
     slots[S_HAVE_PREV] = 1.0;
+    if (slots[S_CG + CT_CG_ITERS] > 0.0) slots[S_XCLEAN] = 0.0;  // CG moved x
   }
 }
 
 __global__ void k_reset_call(double* __restrict__ slots) {
   slots[S_REC] = 0.0;
   slots[S_HAVE_PREV] = 0.0;
+  slots[S_XCLEAN] = 0.0;  // the caller may have changed x between calls
 }
 
 // ---------------------------------------------------------------------------
@@ -313,7 +338,7 @@ struct Layout {
   int ng;
   ct::Proj2dPlan plan;
   size_t off_slots, off_red, off_atyc, off_rhs, off_r, off_p, off_ap, off_adj, off_sino, off_z, off_u,
-      off_dz, off_fwd, off_adjpart, total;
+      off_dz, off_fwd, off_adjpart, off_lhsx, off_sinox, total;
 };
 
 Layout layout(const ct_admm_tv_desc* d) {
@@ -343,6 +368,8 @@ Layout layout(const ct_admm_tv_desc* d) {
   L.off_dz = take(L.N * 8 * (size_t)(L.ng > 0 ? L.ng : 1));
   L.off_fwd = take(L.plan.fwd_bytes);
   L.off_adjpart = take(L.plan.adj_bytes > 0 ? L.plan.adj_bytes : 256);
+  L.off_lhsx = take(L.N * 4);
+  L.off_sinox = take(L.S * 4);
   L.total = o;
   return L;
 }
@@ -381,70 +408,89 @@ struct Ctx {
     if (_st != CT_OK) return _st;    \
   } while (0)
 
-ct_status project(const Ctx& c, const float* img, cudaStream_t s, const double* skip) {
-  return ct::proj2d_fwd_launch(&c.d->geom, c.L.plan, img, c.at<float>(c.L.off_sino), 1,
-                               c.at<float>(c.L.off_fwd), s, skip);
+ct_status project(const Ctx& c, const float* img, float* sino, cudaStream_t s, const double* skip) {
+  return ct::proj2d_fwd_launch(&c.d->geom, c.L.plan, img, sino, 1, c.at<float>(c.L.off_fwd), s, skip);
 }
 
-// A^T of the sinogram buffer into the adjoint buffer (or its view splits);
-// returns the buffer to read.
-const float* backproject(const Ctx& c, cudaStream_t s, const double* skip, ct_status& st) {
+// A^T of a sinogram into the adjoint buffer (or its view splits); returns
+// the buffer to read.
+const float* backproject(const Ctx& c, const float* sino, cudaStream_t s, const double* skip, ct_status& st) {
   float* adj = c.at<float>(c.L.off_adj);
   float* part = c.at<float>(c.L.off_adjpart);
-  st = ct::proj2d_adj_launch(&c.d->geom, c.L.plan, c.at<float>(c.L.off_sino), adj, part, 1, s, skip);
+  st = ct::proj2d_adj_launch(&c.d->geom, c.L.plan, sino, adj, part, 1, s, skip);
   return c.L.plan.nsplit > 1 ? part : adj;
 }
 
-// Kernels of one ADMM iteration (also the body of the captured graph).
-ct_status enqueue_iteration(const Ctx& c, cudaStream_t s) {
+// The three phases of one ADMM iteration.  cond/use_cond: the conditional
+// handle of the graph's CG loop (use_cond = 0 outside such a graph).
+ct_status enqueue_pre(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
   const int R = c.d->geom.rows, C = c.d->geom.cols;
-  const int K = c.d->cg_maxiter;
   float* r = c.at<float>(c.L.off_r);
   float* p = c.at<float>(c.L.off_p);
-  float* ap = c.at<float>(c.L.off_ap);
   float* rhs = c.at<float>(c.L.off_rhs);
-  float* z = c.at<float>(c.L.off_z);
-  float* u = c.at<float>(c.L.off_u);
-  float* dz = c.at<float>(c.L.off_dz);
-  const double* done = c.cg() + CT_CG_DONE;
-
-  k_rhs<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_atyc), z, u, dz, rhs, R, C, c.tp, c.slots(), c.partials(),
-                          c.ticket());
+  float* sinox = c.at<float>(c.L.off_sinox);
+  const double* clean = c.slots() + S_XCLEAN;
+  k_rhs<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
+                          c.at<float>(c.L.off_dz), rhs, R, C, c.tp, c.slots(), c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_rhs"));
-  CT_TRY(project(c, c.x, s, nullptr));
-  k_resid2<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_sino), c.y, c.L.S, c.slots(), c.partials(), c.ticket());
+  CT_TRY(project(c, c.x, sinox, s, clean));
+  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.L.S, c.slots(), c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_resid2"));
   k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.d->maxiter, c.d->loss_scale, c.d->lam_l21, c.d->lam_l1, 0);
   CT_TRY(ct::launch_check("k_itstat"));
   ct_status st;
-  const float* adj = backproject(c, s, nullptr, st);
+  const float* adj = backproject(c, sinox, s, clean, st);
   CT_TRY(st);
-  k_lhs_finish<true><<<NB, NT, 0, s>>>(adj, c.L.plan.nsplit, c.x, R, C, c.tp, r, rhs, p, c.cg(),
-                                       c.d->cg_tol, c.d->cg_atol, K, c.partials(), c.ticket());
-  CT_TRY(ct::launch_check("k_lhs_finish<init>"));
-  for (int it = 0; it < K; ++it) {
-    CT_TRY(project(c, p, s, done));
-    adj = backproject(c, s, done, st);
-    CT_TRY(st);
-    k_lhs_finish<false><<<NB, NT, 0, s>>>(adj, c.L.plan.nsplit, p, R, C, c.tp, ap, nullptr, nullptr,
-                                          c.cg(), 0.0, 0.0, K, c.partials(), c.ticket());
-    CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
-    CT_TRY(ct::cg_update_launch(c.x, r, p, ap, c.L.N, c.cg(), c.ws + c.L.off_red, s));
-    CT_TRY(ct::cg_direction_launch(p, r, c.L.N, c.cg(), c.ws + c.L.off_red, s));
-  }
-  k_zu<<<NB, NT, 0, s>>>(c.x, z, u, dz, R, C, c.tp, c.slots(), c.partials(), c.ticket());
+  k_lhs_finish<true><<<NB, NT, 0, s>>>(adj, c.L.plan.nsplit, c.x, R, C, c.tp, r, rhs, p,
+                                       c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.d->cg_tol,
+                                       c.d->cg_atol, c.d->cg_maxiter, c.partials(), c.ticket(), cond, use_cond);
+  return ct::launch_check("k_lhs_finish<init>");
+}
+
+ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
+  const int R = c.d->geom.rows, C = c.d->geom.cols;
+  float* r = c.at<float>(c.L.off_r);
+  float* p = c.at<float>(c.L.off_p);
+  float* ap = c.at<float>(c.L.off_ap);
+  float* sino = c.at<float>(c.L.off_sino);
+  const double* done = c.cg() + CT_CG_DONE;
+  CT_TRY(project(c, p, sino, s, done));
+  ct_status st;
+  const float* adj = backproject(c, sino, s, done, st);
+  CT_TRY(st);
+  k_lhs_finish<false><<<NB, NT, 0, s>>>(adj, c.L.plan.nsplit, p, R, C, c.tp, ap, nullptr, nullptr, nullptr,
+                                        c.slots(), c.cg(), 0.0, 0.0, c.d->cg_maxiter, c.partials(), c.ticket(),
+                                        0, 0);
+  CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
+  CT_TRY(ct::cg_update_launch(c.x, r, p, ap, c.L.N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond));
+  return ct::cg_direction_launch(p, r, c.L.N, c.cg(), c.ws + c.L.off_red, s);
+}
+
+ct_status enqueue_post(const Ctx& c, cudaStream_t s) {
+  const int R = c.d->geom.rows, C = c.d->geom.cols;
+  k_zu<<<NB, NT, 0, s>>>(c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), R, C,
+                         c.tp, c.slots(), c.partials(), c.ticket());
   return ct::launch_check("k_zu");
+}
+
+// One iteration as plain launches (no graph): cg_maxiter CG steps that turn
+// into no-ops once CG has converged.
+ct_status enqueue_iteration(const Ctx& c, cudaStream_t s) {
+  CT_TRY(enqueue_pre(c, s, 0, 0));
+  for (int it = 0; it < c.d->cg_maxiter; ++it) CT_TRY(enqueue_cg_step(c, s, 0, 0));
+  return enqueue_post(c, s);
 }
 
 // Statistics of the last iteration: dual residual (k_rhs), objective.
 ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
   const int R = c.d->geom.rows, C = c.d->geom.cols;
+  float* sinox = c.at<float>(c.L.off_sinox);
   k_rhs<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
                           c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), R, C, c.tp, c.slots(),
                           c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_rhs"));
-  CT_TRY(project(c, c.x, s, nullptr));
-  k_resid2<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_sino), c.y, c.L.S, c.slots(), c.partials(), c.ticket());
+  CT_TRY(project(c, c.x, sinox, s, c.slots() + S_XCLEAN));
+  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.L.S, c.slots(), c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_resid2"));
   k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.d->maxiter, c.d->loss_scale, c.d->lam_l21, c.d->lam_l1, 1);
   return ct::launch_check("k_itstat");
@@ -476,6 +522,59 @@ size_t make_key(const Ctx& c, unsigned char* key) {
   return n;
 }
 
+// The iteration graph: pre-phase kernels, then a conditional WHILE node
+// whose body is one CG step (the CG start and every CG update set the
+// condition on the device: run while CG has not converged), then the z/u
+// update.  Each phase is stream-captured into its place in the graph.
+ct_status build_iteration_graph(const Ctx& c, cudaStream_t cs, cudaGraph_t& graph) {
+  CT_TRY(ct::cuda_check(cudaGraphCreate(&graph, 0), "graph create"));
+  cudaGraphConditionalHandle cond = 0;
+  CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&cond, graph, 0, cudaGraphCondAssignDefault),
+                        "conditional handle"));
+  // pre phase
+  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0,
+                                                      cudaStreamCaptureModeThreadLocal),
+                        "capture pre"));
+  ct_status st = enqueue_pre(c, cs, cond, 1);
+  cudaStreamCaptureStatus cst;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  cudaError_t ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &deps, nullptr, &ndeps);
+  cudaGraphNode_t pre_tail[8];
+  const size_t npre = ndeps < 8 ? ndeps : 8;
+  for (size_t k = 0; ce == cudaSuccess && k < npre; ++k) pre_tail[k] = deps[k];
+  cudaGraph_t out = nullptr;
+  cudaError_t ce2 = cudaStreamEndCapture(cs, &out);
+  CT_TRY(st);
+  CT_TRY(ct::cuda_check(ce, "capture info"));
+  CT_TRY(ct::cuda_check(ce2, "end capture pre"));
+  if (ndeps > 8) return ct::fail(CT_ERR_CUDA, "unexpected capture frontier of %zu nodes", ndeps);
+  // conditional WHILE node for the CG loop
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode = nullptr;
+  CT_TRY(ct::cuda_check(cudaGraphAddNode(&cnode, graph, pre_tail, nullptr, npre, &cp), "conditional node"));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                                      cudaStreamCaptureModeThreadLocal),
+                        "capture body"));
+  st = enqueue_cg_step(c, cs, cond, 1);
+  ce2 = cudaStreamEndCapture(cs, &out);
+  CT_TRY(st);
+  CT_TRY(ct::cuda_check(ce2, "end capture body"));
+  // post phase after the loop
+  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, graph, &cnode, nullptr, 1,
+                                                      cudaStreamCaptureModeThreadLocal),
+                        "capture post"));
+  st = enqueue_post(c, cs);
+  ce2 = cudaStreamEndCapture(cs, &out);
+  CT_TRY(st);
+  return ct::cuda_check(ce2, "end capture post");
+}
+
 ct_status run_graph(const Ctx& c, cudaStream_t caller) {
   std::lock_guard<std::mutex> lock(g_cache.m);
   int dev = 0;
@@ -497,16 +596,12 @@ ct_status run_graph(const Ctx& c, cudaStream_t caller) {
       g_cache.exec = nullptr;
     }
     cudaGraph_t graph = nullptr;
-    CT_TRY(ct::cuda_check(cudaStreamBeginCapture(g_cache.cs, cudaStreamCaptureModeThreadLocal),
-                          "begin capture"));
-    ct_status st = enqueue_iteration(c, g_cache.cs);
-    cudaError_t ce = cudaStreamEndCapture(g_cache.cs, &graph);
+    ct_status st = build_iteration_graph(c, g_cache.cs, graph);
     if (st != CT_OK) {
       if (graph) cudaGraphDestroy(graph);
       return st;
     }
-    CT_TRY(ct::cuda_check(ce, "end capture"));
-    ce = cudaGraphInstantiate(&g_cache.exec, graph, 0);
+    cudaError_t ce = cudaGraphInstantiate(&g_cache.exec, graph, 0);
     cudaGraphDestroy(graph);
     CT_TRY(ct::cuda_check(ce, "graph instantiate"));
     memcpy(g_cache.key, key, kl);

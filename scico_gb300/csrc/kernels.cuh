@@ -33,8 +33,11 @@ ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
                             float* part, int batch, cudaStream_t s, const double* skip);
 
 // ---- CG vector steps (vec.cu) ----------------------------------------------
+// cond/use_cond: in a graph with a conditional WHILE CG loop, the update sets
+// the loop condition to "not converged".
 ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, size_t n,
-                           double* scalars, void* red_ws, cudaStream_t s);
+                           double* scalars, void* red_ws, cudaStream_t s,
+                           cudaGraphConditionalHandle cond = 0, int use_cond = 0);
 ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, void* red_ws,
                               cudaStream_t s);
 

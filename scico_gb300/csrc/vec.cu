@@ -76,11 +76,17 @@ __global__ void __launch_bounds__(NT)
 }
 
 // alpha = num/pAp; x += alpha p; r -= alpha Ap; num' = <r,r>.
+// In a CUDA graph whose CG loop is a conditional WHILE node (use_cond != 0)
+// the last block also sets the loop condition to "not DONE".
 __global__ void __launch_bounds__(NT)
     k_cg_update(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
                 const float* __restrict__ Ap, size_t n, double* __restrict__ s,
-                double* __restrict__ partials, unsigned int* __restrict__ ticket) {
-  if (s[CT_CG_DONE] != 0.0) return;  // uniform over the grid
+                double* __restrict__ partials, unsigned int* __restrict__ ticket,
+                cudaGraphConditionalHandle cond, int use_cond) {
+  if (s[CT_CG_DONE] != 0.0) {  // uniform over the grid
+    if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
   const double alpha = s[CT_CG_NUM] / s[CT_CG_PAP];
   const float af = (float)alpha;
   double rr = 0.0;
@@ -102,7 +108,9 @@ __global__ void __launch_bounds__(NT)
     // The direction update still runs for this iteration (reference order);
     // DONE takes effect from the next update on.
     s[CT_CG_RAN] = 1.0;
-    if (!(trr > s[CT_CG_TOL2]) || it >= s[CT_CG_MAXITER]) s[CT_CG_DONE] = 1.0;
+    const bool done = !(trr > s[CT_CG_TOL2]) || it >= s[CT_CG_MAXITER];
+    if (done) s[CT_CG_DONE] = 1.0;
+    if (use_cond) cudaGraphSetConditional(cond, done ? 0u : 1u);
   }
 }
 
@@ -165,7 +173,7 @@ ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap, int6
   ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_update", w);
   if (st != CT_OK) return st;
   k_cg_update<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(x, r, p, Ap, (size_t)n, scalars,
-                                                                  w.partials, w.ticket);
+                                                                  w.partials, w.ticket, 0, 0);
   return ct::launch_check("k_cg_update");
 }
 
@@ -184,10 +192,11 @@ ct_status ct_cg_direction(float* p, const float* r, int64_t n, double* scalars, 
 namespace ct {
 
 ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, size_t n,
-                           double* scalars, void* red_ws, cudaStream_t s) {
+                           double* scalars, void* red_ws, cudaStream_t s, cudaGraphConditionalHandle cond,
+                           int use_cond) {
   unsigned int* ticket = static_cast<unsigned int*>(red_ws);
   double* partials = reinterpret_cast<double*>(static_cast<char*>(red_ws) + 256);
-  k_cg_update<<<kReduceBlocks, NT, 0, s>>>(x, r, p, Ap, n, scalars, partials, ticket);
+  k_cg_update<<<kReduceBlocks, NT, 0, s>>>(x, r, p, Ap, n, scalars, partials, ticket, cond, use_cond);
   return launch_check("k_cg_update");
 }
 
