@@ -330,12 +330,11 @@ def run_gpu(args):
     peak, peak_kind = _hbm_peak()
     achieved = alg_fwd / t_fwd / 1e9
     traffic = None
-    prof = ROOT / "profiles" / "ncu_traffic.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get("proj2d_fwd_c2_bytes_per_launch")
-        except Exception:
-            traffic = None
+    prof = ROOT / "profiles" / f"proj2d_fwd_{args.config}.md"
+    if prof.exists():  # dram__bytes_read.sum + dram__bytes_write.sum of one call (ncu)
+        for line in prof.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_call:"):
+                traffic = int(line.split(":")[1])
 
     # ---- CPU baseline (rank 0, N = 1) -----------------------------------------
     cpu = None
