@@ -100,6 +100,25 @@ ct_status ct_proj2d_fwd(const ct_geom2d* g, const float* img, float* sino,
                         ct_stream_t stream);
 
 /*
+ * Allocation-free variant of ct_proj2d_fwd, for callers that cannot
+ * allocate device memory when they project (inside a stream capture they do
+ * not own, in plugin hosts that give a custom call no allocator or scratch
+ * buffer, in real-time loops that forbid allocation after start-up).  No
+ * counterpart in the reference: scico's projector allocates through XLA.
+ * The scratch is a fixed 16 MiB array in the library's device memory, held
+ * by every GPU that loads the library until the process exits; projections
+ * whose scratch (ct_proj2d_workspace's fwd_bytes) exceeds 16 MiB are
+ * rejected with CT_ERR_UNSUPPORTED.  All calls share that array: calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Nothing in the array needs clearing between
+ * calls.  The first call on a device looks up the array's address for that
+ * device; make it before any stream capture.  Calls no cudaMalloc or cudaFree.
+ */
+ct_status ct_proj2d_fwd_noalloc(const ct_geom2d* g, const float* img,
+                                float* sino, int32_t batch,
+                                ct_stream_t stream);
+
+/*
  * img[b] = A^T sino[b]  (XRayTransform2D.back_project, :148-156,
  * _back_project :267-306).  Pixel-driven gather with the forward's weights,
  * views summed in a fixed order, no atomics.

@@ -124,6 +124,7 @@ _SIGNATURES = {
     "ct_proj2d_views": (ctypes.c_int, [P, c_int32, c_float, c_float, c_float, c_float, c_float, P, P]),
     "ct_proj2d_workspace": (ctypes.c_int, [P, c_int32, P, P]),
     "ct_proj2d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_proj2d_fwd_noalloc": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_proj2d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_fd_out_count": (ctypes.c_int, [P, P]),
     "ct_fd_fwd": (ctypes.c_int, [P, P, P, c_int32, P]),

@@ -28,6 +28,7 @@
 // |Px| < 2^22, checked per tile and view, with a floorf path otherwise):
 // full-rate FP32 operations instead of conversion instructions.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "tma.cuh"
@@ -697,6 +698,65 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img, int32
   const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
   k_sum_splits<<<blocks, 256, 0, s>>>(part, img, n, p.nsplit, n);
   return ct::launch_check("k_sum_splits");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free forward projection.
+//
+// Some callers cannot allocate device memory when they project: code that
+// runs inside a stream capture it does not own, plugin hosts that hand a
+// custom call no allocator and no scratch buffer, and real-time loops that
+// forbid allocation once they are running.  ct_proj2d_fwd_noalloc gives them
+// the forward projection with its scratch in a fixed array in the library's
+// own device memory (kNoallocScratchBytes, held by every GPU that loads the
+// library until the process exits).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocScratchBytes = 16u << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_fwd_scratch[kNoallocScratchBytes];
+
+// Device address of g_fwd_scratch, looked up once per device with that
+// device current (host code only has a stand-in for the symbol).
+float* noalloc_scratch() {
+  static std::mutex m;
+  static float* cached[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(m);
+  if (!cached[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_fwd_scratch) != cudaSuccess) return nullptr;
+    cached[dev] = static_cast<float*>(p);
+  }
+  return cached[dev];
+}
+
+}  // namespace
+
+extern "C" {
+
+ct_status ct_proj2d_fwd_noalloc(const ct_geom2d* g, const float* img, float* sino, int32_t batch,
+                                ct_stream_t stream) {
+  ct_status st = ct::proj2d_check(g, "ct_proj2d_fwd_noalloc");
+  if (st != CT_OK) return st;
+  if (!img || !sino) return ct::fail(CT_ERR_INVALID_ARG, "ct_proj2d_fwd_noalloc: null array");
+  if (batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_proj2d_fwd_noalloc: batch=%d", batch);
+  const ct::Proj2dPlan p = ct::proj2d_plan(g, batch);
+  if (p.fwd_bytes > kNoallocScratchBytes)
+    return ct::fail(CT_ERR_UNSUPPORTED,
+                    "ct_proj2d_fwd_noalloc: this projection needs %zu bytes of scratch, more than the "
+                    "%zu-byte built-in array; use ct_proj2d_fwd with a workspace",
+                    p.fwd_bytes, kNoallocScratchBytes);
+  float* scratch = noalloc_scratch();
+  if (!scratch) return ct::fail(CT_ERR_CUDA, "ct_proj2d_fwd_noalloc: scratch address lookup failed");
+  st = ct::proj2d_prepare(p);
+  if (st != CT_OK) return st;
+  // Every scratch element the second pass reads is written by the first
+  // pass of the same call, so nothing needs clearing between calls.
+  return ct::proj2d_fwd_launch(g, p, img, sino, batch, scratch, ct::as_stream(stream), nullptr);
 }
 
 // Diagnostic: returns (and clears) the projector's internal check word.
