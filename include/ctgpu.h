@@ -128,6 +128,78 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
                         ct_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* 3D parallel-beam projector (XRayTransform3D)                             */
+/* ------------------------------------------------------------------------ */
+
+/* Floats per view in the table ct_proj3d_views writes: the (2,4) projection
+ * matrix row-major (entries 0..7), the axis along which the ray direction
+ * has its largest component (entry 8, as a float), three unused. */
+#define CT_VIEW3D_STRIDE 12
+/* uint16 entries per view in the walk-order table of CT_PROJ3D_AXIS0. */
+#define CT_PROJ3D_ORDER 1024
+
+/* Geometry kinds.  AXIS0: every view leaves volume axis 0 on detector rows
+ * (M[0][1] = M[0][2] = M[1][0] = 0, |M[1][1]|, |M[1][2]| <= 1) and, in every
+ * view, slice i lands on detector row i + row_offset with to_next = 0.5, so
+ * only the ul/ll taps carry weight --
+ * the rotation-about-axis-0 geometry of matrices_from_euler_angles(..., "X",
+ * ...) with equal slice and detector-row counts or an even difference.
+ * The AXIS0 kernels compute each column weight once per view and apply it to
+ * every slice.  GENERAL: any other matrices. */
+#define CT_PROJ3D_GENERAL 0
+#define CT_PROJ3D_AXIS0 1
+
+/*
+ * Host: build the per-view tables of a geometry (XRayTransform3D.__init__
+ * keeps the (V,2,4) matrices as float32, scico/linop/xray/_xray3d.py:80) and
+ * classify it.  matrices: host (n_views,2,4) float32.  views_out: host
+ * n_views*CT_VIEW3D_STRIDE floats.  order_out: host n_views*CT_PROJ3D_ORDER
+ * uint16 (the AXIS0 walk order of a 32x32 pixel tile, ordered along the
+ * detector), or NULL, in which case the kind is always GENERAL.
+ * Fails with CT_ERR_UNSUPPORTED when a matrix has parallel rows (a view
+ * that maps the volume onto a line).
+ */
+ct_status ct_proj3d_views(const float* matrices, int32_t n_views,
+                          const int32_t* shape, const int32_t* det_shape,
+                          float* views_out, uint16_t* order_out,
+                          int32_t* kind_out, int32_t* row_offset_out);
+
+typedef struct ct_geom3d {
+  int32_t shape[3];        /* volume (n0, n1, n2), C order              */
+  int32_t det_shape[2];    /* detector (rows, cols)                     */
+  int32_t n_views;
+  int32_t kind;            /* CT_PROJ3D_GENERAL or CT_PROJ3D_AXIS0      */
+  int32_t row_offset;      /* AXIS0: detector row of slice i - i        */
+  const float* views;      /* device, n_views*CT_VIEW3D_STRIDE          */
+  const uint16_t* order;   /* device, n_views*CT_PROJ3D_ORDER (AXIS0)   */
+} ct_geom3d;
+
+/* Workspace bytes that ct_proj3d_fwd / ct_proj3d_adj need for `batch`. */
+ct_status ct_proj3d_workspace(const ct_geom3d* g, int32_t batch,
+                              size_t* fwd_bytes, size_t* adj_bytes);
+
+/*
+ * proj[b] = A vol[b]  (XRayTransform3D.project / _project / _project_single,
+ * _xray3d.py:95-159; weights _calc_weights :206-266).  vol (batch, n0, n1, n2)
+ * -> proj (batch, n_views, rows, cols).  The reference scatters four taps
+ * per voxel with mode="drop"; here every detector pixel gathers its taps
+ * (GENERAL) or each slice's column contributions are accumulated by one
+ * owner in a fixed order (AXIS0): no atomics, deterministic.
+ */
+ct_status ct_proj3d_fwd(const ct_geom3d* g, const float* vol, float* proj,
+                        int32_t batch, void* workspace, size_t workspace_bytes,
+                        ct_stream_t stream);
+
+/*
+ * vol[b] = A^T proj[b]  (XRayTransform3D.back_project / _back_project /
+ * _back_project_single, :161-204).  Voxel-driven gather with the forward's
+ * weights, views summed in a fixed order.
+ */
+ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol,
+                        int32_t batch, void* workspace, size_t workspace_bytes,
+                        ct_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Finite differences (FiniteDifference / SingleAxisFiniteDifference)       */
 /* ------------------------------------------------------------------------ */
 

@@ -34,7 +34,10 @@ CT_ERR_WORKSPACE = 7
 CT_ERR_NO_DEVICE = 8
 
 CT_VIEW2D_STRIDE = 8
-CT_VIEW3D_STRIDE = 8
+CT_VIEW3D_STRIDE = 12
+CT_PROJ3D_ORDER = 1024
+CT_PROJ3D_GENERAL = 0
+CT_PROJ3D_AXIS0 = 1
 
 # CG scalar slots (double[16])
 CT_CG_NUM = 0
@@ -81,10 +84,12 @@ class Geom2D(ctypes.Structure):
 class Geom3D(ctypes.Structure):
     _fields_ = [
         ("shape", c_int32 * 3),
-        ("n_views", c_int32),
         ("det_shape", c_int32 * 2),
+        ("n_views", c_int32),
+        ("kind", c_int32),
+        ("row_offset", c_int32),
         ("views", c_void_p),
-        ("axis0_rotation", c_int32),
+        ("order", c_void_p),
     ]
 
 
@@ -126,6 +131,10 @@ _SIGNATURES = {
     "ct_proj2d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_proj2d_fwd_noalloc": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_proj2d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_proj3d_views": (ctypes.c_int, [P, c_int32, P, P, P, P, P, P]),
+    "ct_proj3d_workspace": (ctypes.c_int, [P, c_int32, P, P]),
+    "ct_proj3d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_proj3d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_fd_out_count": (ctypes.c_int, [P, P]),
     "ct_fd_fwd": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_fd_adj": (ctypes.c_int, [P, P, P, c_int32, P]),

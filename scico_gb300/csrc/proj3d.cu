@@ -1,0 +1,824 @@
+// 3D parallel-beam X-ray projector: XRayTransform3D.project / back_project
+// (scico/linop/xray/_xray3d.py:95-266) for sm_103a.
+//
+// Weight model (_calc_weights, :206-266).  Voxel (i0, i1, i2) has its centre
+// at x = (i0+0.5, i1+0.5, i2+0.5) and lands on the detector at
+//   Px_r = ((M[r][0]*x0 + M[r][1]*x1) + M[r][2]*x2) + M[r][3]      (r = 0, 1)
+// in float32, each operation rounded.  left = Px - 0.25,
+// to_next t = min(ceil(left) - left, 0.5), ul = floor(left), and the four taps
+//   (ul0,   ul1)   t0*t1*4          (ul0+1, ul1)   (0.5-t0)*t1*4
+//   (ul0,   ul1+1) t0*(0.5-t1)*4    (ul0+1, ul1+1) (0.5-t0)*(0.5-t1)*4
+// each zeroed when its detector pixel is out of range.  Every kernel here
+// evaluates these expressions with the same float32 operations in the same
+// order (no contraction), so forward and adjoint use bit-identical weights.
+//
+// Two geometry kinds (ct_proj3d_views classifies):
+//  * AXIS0 -- rotation about volume axis 0, slice i on detector row
+//    i + row_offset with t0 = 0.5.  Then ul = 2*t1, ll = 2*(0.5-t1) (both
+//    exact) and the two other taps are zero, and the column weights of pixel
+//    (i1, i2) are the same for every slice.  The kernels compute each column
+//    weight once per view and tile and apply it to 32 slices at a time:
+//      forward  k_p3_ax0_fwd: lanes = slices; a warp walks a 32x32 pixel tile
+//               (staged in shared memory, [pixel][slice]) in the per-view
+//               detector order of the order table, carrying the two open bins
+//               in registers and flushing into a per-warp [bin][slice]
+//               accumulator; accumulators go to a [group][view][col][slice]
+//               buffer that k_p3_ax0_rows transposes into the sinogram.
+//      adjoint  k_p3_ax0_adj: lanes = pixels along axis 2, 32 slices of
+//               accumulators per thread; the view's detector rows of the
+//               CTA's slices are staged as (y[c], y[c+1]) pairs, read with
+//               one 8-byte shared load per slice.
+//  * GENERAL -- any matrices.  The adjoint is voxel-driven (four gathers per
+//    view, as the reference's _back_project_single).  The forward is
+//    detector-driven: each detector pixel marches along the axis on which
+//    the ray direction is largest and, in each plane, visits the voxels whose
+//    footprint can cover it (an exact membership test on the rounded ul
+//    decides), so each output has a single owner and no atomics are needed.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace ct {
+namespace {
+
+constexpr int kVT = CT_VIEW3D_STRIDE;
+constexpr int kOrd = CT_PROJ3D_ORDER;
+constexpr int kTile = 32;  // AXIS0 forward pixel tile edge (kTile*kTile == kOrd)
+constexpr int kSvStride = 33;  // shared [pixel][slice] row stride (floats)
+constexpr int kTabChunk = 128;  // walk-table entries built per warp per pass
+constexpr int kFwdViewsPerCta = 16;
+constexpr int kAccSpan = 2 * (32 - 1) + 6;  // accumulator bins per warp: 31(|m11|+|m12|) + 5
+constexpr int kAdjRows = 16;  // AXIS0 adjoint tile: 16 (axis 1) x 32 (axis 2) pixels
+constexpr int kAdjTargetCtas = 304;
+constexpr int kGenViewChunk = 64;
+
+static_assert(kTile * kTile == kOrd, "order table covers one tile");
+
+// Device error word of the 3D kernels' internal checks (bit 0: forward
+// accumulator span, bit 1: adjoint window span).
+__device__ int g_proj3d_err = 0;
+
+int* errflag3_ptr() {
+  static int* cached[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!cached[dev]) {
+    int* p = nullptr;
+    if (cudaGetSymbolAddress((void**)&p, g_proj3d_err) != cudaSuccess) return nullptr;
+    cached[dev] = p;
+  }
+  return cached[dev];
+}
+
+// Detector coordinate of voxel centre (x0, x1, x2) on detector axis r of a
+// view (_xray3d.py:214-219), rounded like the reference's float32 expression.
+__device__ __forceinline__ float px3(float m0, float m1, float m2, float m3, float x0, float x1,
+                                     float x2) {
+  return fadd(fadd(fadd(fmul(m0, x0), fmul(m1, x1)), fmul(m2, x2)), m3);
+}
+
+// left = Px - w/2, to_next = min(ceil(left) - left, w), ul = floor(left)
+// with w = 0.5 (:222-225).
+__device__ __forceinline__ void edge3(float px, int& ul, float& t) {
+  const float left = fsub(px, 0.25f);
+  t = fminf(fsub(ceilf(left), left), 0.5f);
+  ul = (int)floorf(left);
+}
+
+// ---------------------------------------------------------------------------
+// AXIS0 forward
+// ---------------------------------------------------------------------------
+struct Ax0FwdArgs {
+  const float* vol;  // (S, NJ, NK)
+  float* acc_out;    // [G][V][C][Spad]
+  const float* views;
+  const uint16_t* order;
+  int S, NJ, NK, V, C, Spad;
+  int tiles_k, n_tiles, G;
+  int vpc;   // views per CTA
+  int span;  // accumulator bins per warp
+  int vec4;  // NK % 4 == 0 and vol 16-B aligned
+  int* errflag;
+};
+
+// Bin range of one 32x32 tile for one view.  Every operation of the rounded
+// Px is monotone in each pixel index, so the tile's extremes are at corner
+// pixels; floor(left) of those, widened by one bin below and two above
+// (room for the second tap and the carried bin), gives [lo, hi).
+__device__ __forceinline__ void tile_bins(float m11, float m12, float m13, int j0, int k0,
+                                          int& lo, int& hi) {
+  const float ja = (float)j0 + 0.5f, jb = (float)(j0 + kTile - 1) + 0.5f;
+  const float ka = (float)k0 + 0.5f, kb = (float)(k0 + kTile - 1) + 0.5f;
+  const float a0 = fmul(m11, ja), a1 = fmul(m11, jb);
+  const float b0 = fmul(m12, ka), b1 = fmul(m12, kb);
+  const float pmin = fadd(fminf(a0, a1) + fminf(b0, b1), m13);
+  const float pmax = fadd(fmaxf(a0, a1) + fmaxf(b0, b1), m13);
+  lo = (int)floorf(pmin - 0.25f) - 1;
+  hi = (int)floorf(pmax - 0.25f) + 3;
+}
+
+__global__ void __launch_bounds__(256, 1) k_p3_ax0_fwd(const Ax0FwdArgs a) {
+  extern __shared__ __align__(16) float smem[];
+  float* sv = smem;                                      // [kOrd][kSvStride]
+  float4* tab = reinterpret_cast<float4*>(sv + kOrd * kSvStride);  // [8][kTabChunk]
+  float* acc = reinterpret_cast<float*>(tab + 8 * kTabChunk);      // [8][span][32]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = blockIdx.x, i0 = blockIdx.y * 32, v0 = blockIdx.z * a.vpc;
+  const int nvh = min(a.vpc, a.V - v0);
+  float* accw = acc + (size_t)warp * a.span * 32;
+  float4* tabw = tab + warp * kTabChunk;
+
+  // zero this CTA's slice of the output accumulator and the warp accumulators
+  for (int v = 0; v < nvh; ++v) {
+    float* o = a.acc_out + ((size_t)g * a.V + v0 + v) * a.C * a.Spad + i0;
+    for (int e = tid; e < a.C * 32; e += 256) o[(size_t)(e >> 5) * a.Spad + (e & 31)] = 0.0f;
+  }
+  for (int e = tid; e < 8 * a.span * 32; e += 256) acc[e] = 0.0f;
+  __syncthreads();
+
+  for (int t = g; t < a.n_tiles; t += a.G) {
+    const int j0 = (t / a.tiles_k) * kTile, k0 = (t % a.tiles_k) * kTile;
+    // stage vol[i0+s][j0+j][k0+k] as sv[(j*32+k)*33 + s]: one warp
+    // instruction covers four consecutive slices of one row (bank-conflict
+    // free, see the index arithmetic: bank = (k + s) mod 32)
+#pragma unroll 4
+    for (int q = 0; q < 32; ++q) {
+      const int R = (q * 8 + warp) * 4 + (lane >> 3);
+      const int s = R & 31, j = R >> 5, kq = (lane & 7) * 4;
+      const int gi = i0 + s, gj = j0 + j, gk = k0 + kq;
+      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gi < a.S && gj < a.NJ) {
+        const float* src = a.vol + ((size_t)gi * a.NJ + gj) * a.NK + gk;
+        if (a.vec4 && gk + 3 < a.NK) {
+          x = __ldg(reinterpret_cast<const float4*>(src));
+        } else {
+          if (gk < a.NK) x.x = __ldg(src);
+          if (gk + 1 < a.NK) x.y = __ldg(src + 1);
+          if (gk + 2 < a.NK) x.z = __ldg(src + 2);
+          if (gk + 3 < a.NK) x.w = __ldg(src + 3);
+        }
+      }
+      float* d = sv + (j * kTile + kq) * kSvStride + s;
+      d[0] = x.x;
+      d[kSvStride] = x.y;
+      d[2 * kSvStride] = x.z;
+      d[3 * kSvStride] = x.w;
+    }
+    __syncthreads();
+
+    for (int vi = warp; vi < nvh; vi += 8) {
+      const int v = v0 + vi;
+      const float* m = a.views + (size_t)v * kVT;
+      const float m11 = m[5], m12 = m[6], m13 = m[7];
+      int lo, hi;
+      tile_bins(m11, m12, m13, j0, k0, lo, hi);
+      const int nb = hi - lo;
+      if (nb > a.span) {  // cannot happen for |m11|, |m12| <= 1
+        if (lane == 0) atomicOr(a.errflag, 1);
+        continue;
+      }
+      const uint16_t* ord = a.order + (size_t)v * kOrd;
+      int cur = 1;  // accumulator row of the open bin (relative to lo)
+      float A = 0.f, B = 0.f;
+      for (int ch = 0; ch < kOrd; ch += kTabChunk) {
+#pragma unroll
+        for (int q = 0; q < kTabChunk / 32; ++q) {
+          const int p = ord[ch + q * 32 + lane];
+          const int pj = p >> 5, pk = p & 31;
+          const float x1 = (float)(j0 + pj) + 0.5f, x2 = (float)(k0 + pk) + 0.5f;
+          // Px_1 with M[1][0] = 0: the x0 term is an exact zero
+          const float px = fadd(fadd(fmul(m11, x1), fmul(m12, x2)), m13);
+          int ul;
+          float t1;
+          edge3(px, ul, t1);
+          const float w0 = (ul >= 0 && ul < a.C) ? fmul(2.0f, t1) : 0.0f;
+          const float w1 = (ul + 1 >= 0 && ul + 1 < a.C) ? fmul(2.0f, fsub(0.5f, t1)) : 0.0f;
+          int rel = ul - lo;
+          rel = min(max(rel, 0), nb - 2);  // in range: Px is monotone, extremes at corners
+          tabw[q * 32 + lane] =
+              make_float4(w0, w1, __int_as_float(rel * 32), __int_as_float(p * kSvStride));
+        }
+        __syncwarp();
+        const int curb = cur * 32;
+        int cb = curb;
+#pragma unroll 8
+        for (int e = 0; e < kTabChunk; ++e) {
+          const float4 T = tabw[e];
+          const float x = sv[__float_as_int(T.w) + lane];
+          const int rb = __float_as_int(T.z);
+          if (rb != cb) {  // warp-uniform: every lane reads the same entry
+            accw[cb + lane] += A;
+            if (rb == cb + 32) {
+              A = B;
+            } else {
+              accw[cb + 32 + lane] += B;
+              A = 0.f;
+            }
+            B = 0.f;
+            cb = rb;
+          }
+          A = fmaf(T.x, x, A);
+          B = fmaf(T.y, x, B);
+        }
+        cur = cb >> 5;
+        __syncwarp();
+      }
+      accw[cur * 32 + lane] += A;
+      accw[(cur + 1) * 32 + lane] += B;
+      __syncwarp();
+      // add the tile's bins into the output accumulator and clear them
+      float* o = a.acc_out + (((size_t)g * a.V + v) * a.C) * a.Spad + i0 + lane;
+      for (int r = 0; r < nb; ++r) {
+        const int c = lo + r;
+        const float val = accw[r * 32 + lane];
+        accw[r * 32 + lane] = 0.f;
+        if (c >= 0 && c < a.C) o[(size_t)c * a.Spad] += val;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+}
+
+// proj[v][r][c] = sum_g acc_out[g][v][c][r - row_offset] (0 where no slice
+// lands on row r).  32x32 (col, row) tiles through shared memory.
+__global__ void k_p3_ax0_rows(const float* __restrict__ acc, float* __restrict__ proj, int V,
+                              int R, int C, int S, int Spad, int G, int row_offset) {
+  __shared__ float t[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32, v = blockIdx.z;
+  const int lx = threadIdx.x, ly = threadIdx.y;  // 32 x 8
+  for (int q = 0; q < 4; ++q) {
+    const int cl = ly + 8 * q, c = c0 + cl;
+    const int i = r0 + lx - row_offset;
+    float s = 0.f;
+    if (c < C && i >= 0 && i < S) {
+      for (int gg = 0; gg < G; ++gg) s += acc[(((size_t)gg * V + v) * C + c) * Spad + i];
+    }
+    t[cl][lx] = s;
+  }
+  __syncthreads();
+  for (int q = 0; q < 4; ++q) {
+    const int rl = ly + 8 * q, r = r0 + rl, c = c0 + lx;
+    if (r < R && c < C) proj[((size_t)v * R + r) * C + c] = t[lx][rl];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// AXIS0 adjoint
+// ---------------------------------------------------------------------------
+struct Ax0AdjArgs {
+  const float* proj;  // (V, R, C)
+  float* out;         // (S, NJ, NK), or split partials
+  const float* views;
+  int S, NJ, NK, V, R, C, row_offset;
+  int W;  // staged bins per slice row
+  int per_split;
+  size_t split_stride;
+  int* errflag;
+};
+
+__device__ __forceinline__ float2 ld_shared_f2(uint32_t addr) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+  return v;
+}
+
+__global__ void __launch_bounds__(256, 2) k_p3_ax0_adj(const Ax0AdjArgs a) {
+  extern __shared__ __align__(16) float2 sy[];  // [2][32][W]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k0 = blockIdx.x * 32, j0 = blockIdx.y * kAdjRows;
+  const int nsg = (a.S + 31) / 32;
+  const int sg = blockIdx.z % nsg, split = blockIdx.z / nsg;
+  const int i0 = sg * 32;
+  const int k = k0 + lane;
+  const int jj[2] = {j0 + warp, j0 + warp + 8};
+  const int vs = split * a.per_split, ve = min(a.V, vs + a.per_split);
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sy);
+  float acc[2][32];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int s = 0; s < 32; ++s) acc[q][s] = 0.f;
+
+  for (int v = vs; v < ve; ++v) {
+    const int buf = (v - vs) & 1;
+    const float* m = a.views + (size_t)v * kVT;
+    const float m11 = m[5], m12 = m[6], m13 = m[7];
+    // bin window of the 16x32 tile (corner bound, as tile_bins)
+    const float ja = (float)j0 + 0.5f, jb = (float)(j0 + kAdjRows - 1) + 0.5f;
+    const float ka = (float)k0 + 0.5f, kb = (float)(k0 + 31) + 0.5f;
+    const float a0 = fmul(m11, ja), a1 = fmul(m11, jb), b0 = fmul(m12, ka), b1 = fmul(m12, kb);
+    const int lo = (int)floorf(fadd(fminf(a0, a1) + fminf(b0, b1), m13) - 0.25f) - 1;
+    const int hi = (int)floorf(fadd(fmaxf(a0, a1) + fmaxf(b0, b1), m13) - 0.25f) + 3;
+    const int nb = min(hi - lo, a.W);
+    if (hi - lo > a.W && tid == 0) atomicOr(a.errflag, 2);
+    // stage rows i0+s+row_offset, columns lo .. lo+nb-1 as (y[c], y[c+1])
+    float2* dst = sy + (size_t)buf * 32 * a.W;
+    const float* src = a.proj + (size_t)v * a.R * a.C;
+    for (int e = tid; e < 32 * nb; e += 256) {
+      const int s = e / nb, bl = e - s * nb;
+      const int r = i0 + s + a.row_offset, c = lo + bl;
+      float y0 = 0.f, y1 = 0.f;
+      if (i0 + s < a.S && r >= 0 && r < a.R) {
+        const float* row = src + (size_t)r * a.C;
+        if (c >= 0 && c < a.C) y0 = __ldg(row + c);
+        if (c + 1 >= 0 && c + 1 < a.C) y1 = __ldg(row + c + 1);
+      }
+      dst[s * a.W + bl] = make_float2(y0, y1);
+    }
+    __syncthreads();
+    const uint32_t vbase = sbase + (uint32_t)(buf * 32 * a.W) * 8u;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float x1 = (float)jj[q] + 0.5f, x2 = (float)k + 0.5f;
+      const float px = fadd(fadd(fmul(m11, x1), fmul(m12, x2)), m13);
+      int ul;
+      float t1;
+      edge3(px, ul, t1);
+      float w0 = (ul >= 0 && ul < a.C) ? fmul(2.0f, t1) : 0.0f;
+      float w1 = (ul + 1 >= 0 && ul + 1 < a.C) ? fmul(2.0f, fsub(0.5f, t1)) : 0.0f;
+      int rel = ul - lo;
+      if (rel < 0 || rel >= nb - 1) {  // outside the staged window (cannot happen)
+        rel = 0;
+        w0 = 0.f;
+        w1 = 0.f;
+      }
+      const uint32_t addr = vbase + (uint32_t)rel * 8u;
+#pragma unroll
+      for (int s = 0; s < 32; ++s) {
+        const float2 y = ld_shared_f2(addr + (uint32_t)(s * a.W) * 8u);
+        acc[q][s] = fmaf(w0, y.x, acc[q][s]);
+        acc[q][s] = fmaf(w1, y.y, acc[q][s]);
+      }
+    }
+  }
+  float* out = a.out + (size_t)split * a.split_stride;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    if (jj[q] >= a.NJ || k >= a.NK) continue;
+#pragma unroll
+    for (int s = 0; s < 32; ++s) {
+      if (i0 + s < a.S) out[((size_t)(i0 + s) * a.NJ + jj[q]) * a.NK + k] = acc[q][s];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GENERAL adjoint: one voxel per thread, views in order, four gathers each
+// (_back_project_single, :192-204).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_p3_gen_adj(const float* __restrict__ proj,
+                                                    float* __restrict__ out,
+                                                    const float* __restrict__ views, int n0,
+                                                    int n1, int n2, int V, int R, int C,
+                                                    int per_split, size_t split_stride) {
+  __shared__ float sm[kGenViewChunk * 8];
+  const size_t n = (size_t)n0 * n1 * n2;
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int split = blockIdx.y;
+  const int vs = split * per_split, ve = min(V, vs + per_split);
+  int i0 = 0, i1 = 0, i2 = 0;
+  if (e < n) {
+    i2 = (int)(e % n2);
+    const size_t r = e / n2;
+    i1 = (int)(r % n1);
+    i0 = (int)(r / n1);
+  }
+  const float x0 = (float)i0 + 0.5f, x1 = (float)i1 + 0.5f, x2 = (float)i2 + 0.5f;
+  float acc = 0.f;
+  for (int vc = vs; vc < ve; vc += kGenViewChunk) {
+    const int nvc = min(kGenViewChunk, ve - vc);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nvc * 8; q += blockDim.x)
+      sm[q] = views[(size_t)(vc + q / 8) * kVT + (q & 7)];
+    __syncthreads();
+    if (e >= n) continue;
+    for (int vi = 0; vi < nvc; ++vi) {
+      const float* m = sm + vi * 8;
+      int u0, u1;
+      float t0, t1;
+      edge3(px3(m[0], m[1], m[2], m[3], x0, x1, x2), u0, t0);
+      edge3(px3(m[4], m[5], m[6], m[7], x0, x1, x2), u1, t1);
+      const float s0 = fsub(0.5f, t0), s1 = fsub(0.5f, t1);
+      const bool r0 = u0 >= 0 && u0 < R, r1 = u0 + 1 >= 0 && u0 + 1 < R;
+      const bool c0 = u1 >= 0 && u1 < C, c1 = u1 + 1 >= 0 && u1 + 1 < C;
+      const float* y = proj + (size_t)(vc + vi) * R * C;
+      if (r0 && c0) acc = fmaf(__ldg(y + (size_t)u0 * C + u1), fmul(fmul(t0, t1), 4.0f), acc);
+      if (r1 && c0) acc = fmaf(__ldg(y + (size_t)(u0 + 1) * C + u1), fmul(fmul(s0, t1), 4.0f), acc);
+      if (r0 && c1) acc = fmaf(__ldg(y + (size_t)u0 * C + u1 + 1), fmul(fmul(t0, s1), 4.0f), acc);
+      if (r1 && c1)
+        acc = fmaf(__ldg(y + (size_t)(u0 + 1) * C + u1 + 1), fmul(fmul(s0, s1), 4.0f), acc);
+    }
+  }
+  if (e < n) out[(size_t)split * split_stride + e] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// GENERAL forward: one detector pixel per thread.
+// ---------------------------------------------------------------------------
+// x range [lo, hi] of voxel centres along one axis allowed by the detector
+// window [wlo, whi] on one detector axis, given Px = beta + mq * x.
+__device__ __forceinline__ void narrow(float beta, float mq, float wlo, float whi, float& lo,
+                                       float& hi) {
+  if (fabsf(mq) > 1e-20f) {
+    const float u = (wlo - beta) / mq, w = (whi - beta) / mq;
+    lo = fmaxf(lo, fminf(u, w));
+    hi = fminf(hi, fmaxf(u, w));
+  } else if (beta < wlo || beta > whi) {
+    lo = 1.0f;
+    hi = 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_p3_gen_fwd(const float* __restrict__ vol,
+                                                    float* __restrict__ proj,
+                                                    const float* __restrict__ views, int n0,
+                                                    int n1, int n2, int V, int R, int C) {
+  const int v = blockIdx.y;
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= R * C) return;
+  const int r = pix / C, c = pix - (pix / C) * C;
+  const float* m = views + (size_t)v * kVT;
+  float mm[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) mm[q] = m[q];
+  const int ax = (int)m[8];
+  // the other two axes, ascending: p = ax==0 ? 1 : 0, q = ax==2 ? 1 : 2
+  auto pick = [ax](float a0, float a1, float a2, int which) {
+    // which: 0 = the marching axis, 1 = p, 2 = q
+    const int k = which == 0 ? ax : (which == 1 ? (ax == 0 ? 1 : 0) : (ax == 2 ? 1 : 2));
+    return k == 0 ? a0 : (k == 1 ? a1 : a2);
+  };
+  const float na_f = pick((float)n0, (float)n1, (float)n2, 0);
+  const int na = (int)na_f, np = (int)pick((float)n0, (float)n1, (float)n2, 1),
+            nq = (int)pick((float)n0, (float)n1, (float)n2, 2);
+  const float ma0 = pick(mm[0], mm[1], mm[2], 0), mp0 = pick(mm[0], mm[1], mm[2], 1),
+              mq0 = pick(mm[0], mm[1], mm[2], 2);
+  const float ma1 = pick(mm[4], mm[5], mm[6], 0), mp1 = pick(mm[4], mm[5], mm[6], 1),
+              mq1 = pick(mm[4], mm[5], mm[6], 2);
+  // taps reaching (r, c) come from voxels with floor(left) in {r-1, r} x
+  // {c-1, c}: Px in [r-0.75, r+1.25) x [c-0.75, c+1.25); widened by a margin
+  // far above the rounding of the range arithmetic (the exact test decides)
+  const float mg = 0.05f;
+  const float w0lo = (float)r - 0.75f - mg, w0hi = (float)r + 1.25f + mg;
+  const float w1lo = (float)c - 0.75f - mg, w1hi = (float)c + 1.25f + mg;
+  // |x_p - centre_p| <= e_p from the 2x2 system of the (p, q) plane
+  const float det = mp0 * mq1 - mq0 * mp1;
+  const float h0 = 0.5f * (w0hi - w0lo), h1 = 0.5f * (w1hi - w1lo);
+  const float ep = (fabsf(mq1) * h0 + fabsf(mq0) * h1) / fabsf(det);
+  // voxel strides of the marching, p and q axes
+  const size_t sa = (size_t)pick((float)((size_t)n1 * n2), (float)n2, 1.0f, 0);
+  const size_t sp = ax == 0 ? (size_t)n2 : (size_t)n1 * n2;
+  const size_t sq = ax == 2 ? (size_t)n2 : 1;
+  float acc = 0.f;
+  for (int ia = 0; ia < na; ++ia) {
+    const float xa = (float)ia + 0.5f;
+    const float al0 = ma0 * xa + mm[3], al1 = ma1 * xa + mm[7];
+    const float cr0 = 0.5f * (w0lo + w0hi) - al0, cr1 = 0.5f * (w1lo + w1hi) - al1;
+    const float cp = (mq1 * cr0 - mq0 * cr1) / det;
+    const float plo = fmaxf(0.5f, cp - ep - mg), phi = fminf((float)np - 0.5f, cp + ep + mg);
+    if (!(plo <= phi)) continue;
+    const int ip0 = max(0, (int)ceilf(plo - 0.5f)), ip1 = min(np - 1, (int)floorf(phi - 0.5f));
+    for (int ip = ip0; ip <= ip1; ++ip) {
+      const float xp = (float)ip + 0.5f;
+      float qlo = 0.5f, qhi = (float)nq - 0.5f;
+      narrow(al0 + mp0 * xp, mq0, w0lo, w0hi, qlo, qhi);
+      narrow(al1 + mp1 * xp, mq1, w1lo, w1hi, qlo, qhi);
+      if (!(qlo <= qhi)) continue;
+      const int iq0 = max(0, (int)ceilf(qlo - 0.5f - mg)), iq1 = min(nq - 1, (int)floorf(qhi - 0.5f + mg));
+      for (int iq = iq0; iq <= iq1; ++iq) {
+        const int i0 = ax == 0 ? ia : ip;
+        const int i1 = ax == 0 ? ip : (ax == 1 ? ia : iq);
+        const int i2 = ax == 2 ? ia : iq;
+        const float x0 = (float)i0 + 0.5f, x1 = (float)i1 + 0.5f, x2 = (float)i2 + 0.5f;
+        int u0, u1;
+        float t0, t1;
+        edge3(px3(mm[0], mm[1], mm[2], mm[3], x0, x1, x2), u0, t0);
+        edge3(px3(mm[4], mm[5], mm[6], mm[7], x0, x1, x2), u1, t1);
+        const int d0 = r - u0, d1 = c - u1;
+        if ((unsigned)d0 > 1u || (unsigned)d1 > 1u) continue;
+        const float f0 = d0 ? fsub(0.5f, t0) : t0;
+        const float f1 = d1 ? fsub(0.5f, t1) : t1;
+        const float w = fmul(fmul(f0, f1), 4.0f);
+        acc = fmaf(w, __ldg(vol + ia * sa + ip * sp + iq * sq), acc);
+      }
+    }
+  }
+  proj[((size_t)v * R + r) * C + c] = acc;
+}
+
+__global__ void k_p3_sum_splits(const float* __restrict__ part, float* __restrict__ out, size_t n,
+                                int nsplit, size_t stride) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int k = 0; k < nsplit; ++k) s += part[(size_t)k * stride + e];
+    out[e] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host planning
+// ---------------------------------------------------------------------------
+struct Proj3dPlan {
+  // AXIS0 forward
+  int Spad = 0, tiles_k = 0, n_tiles = 0, G = 1, vpc = kFwdViewsPerCta, span = 0;
+  size_t fwd_smem = 0;
+  // AXIS0 adjoint
+  int W = 0;
+  size_t adj_smem = 0;
+  // adjoint view splits (both kinds)
+  int nsplit = 1, per_split = 0;
+  size_t fwd_bytes = 0, adj_bytes = 0;
+};
+
+ct_status proj3d_check(const ct_geom3d* g, const char* who) {
+  if (!g) return fail(CT_ERR_INVALID_ARG, "%s: null geometry", who);
+  for (int q = 0; q < 3; ++q)
+    if (g->shape[q] <= 0) return fail(CT_ERR_SHAPE, "%s: shape[%d]=%d", who, q, g->shape[q]);
+  if (g->det_shape[0] <= 0 || g->det_shape[1] <= 0)
+    return fail(CT_ERR_SHAPE, "%s: det_shape=(%d, %d)", who, g->det_shape[0], g->det_shape[1]);
+  if (g->n_views <= 0) return fail(CT_ERR_SHAPE, "%s: n_views=%d", who, g->n_views);
+  if (!g->views) return fail(CT_ERR_INVALID_ARG, "%s: null view table", who);
+  if (g->kind != CT_PROJ3D_GENERAL && g->kind != CT_PROJ3D_AXIS0)
+    return fail(CT_ERR_INVALID_ARG, "%s: kind=%d", who, g->kind);
+  if (g->kind == CT_PROJ3D_AXIS0 && !g->order)
+    return fail(CT_ERR_INVALID_ARG, "%s: AXIS0 geometry without an order table", who);
+  const double n = (double)g->shape[0] * g->shape[1] * g->shape[2];
+  if (n > 2147483647.0 || (double)g->det_shape[0] * g->det_shape[1] > 2147483647.0)
+    return fail(CT_ERR_UNSUPPORTED, "%s: volume or detector above 2^31 elements", who);
+  return CT_OK;
+}
+
+// The AXIS0 span bounds need max |M[1][1]| and |M[1][2]|; ct_proj3d_views
+// guarantees both <= 1, so the bounds are fixed.
+Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch) {
+  Proj3dPlan p;
+  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
+  const int C = g->det_shape[1];
+  const int sms = std::max(1, sm_count());
+  if (g->kind == CT_PROJ3D_AXIS0) {
+    p.Spad = (S + 31) / 32 * 32;
+    p.tiles_k = (NK + kTile - 1) / kTile;
+    p.n_tiles = p.tiles_k * ((NJ + kTile - 1) / kTile);
+    p.span = kAccSpan;
+    const long base = (long)(p.Spad / 32) * ((V + p.vpc - 1) / p.vpc);
+    int G = 1;
+    while (G < 4 && G < p.n_tiles && base * G < 3L * sms) ++G;
+    p.G = G;
+    p.fwd_smem = sizeof(float) * (size_t)kOrd * kSvStride + sizeof(float4) * 8 * kTabChunk +
+                 sizeof(float) * 8 * (size_t)p.span * 32;
+    p.fwd_bytes = round_up(sizeof(float) * (size_t)p.G * V * C * p.Spad, 256);
+    p.W = (kAdjRows - 1) + 31 + 6;
+    p.adj_smem = sizeof(float2) * 2 * 32 * (size_t)p.W;
+    const long ctas = (long)((NK + 31) / 32) * ((NJ + kAdjRows - 1) / kAdjRows) * (p.Spad / 32);
+    int ns = 1;
+    if (ctas < kAdjTargetCtas) ns = (int)((kAdjTargetCtas + ctas - 1) / ctas);
+    ns = std::min(ns, std::max(1, V / 16));
+    p.per_split = (V + ns - 1) / ns;
+    p.nsplit = (V + p.per_split - 1) / p.per_split;
+  } else {
+    const double n = (double)S * NJ * NK;
+    const long ctas = (long)((n + 255) / 256);
+    int ns = 1;
+    if (ctas < 4L * sms) ns = (int)((4L * sms + ctas - 1) / ctas);
+    ns = std::min(ns, std::max(1, V / 8));
+    p.per_split = (V + ns - 1) / ns;
+    p.nsplit = (V + p.per_split - 1) / p.per_split;
+  }
+  p.adj_bytes = p.nsplit > 1 ? round_up(sizeof(float) * (size_t)p.nsplit * S * NJ * NK, 256) : 0;
+  (void)batch;
+  return p;
+}
+
+ct_status need_ws(const char* who, size_t need, void* ws, size_t bytes) {
+  if (need == 0) return CT_OK;
+  if (!ws || bytes < need || !aligned(ws, 256))
+    return fail(CT_ERR_WORKSPACE, "%s: need %zu bytes (256-B aligned), got %zu", who, need, bytes);
+  return CT_OK;
+}
+
+}  // namespace
+}  // namespace ct
+
+extern "C" {
+
+ct_status ct_proj3d_views(const float* matrices, int32_t n_views, const int32_t* shape,
+                          const int32_t* det_shape, float* views_out, uint16_t* order_out,
+                          int32_t* kind_out, int32_t* row_offset_out) {
+  using ct::fail;
+  if (!matrices || !shape || !det_shape || !views_out || !kind_out || !row_offset_out)
+    return fail(CT_ERR_INVALID_ARG, "ct_proj3d_views: null argument");
+  if (n_views <= 0) return fail(CT_ERR_SHAPE, "ct_proj3d_views: n_views=%d", n_views);
+  for (int q = 0; q < 3; ++q)
+    if (shape[q] <= 0) return fail(CT_ERR_SHAPE, "ct_proj3d_views: shape[%d]=%d", q, shape[q]);
+  if (det_shape[0] <= 0 || det_shape[1] <= 0)
+    return fail(CT_ERR_SHAPE, "ct_proj3d_views: det_shape=(%d, %d)", det_shape[0], det_shape[1]);
+  for (int v = 0; v < n_views; ++v) {
+    const float* m = matrices + (size_t)v * 8;
+    float* t = views_out + (size_t)v * CT_VIEW3D_STRIDE;
+    for (int q = 0; q < 8; ++q) {
+      if (!std::isfinite(m[q]))
+        return fail(CT_ERR_NONFINITE, "ct_proj3d_views: matrix %d has a non-finite entry", v);
+      t[q] = m[q];
+    }
+    const double d[3] = {(double)m[1] * m[6] - (double)m[2] * m[5],
+                         (double)m[2] * m[4] - (double)m[0] * m[6],
+                         (double)m[0] * m[5] - (double)m[1] * m[4]};
+    int ax = 0;
+    for (int q = 1; q < 3; ++q)
+      if (std::fabs(d[q]) > std::fabs(d[ax])) ax = q;
+    const double n0 = std::sqrt((double)m[0] * m[0] + (double)m[1] * m[1] + (double)m[2] * m[2]);
+    const double n1 = std::sqrt((double)m[4] * m[4] + (double)m[5] * m[5] + (double)m[6] * m[6]);
+    if (!(std::fabs(d[ax]) > 1e-6 * n0 * n1))
+      return fail(CT_ERR_UNSUPPORTED,
+                  "ct_proj3d_views: matrix %d maps the volume onto a line (parallel rows)", v);
+    t[8] = (float)ax;
+    t[9] = t[10] = t[11] = 0.0f;
+  }
+  // AXIS0: rows of axis 0 only, shared by all views, each slice on one row
+  // with to_next 0.5 (float32 arithmetic as the reference's; the zero terms
+  // of Px_0 are exact)
+  bool ax0 = order_out != nullptr;
+  int32_t off = 0;
+  for (int v = 0; ax0 && v < n_views; ++v) {
+    const float* m = matrices + (size_t)v * 8;
+    ax0 = m[1] == 0.0f && m[2] == 0.0f && m[4] == 0.0f && std::fabs(m[5]) <= 1.0f &&
+          std::fabs(m[6]) <= 1.0f;
+    // every view must put slice i on row i + off with to_next 0.5 (the
+    // translation may differ between views by amounts below one ulp)
+    for (int i = 0; ax0 && i < shape[0]; ++i) {
+      const float x0 = (float)i + 0.5f;
+      const float px = m[0] * x0 + m[3];  // two roundings; host code is not contracted
+      const float left = px - 0.25f;
+      const float tn = std::fmin(std::ceil(left) - left, 0.5f);
+      const int ul = (int)std::floor(left);
+      if (v == 0 && i == 0) off = ul;
+      ax0 = tn == 0.5f && ul == i + off;
+    }
+  }
+  *kind_out = ax0 ? CT_PROJ3D_AXIS0 : CT_PROJ3D_GENERAL;
+  *row_offset_out = ax0 ? off : 0;
+  if (ax0) {
+    std::vector<std::pair<double, int>> key(CT_PROJ3D_ORDER);
+    for (int v = 0; v < n_views; ++v) {
+      const float* m = matrices + (size_t)v * 8;
+      for (int p = 0; p < CT_PROJ3D_ORDER; ++p)
+        key[p] = {(double)m[5] * (p >> 5) + (double)m[6] * (p & 31), p};
+      std::stable_sort(key.begin(), key.end(),
+                       [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+                         return a.first < b.first;
+                       });
+      for (int p = 0; p < CT_PROJ3D_ORDER; ++p)
+        order_out[(size_t)v * CT_PROJ3D_ORDER + p] = (uint16_t)key[p].second;
+    }
+  }
+  return CT_OK;
+}
+
+ct_status ct_proj3d_workspace(const ct_geom3d* g, int32_t batch, size_t* fwd_bytes,
+                              size_t* adj_bytes) {
+  ct_status st = ct::proj3d_check(g, "ct_proj3d_workspace");
+  if (st != CT_OK) return st;
+  if (batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_proj3d_workspace: batch=%d", batch);
+  const ct::Proj3dPlan p = ct::proj3d_plan(g, batch);
+  if (fwd_bytes) *fwd_bytes = p.fwd_bytes;
+  if (adj_bytes) *adj_bytes = p.adj_bytes;
+  return CT_OK;
+}
+
+ct_status ct_proj3d_fwd(const ct_geom3d* g, const float* vol, float* proj, int32_t batch,
+                        void* workspace, size_t workspace_bytes, ct_stream_t stream) {
+  using namespace ct;
+  ct_status st = proj3d_check(g, "ct_proj3d_fwd");
+  if (st != CT_OK) return st;
+  if (!vol || !proj) return fail(CT_ERR_INVALID_ARG, "ct_proj3d_fwd: null array");
+  if (batch <= 0) return fail(CT_ERR_INVALID_ARG, "ct_proj3d_fwd: batch=%d", batch);
+  const Proj3dPlan p = proj3d_plan(g, batch);
+  st = need_ws("ct_proj3d_fwd", p.fwd_bytes, workspace, workspace_bytes);
+  if (st != CT_OK) return st;
+  cudaStream_t s = as_stream(stream);
+  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
+  const int R = g->det_shape[0], C = g->det_shape[1];
+  const size_t vol_n = (size_t)S * NJ * NK, proj_n = (size_t)V * R * C;
+  if (g->kind == CT_PROJ3D_AXIS0) {
+    int* ef = errflag3_ptr();
+    if (!ef) return fail(CT_ERR_CUDA, "proj3d: error-word address unavailable");
+    st = cuda_check(cudaFuncSetAttribute(k_p3_ax0_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p.fwd_smem),
+                    "k_p3_ax0_fwd smem attribute");
+    if (st != CT_OK) return st;
+    for (int b = 0; b < batch; ++b) {
+      Ax0FwdArgs a;
+      a.vol = vol + b * vol_n;
+      a.acc_out = static_cast<float*>(workspace);
+      a.views = g->views;
+      a.order = g->order;
+      a.S = S;
+      a.NJ = NJ;
+      a.NK = NK;
+      a.V = V;
+      a.C = C;
+      a.Spad = p.Spad;
+      a.tiles_k = p.tiles_k;
+      a.n_tiles = p.n_tiles;
+      a.G = p.G;
+      a.vpc = p.vpc;
+      a.span = p.span;
+      a.vec4 = ((NK & 3) == 0 && aligned(vol, 16)) ? 1 : 0;
+      a.errflag = ef;
+      dim3 grid(p.G, p.Spad / 32, (V + p.vpc - 1) / p.vpc);
+      k_p3_ax0_fwd<<<grid, 256, p.fwd_smem, s>>>(a);
+      st = launch_check("k_p3_ax0_fwd");
+      if (st != CT_OK) return st;
+      dim3 g2((C + 31) / 32, (R + 31) / 32, V);
+      k_p3_ax0_rows<<<g2, dim3(32, 8), 0, s>>>(a.acc_out, proj + b * proj_n, V, R, C, S, p.Spad,
+                                               p.G, g->row_offset);
+      st = launch_check("k_p3_ax0_rows");
+      if (st != CT_OK) return st;
+    }
+    return CT_OK;
+  }
+  for (int b = 0; b < batch; ++b) {
+    dim3 grid((R * C + 255) / 256, V);
+    k_p3_gen_fwd<<<grid, 256, 0, s>>>(vol + b * vol_n, proj + b * proj_n, g->views, S, NJ, NK, V,
+                                      R, C);
+    st = launch_check("k_p3_gen_fwd");
+    if (st != CT_OK) return st;
+  }
+  return CT_OK;
+}
+
+ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol, int32_t batch,
+                        void* workspace, size_t workspace_bytes, ct_stream_t stream) {
+  using namespace ct;
+  ct_status st = proj3d_check(g, "ct_proj3d_adj");
+  if (st != CT_OK) return st;
+  if (!vol || !proj) return fail(CT_ERR_INVALID_ARG, "ct_proj3d_adj: null array");
+  if (batch <= 0) return fail(CT_ERR_INVALID_ARG, "ct_proj3d_adj: batch=%d", batch);
+  const Proj3dPlan p = proj3d_plan(g, batch);
+  st = need_ws("ct_proj3d_adj", p.adj_bytes, workspace, workspace_bytes);
+  if (st != CT_OK) return st;
+  cudaStream_t s = as_stream(stream);
+  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
+  const int R = g->det_shape[0], C = g->det_shape[1];
+  const size_t vol_n = (size_t)S * NJ * NK, proj_n = (size_t)V * R * C;
+  float* part = static_cast<float*>(workspace);
+  int* ef = errflag3_ptr();
+  if (!ef) return fail(CT_ERR_CUDA, "proj3d: error-word address unavailable");
+  if (g->kind == CT_PROJ3D_AXIS0) {
+    st = cuda_check(cudaFuncSetAttribute(k_p3_ax0_adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p.adj_smem),
+                    "k_p3_ax0_adj smem attribute");
+    if (st != CT_OK) return st;
+  }
+  for (int b = 0; b < batch; ++b) {
+    float* dst = p.nsplit > 1 ? part : vol + b * vol_n;
+    if (g->kind == CT_PROJ3D_AXIS0) {
+      Ax0AdjArgs a;
+      a.proj = proj + b * proj_n;
+      a.out = dst;
+      a.views = g->views;
+      a.S = S;
+      a.NJ = NJ;
+      a.NK = NK;
+      a.V = V;
+      a.R = R;
+      a.C = C;
+      a.row_offset = g->row_offset;
+      a.W = p.W;
+      a.per_split = p.per_split;
+      a.split_stride = vol_n;
+      a.errflag = ef;
+      dim3 grid((NK + 31) / 32, (NJ + kAdjRows - 1) / kAdjRows, (p.Spad / 32) * p.nsplit);
+      k_p3_ax0_adj<<<grid, 256, p.adj_smem, s>>>(a);
+      st = launch_check("k_p3_ax0_adj");
+    } else {
+      dim3 grid((unsigned)((vol_n + 255) / 256), p.nsplit);
+      k_p3_gen_adj<<<grid, 256, 0, s>>>(proj + b * proj_n, dst, g->views, S, NJ, NK, V, R, C,
+                                        p.per_split, vol_n);
+      st = launch_check("k_p3_gen_adj");
+    }
+    if (st != CT_OK) return st;
+    if (p.nsplit > 1) {
+      const int blocks = (int)std::min<size_t>((vol_n + 255) / 256, 4096);
+      k_p3_sum_splits<<<blocks, 256, 0, s>>>(part, vol + b * vol_n, vol_n, p.nsplit, vol_n);
+      st = launch_check("k_p3_sum_splits");
+      if (st != CT_OK) return st;
+    }
+  }
+  return CT_OK;
+}
+
+// Diagnostic: returns (and clears) the 3D projector's internal check word.
+int ct_proj3d_errflag(void) {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, ct::g_proj3d_err, sizeof(int)) != cudaSuccess) return -1;
+  const int zero = 0;
+  cudaMemcpyToSymbol(ct::g_proj3d_err, &zero, sizeof(int));
+  return v;
+}
+
+}  // extern "C"

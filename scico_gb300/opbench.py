@@ -3,7 +3,9 @@
     python -m scico_gb300.opbench --op proj2d_fwd --config c2 --reps 20
 
 Ops: proj2d_fwd, proj2d_adj (one C-ABI call each, CUDA events per call),
-admm (one fused ADMM-TV solve of --iters iterations).  Prints one JSON line
+admm (one fused ADMM-TV solve of --iters iterations), proj3d_fwd and
+proj3d_adj (the 256^3, 360-view workload; --views N takes the first N views,
+--general runs the GENERAL kernels on it).  Prints one JSON line
 with the median time, interactions/s and the algorithmic-byte bandwidth
 (4 B per pixel-view interaction + the output write).  Used for ncu captures
 of single kernels.
@@ -23,15 +25,23 @@ from . import _device, _lib, linop, workloads
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--op", default="proj2d_fwd", choices=["proj2d_fwd", "proj2d_adj", "admm"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--op", default="proj2d_fwd",
+                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
+    ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
+    ap.add_argument("--general", action="store_true",
+                    help="proj3d: run the GENERAL kernels on the workload's geometry")
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--iters", type=int, default=2)
     ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--graph", type=int, default=1, choices=[0, 1],
+                    help="admm: 1 = one CUDA graph per iteration (the default solver), 0 = plain launches")
     a = ap.parse_args(argv)
-    c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
     dev = _device.require_cuda()
+    if a.op.startswith("proj3d"):
+        return _proj3d(a, dev)
+    c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
     A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
     g = A.geometry()
     img = torch.from_numpy(c.phantom()).to(dev).expand(a.batch, c.n, c.n).contiguous()
@@ -52,7 +62,7 @@ def main(argv=None):
         alg = a.batch * (4.0 * c.interactions + 4.0 * c.n * c.n)
     else:
         y = A(img[0].contiguous())
-        desc = _lib.AdmmTvDesc(g, a.iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam, 0.0, c.rho, 0.5, 1.0, 1)
+        desc = _lib.AdmmTvDesc(g, a.iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam, 0.0, c.rho, 0.5, 1.0, a.graph)
         n = _lib.c_size_t()
         _lib.call("ct_admm_tv_workspace", ctypes.addressof(desc), ctypes.addressof(n))
         aws = _device.workspace(n.value)
@@ -79,6 +89,54 @@ def main(argv=None):
     if alg:
         out.update(interactions_per_s=a.batch * c.interactions / t, alg_gbs=alg / t / 1e9)
     print(json.dumps(out))
+
+
+def _time(fn, s, warmup, reps):
+    for _ in range(warmup):
+        fn()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        fn()
+        e1.record(s)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    return statistics.median(ts), min(ts)
+
+
+def _proj3d(a, dev):
+    """3D projector on a Volume3D workload (random volume: the projector's
+    time does not depend on the values)."""
+    c = workloads.C5
+    M = c.matrices()
+    if a.views:
+        M = M[: a.views]
+    A = linop.XRayTransform3D(c.shape, M, c.det_shape)
+    g = A.geometry()
+    if a.general:
+        g.kind = _lib.CT_PROJ3D_GENERAL
+    nv = len(M)
+    vol = torch.rand(c.shape, generator=torch.Generator().manual_seed(0)).to(dev)
+    proj = torch.empty(A.output_shape, device=dev)
+    fwd_b, adj_b = A.workspace_bytes()
+    ws = _device.workspace(max(fwd_b, adj_b))
+    s = torch.cuda.current_stream()
+    if a.op == "proj3d_fwd":
+        fn = lambda: _lib.call("ct_proj3d_fwd", ctypes.addressof(g), vol.data_ptr(), proj.data_ptr(), 1,
+                               ws.data_ptr(), ws.numel(), s.cuda_stream)
+        out_bytes = 4.0 * proj.numel()
+    else:
+        proj.copy_(torch.rand(A.output_shape, generator=torch.Generator().manual_seed(1)))
+        out = torch.empty_like(vol)
+        fn = lambda: _lib.call("ct_proj3d_adj", ctypes.addressof(g), proj.data_ptr(), out.data_ptr(), 1,
+                               ws.data_ptr(), ws.numel(), s.cuda_stream)
+        out_bytes = 4.0 * vol.numel()
+    t, tmin = _time(fn, s, a.warmup, a.reps)
+    inter = c.n**3 * nv
+    print(json.dumps({"op": a.op, "config": "c5", "views": nv, "kind": "general" if a.general else A.kind,
+                      "median_s": t, "min_s": tmin, "interactions_per_s": inter / t,
+                      "alg_gbs": (4.0 * inter + out_bytes) / t / 1e9}))
 
 
 if __name__ == "__main__":

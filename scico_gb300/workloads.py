@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List, Optional
+from typing import List, Tuple, Optional
 
 import numpy as np
 
@@ -104,6 +104,52 @@ class Slice2D:
 C1 = Slice2D(256, 180, 363, 0.01, 1.0, 50, 10, 1e-4, 0, 10, 0.01, 1)
 # C2: 512x512, 360 views, 725 bins, lambda 0.005, rho 2, 100 it, CG <= 10
 C2 = Slice2D(512, 360, 725, 0.005, 2.0, 100, 10, 1e-4, 2, 20, 0.005, 3)
+
+
+@dataclasses.dataclass
+class Volume3D:
+    """One 3D parallel-beam ADMM-TV problem: rotation about volume axis 0
+    (``matrices_from_euler_angles(shape, det, "X", angles[:, None])``),
+    g = lam_l1 ||Dx||_1 + lam_l21 ||Dx||_2,1 on one finite difference."""
+
+    n: int
+    n_views: int
+    det_shape: Tuple[int, int]
+    lam_l1: float
+    lam_l21: float
+    rho: float
+    maxiter: int
+    cg_maxiter: int
+    cg_tol: float
+    phantom_seed: int
+    n_ellipsoids: int
+    noise: float
+    noise_seed: int
+
+    @property
+    def shape(self) -> Tuple[int, int, int]:
+        return (self.n, self.n, self.n)
+
+    @property
+    def angles(self) -> np.ndarray:
+        return np.linspace(0, np.pi, self.n_views, endpoint=False)
+
+    @property
+    def interactions(self) -> int:
+        return self.n**3 * self.n_views
+
+    def matrices(self) -> np.ndarray:
+        from .linop import XRayTransform3D
+
+        return XRayTransform3D.matrices_from_euler_angles(self.shape, self.det_shape, "X", self.angles[:, None])
+
+    def phantom(self) -> np.ndarray:
+        return random_ellipsoids(self.n, self.n_ellipsoids, self.phantom_seed)
+
+
+# C5: 256^3, 360 views about axis 0, 256 x 363 detector, lambda 0.005 (L1 and
+# L21 on the same FD), rho 1, 30 it, CG <= 8
+C5 = Volume3D(256, 360, (256, 363), 0.005, 0.005, 1.0, 30, 8, 1e-4, 6, 30, 0.01, 7)
 
 
 def batched_configs(count: int = 64, seed: int = 3) -> List[Slice2D]:
