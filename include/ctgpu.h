@@ -135,8 +135,9 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
  * matrix row-major (entries 0..7), the axis along which the ray direction
  * has its largest component (entry 8, as a float), three unused. */
 #define CT_VIEW3D_STRIDE 12
-/* uint16 entries per view in the walk-order table of CT_PROJ3D_AXIS0. */
-#define CT_PROJ3D_ORDER 1024
+/* uint16 entries per view in the walk-order table of CT_PROJ3D_AXIS0 (one
+ * 16 x 16 pixel tile, entry = 16 * row + column). */
+#define CT_PROJ3D_ORDER 256
 
 /* Geometry kinds.  AXIS0: every view leaves volume axis 0 on detector rows
  * (M[0][1] = M[0][2] = M[1][0] = 0, |M[1][1]|, |M[1][2]| <= 1) and, in every
@@ -154,7 +155,7 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
  * keeps the (V,2,4) matrices as float32, scico/linop/xray/_xray3d.py:80) and
  * classify it.  matrices: host (n_views,2,4) float32.  views_out: host
  * n_views*CT_VIEW3D_STRIDE floats.  order_out: host n_views*CT_PROJ3D_ORDER
- * uint16 (the AXIS0 walk order of a 32x32 pixel tile, ordered along the
+ * uint16 (the AXIS0 walk order of a 16x16 pixel tile, ordered along the
  * detector), or NULL, in which case the kind is always GENERAL.
  * Fails with CT_ERR_UNSUPPORTED when a matrix has parallel rows (a view
  * that maps the volume onto a line).

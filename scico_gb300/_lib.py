@@ -35,7 +35,7 @@ CT_ERR_NO_DEVICE = 8
 
 CT_VIEW2D_STRIDE = 8
 CT_VIEW3D_STRIDE = 12
-CT_PROJ3D_ORDER = 1024
+CT_PROJ3D_ORDER = 256
 CT_PROJ3D_GENERAL = 0
 CT_PROJ3D_AXIS0 = 1
 

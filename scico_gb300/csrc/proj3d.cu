@@ -18,12 +18,13 @@
 //    exact) and the two other taps are zero, and the column weights of pixel
 //    (i1, i2) are the same for every slice.  The kernels compute each column
 //    weight once per view and tile and apply it to 32 slices at a time:
-//      forward  k_p3_ax0_fwd: lanes = slices; a warp walks a 32x32 pixel tile
-//               (staged in shared memory, [pixel][slice]) in the per-view
+//      forward  k_p3_ax0_fwd: lanes = slice pairs; a warp walks a 16x16 pixel
+//               tile (staged in shared memory, [pixel][slice]) in the per-view
 //               detector order of the order table, carrying the two open bins
-//               in registers and flushing into a per-warp [bin][slice]
-//               accumulator; accumulators go to a [group][view][col][slice]
-//               buffer that k_p3_ax0_rows transposes into the sinogram.
+//               in registers; each completed bin is added into the warp's own
+//               slice of a [group][view][col][slice] accumulator in global
+//               memory (old values loaded three bins ahead), which
+//               k_p3_ax0_rows transposes into the sinogram.
 //      adjoint  k_p3_ax0_adj: lanes = pixels along axis 2, 32 slices of
 //               accumulators per thread; the view's detector rows of the
 //               CTA's slices are staged as (y[c], y[c+1]) pairs, read with
@@ -45,16 +46,17 @@ namespace {
 
 constexpr int kVT = CT_VIEW3D_STRIDE;
 constexpr int kOrd = CT_PROJ3D_ORDER;
-constexpr int kTile = 32;  // AXIS0 forward pixel tile edge (kTile*kTile == kOrd)
-constexpr int kSvStride = 33;  // shared [pixel][slice] row stride (floats)
-constexpr int kTabChunk = 128;  // walk-table entries built per warp per pass
+constexpr int kTileJ = 16, kTileK = 16;  // AXIS0 forward pixel tile (axis 1 x axis 2)
+constexpr int kFwdSlices = 64;  // slices per forward CTA: two per lane
+constexpr int kSvStride = 66;   // shared [pixel][slice] row stride (floats, even: float2 reads)
+constexpr int kWalkGroup = 8;   // walk entries whose loads are issued together
 constexpr int kFwdViewsPerCta = 16;
-constexpr int kAccSpan = 2 * (32 - 1) + 6;  // accumulator bins per warp: 31(|m11|+|m12|) + 5
+constexpr int kFwdViewsPerWarp = kFwdViewsPerCta / 8;
 constexpr int kAdjRows = 16;  // AXIS0 adjoint tile: 16 (axis 1) x 32 (axis 2) pixels
 constexpr int kAdjTargetCtas = 304;
 constexpr int kGenViewChunk = 64;
 
-static_assert(kTile * kTile == kOrd, "order table covers one tile");
+static_assert(kTileJ * kTileK == kOrd, "order table covers one tile");
 
 // Device error word of the 3D kernels' internal checks (bit 0: forward
 // accumulator span, bit 1: adjoint window span).
@@ -87,6 +89,18 @@ __device__ __forceinline__ void edge3(float px, int& ul, float& t) {
   ul = (int)floorf(left);
 }
 
+// 4-byte global -> shared copy that bypasses registers; zero-fills when
+// `valid` is false (source size 0, nothing is read).
+__device__ __forceinline__ void cp_async4(uint32_t dst, const float* src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // AXIS0 forward
 // ---------------------------------------------------------------------------
@@ -98,19 +112,17 @@ struct Ax0FwdArgs {
   int S, NJ, NK, V, C, Spad;
   int tiles_k, n_tiles, G;
   int vpc;   // views per CTA
-  int span;  // accumulator bins per warp
-  int vec4;  // NK % 4 == 0 and vol 16-B aligned
   int* errflag;
 };
 
-// Bin range of one 32x32 tile for one view.  Every operation of the rounded
+// Bin range of one 16x32 tile for one view.  Every operation of the rounded
 // Px is monotone in each pixel index, so the tile's extremes are at corner
 // pixels; floor(left) of those, widened by one bin below and two above
 // (room for the second tap and the carried bin), gives [lo, hi).
 __device__ __forceinline__ void tile_bins(float m11, float m12, float m13, int j0, int k0,
                                           int& lo, int& hi) {
-  const float ja = (float)j0 + 0.5f, jb = (float)(j0 + kTile - 1) + 0.5f;
-  const float ka = (float)k0 + 0.5f, kb = (float)(k0 + kTile - 1) + 0.5f;
+  const float ja = (float)j0 + 0.5f, jb = (float)(j0 + kTileJ - 1) + 0.5f;
+  const float ka = (float)k0 + 0.5f, kb = (float)(k0 + kTileK - 1) + 0.5f;
   const float a0 = fmul(m11, ja), a1 = fmul(m11, jb);
   const float b0 = fmul(m12, ka), b1 = fmul(m12, kb);
   const float pmin = fadd(fminf(a0, a1) + fminf(b0, b1), m13);
@@ -119,123 +131,138 @@ __device__ __forceinline__ void tile_bins(float m11, float m12, float m13, int j
   hi = (int)floorf(pmax - 0.25f) + 3;
 }
 
-__global__ void __launch_bounds__(256, 1) k_p3_ax0_fwd(const Ax0FwdArgs a) {
+__global__ void __launch_bounds__(256, 2) k_p3_ax0_fwd(const Ax0FwdArgs a) {
   extern __shared__ __align__(16) float smem[];
-  float* sv = smem;                                      // [kOrd][kSvStride]
-  float4* tab = reinterpret_cast<float4*>(sv + kOrd * kSvStride);  // [8][kTabChunk]
-  float* acc = reinterpret_cast<float*>(tab + 8 * kTabChunk);      // [8][span][32]
+  float* sv = smem;                                           // [kOrd][kSvStride]
+  float2* tab = reinterpret_cast<float2*>(sv + kOrd * kSvStride);  // [8][kOrd]
+  __shared__ float vpar[kFwdViewsPerCta][4];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = blockIdx.x, i0 = blockIdx.y * 32, v0 = blockIdx.z * a.vpc;
+  const int g = blockIdx.x, i0 = blockIdx.y * kFwdSlices, v0 = blockIdx.z * a.vpc;
   const int nvh = min(a.vpc, a.V - v0);
-  float* accw = acc + (size_t)warp * a.span * 32;
-  float4* tabw = tab + warp * kTabChunk;
+  float2* tabw = tab + warp * kOrd;
+  const uint32_t sv_s = (uint32_t)__cvta_generic_to_shared(sv);
 
-  // zero this CTA's slice of the output accumulator and the warp accumulators
+  // zero this CTA's slices of the output accumulator; fetch the CTA's view
+  // parameters (M[1][1..3]) and each warp's walk orders (entry 32u + lane),
+  // which do not depend on the tile
   for (int v = 0; v < nvh; ++v) {
     float* o = a.acc_out + ((size_t)g * a.V + v0 + v) * a.C * a.Spad + i0;
-    for (int e = tid; e < a.C * 32; e += 256) o[(size_t)(e >> 5) * a.Spad + (e & 31)] = 0.0f;
+    for (int e = tid; e < a.C * kFwdSlices; e += 256)
+      o[(size_t)(e / kFwdSlices) * a.Spad + (e % kFwdSlices)] = 0.0f;
   }
-  for (int e = tid; e < 8 * a.span * 32; e += 256) acc[e] = 0.0f;
+  if (tid < 3 * nvh) vpar[tid / 3][tid % 3] = a.views[(size_t)(v0 + tid / 3) * kVT + 5 + tid % 3];
+  int ordr[kFwdViewsPerWarp][kOrd / 32];
+#pragma unroll
+  for (int w = 0; w < kFwdViewsPerWarp; ++w) {
+    const int vi = warp + 8 * w;
+    const uint16_t* ord = a.order + (size_t)(v0 + min(vi, nvh - 1)) * kOrd;
+#pragma unroll
+    for (int u = 0; u < kOrd / 32; ++u) ordr[w][u] = __ldg(ord + 32 * u + lane);
+  }
   __syncthreads();
 
   for (int t = g; t < a.n_tiles; t += a.G) {
-    const int j0 = (t / a.tiles_k) * kTile, k0 = (t % a.tiles_k) * kTile;
-    // stage vol[i0+s][j0+j][k0+k] as sv[(j*32+k)*33 + s]: one warp
-    // instruction covers four consecutive slices of one row (bank-conflict
-    // free, see the index arithmetic: bank = (k + s) mod 32)
-#pragma unroll 4
-    for (int q = 0; q < 32; ++q) {
-      const int R = (q * 8 + warp) * 4 + (lane >> 3);
-      const int s = R & 31, j = R >> 5, kq = (lane & 7) * 4;
-      const int gi = i0 + s, gj = j0 + j, gk = k0 + kq;
-      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gi < a.S && gj < a.NJ) {
-        const float* src = a.vol + ((size_t)gi * a.NJ + gj) * a.NK + gk;
-        if (a.vec4 && gk + 3 < a.NK) {
-          x = __ldg(reinterpret_cast<const float4*>(src));
-        } else {
-          if (gk < a.NK) x.x = __ldg(src);
-          if (gk + 1 < a.NK) x.y = __ldg(src + 1);
-          if (gk + 2 < a.NK) x.z = __ldg(src + 2);
-          if (gk + 3 < a.NK) x.w = __ldg(src + 3);
-        }
-      }
-      float* d = sv + (j * kTile + kq) * kSvStride + s;
-      d[0] = x.x;
-      d[kSvStride] = x.y;
-      d[2 * kSvStride] = x.z;
-      d[3 * kSvStride] = x.w;
+    const int j0 = (t / a.tiles_k) * kTileJ, k0 = (t % a.tiles_k) * kTileK;
+    // stage vol[i0+s][j0+j][k0+k] as sv[(j*16+k)*66 + s] with register-free
+    // 4-byte async copies, all in flight at once.  A warp copies two
+    // 16-float rows, slices s and s+1 of one j (lanes = k, then the second
+    // half-warp): shared banks 2k + s and 2k + s + 1 are all distinct
+#pragma unroll 8
+    for (int q = 0; q < kOrd * kFwdSlices / 256; ++q) {
+      const int row = 2 * (q * 8 + warp) + (lane >> 4);  // (s, j) = (row % 64, row / 64)
+      const int s = row % kFwdSlices, j = row / kFwdSlices, k = lane & 15;
+      const int gi = i0 + s, gj = j0 + j, gk = k0 + k;
+      const bool ok = gi < a.S && gj < a.NJ && gk < a.NK;
+      const float* src = ok ? a.vol + ((size_t)gi * a.NJ + gj) * a.NK + gk : a.vol;
+      cp_async4(sv_s + (uint32_t)((j * kTileK + k) * kSvStride + s) * 4u, src, ok);
     }
+    cp_async_wait_all();
     __syncthreads();
 
-    for (int vi = warp; vi < nvh; vi += 8) {
+#pragma unroll 1
+    for (int w = 0; w < kFwdViewsPerWarp; ++w) {
+      const int vi = warp + 8 * w;
+      if (vi >= nvh) break;
       const int v = v0 + vi;
-      const float* m = a.views + (size_t)v * kVT;
-      const float m11 = m[5], m12 = m[6], m13 = m[7];
+      const float m11 = vpar[vi][0], m12 = vpar[vi][1], m13 = vpar[vi][2];
       int lo, hi;
       tile_bins(m11, m12, m13, j0, k0, lo, hi);
       const int nb = hi - lo;
-      if (nb > a.span) {  // cannot happen for |m11|, |m12| <= 1
-        if (lane == 0) atomicOr(a.errflag, 1);
-        continue;
-      }
-      const uint16_t* ord = a.order + (size_t)v * kOrd;
-      int cur = 1;  // accumulator row of the open bin (relative to lo)
-      float A = 0.f, B = 0.f;
-      for (int ch = 0; ch < kOrd; ch += kTabChunk) {
+      // table entries: (w0, bin << 16 | pixel*66).  The second tap's weight
+      // is 1 - w0 = 2*(0.5 - t1) exactly; taps on columns off the detector
+      // are accumulated and never written out, so no masks here
+      int po[kOrd / 32];  // this view's order entries (register select, no local memory)
 #pragma unroll
-        for (int q = 0; q < kTabChunk / 32; ++q) {
-          const int p = ord[ch + q * 32 + lane];
-          const int pj = p >> 5, pk = p & 31;
-          const float x1 = (float)(j0 + pj) + 0.5f, x2 = (float)(k0 + pk) + 0.5f;
-          // Px_1 with M[1][0] = 0: the x0 term is an exact zero
-          const float px = fadd(fadd(fmul(m11, x1), fmul(m12, x2)), m13);
-          int ul;
-          float t1;
-          edge3(px, ul, t1);
-          const float w0 = (ul >= 0 && ul < a.C) ? fmul(2.0f, t1) : 0.0f;
-          const float w1 = (ul + 1 >= 0 && ul + 1 < a.C) ? fmul(2.0f, fsub(0.5f, t1)) : 0.0f;
-          int rel = ul - lo;
-          rel = min(max(rel, 0), nb - 2);  // in range: Px is monotone, extremes at corners
-          tabw[q * 32 + lane] =
-              make_float4(w0, w1, __int_as_float(rel * 32), __int_as_float(p * kSvStride));
-        }
-        __syncwarp();
-        const int curb = cur * 32;
-        int cb = curb;
-#pragma unroll 8
-        for (int e = 0; e < kTabChunk; ++e) {
-          const float4 T = tabw[e];
-          const float x = sv[__float_as_int(T.w) + lane];
-          const int rb = __float_as_int(T.z);
-          if (rb != cb) {  // warp-uniform: every lane reads the same entry
-            accw[cb + lane] += A;
-            if (rb == cb + 32) {
-              A = B;
-            } else {
-              accw[cb + 32 + lane] += B;
-              A = 0.f;
+      for (int u = 0; u < kOrd / 32; ++u) {
+        po[u] = ordr[0][u];
+#pragma unroll
+        for (int w2 = 1; w2 < kFwdViewsPerWarp; ++w2) po[u] = w == w2 ? ordr[w2][u] : po[u];
+      }
+#pragma unroll
+      for (int u = 0; u < kOrd / 32; ++u) {
+        const int p = po[u];
+        const float x1 = (float)(j0 + p / kTileK) + 0.5f, x2 = (float)(k0 + p % kTileK) + 0.5f;
+        // Px_1 with M[1][0] = 0: the x0 term is an exact zero
+        const float px = fadd(fadd(fmul(m11, x1), fmul(m12, x2)), m13);
+        int ul;
+        float t1;
+        edge3(px, ul, t1);
+        const int rel = min(max(ul - lo, 0), nb - 2);  // in range: extremes at corners
+        tabw[32 * u + lane] = make_float2(fmul(2.0f, t1), __int_as_float((rel << 16) | (p * kSvStride)));
+      }
+      __syncwarp();
+      // this warp's slices of the output accumulator: column c at o[c * Spad]
+      float2* o = reinterpret_cast<float2*>(a.acc_out + (((size_t)g * a.V + v) * a.C) * a.Spad + i0) + lane;
+      const size_t ostride = (size_t)a.Spad / 2;
+      auto old_at = [&](int c) {
+        return (c >= 0 && c < a.C) ? o[(size_t)c * ostride] : make_float2(0.f, 0.f);
+      };
+      auto put = [&](int c, float2 val) {
+        if (c >= 0 && c < a.C) o[(size_t)c * ostride] = val;
+      };
+      // Open bin cb (tile-relative): its total is cin + sum w0*x over its
+      // own pixels (a); the next bin receives sum (1-w0)*x = s - a.  r0..r2
+      // hold the accumulator's values of bins cb..cb+2, loaded ahead.
+      int cb = 0;
+      float2 cin = make_float2(0.f, 0.f), av = cin, sx = cin;
+      float2 r0 = old_at(lo), r1 = old_at(lo + 1), r2 = old_at(lo + 2);
+      for (int e0 = 0; e0 < kOrd; e0 += kWalkGroup) {
+        float2 T[kWalkGroup], x[kWalkGroup];
+#pragma unroll
+        for (int u = 0; u < kWalkGroup; ++u) T[u] = tabw[e0 + u];
+#pragma unroll
+        for (int u = 0; u < kWalkGroup; ++u)
+          x[u] = *reinterpret_cast<const float2*>(sv + (__float_as_int(T[u].y) & 0xffff) + 2 * lane);
+#pragma unroll
+        for (int u = 0; u < kWalkGroup; ++u) {
+          const int rb = __float_as_int(T[u].y) >> 16;
+          if (__builtin_expect(rb != cb, 0)) {  // warp-uniform: every lane reads the same entry
+            put(lo + cb, make_float2(r0.x + (cin.x + av.x), r0.y + (cin.y + av.y)));
+            const float2 nxt = make_float2(sx.x - av.x, sx.y - av.y);
+            if (rb == cb + 1) {
+              r0 = r1;
+              r1 = r2;
+              r2 = old_at(lo + cb + 3);
+              cin = nxt;
+            } else {  // a jump (rare: rounding at near-ties of the order)
+              put(lo + cb + 1, make_float2(r1.x + nxt.x, r1.y + nxt.y));
+              r0 = old_at(lo + rb);
+              r1 = old_at(lo + rb + 1);
+              r2 = old_at(lo + rb + 2);
+              cin = make_float2(0.f, 0.f);
             }
-            B = 0.f;
+            av = make_float2(0.f, 0.f);
+            sx = av;
             cb = rb;
           }
-          A = fmaf(T.x, x, A);
-          B = fmaf(T.y, x, B);
+          av.x = fmaf(T[u].x, x[u].x, av.x);
+          av.y = fmaf(T[u].x, x[u].y, av.y);
+          sx.x += x[u].x;
+          sx.y += x[u].y;
         }
-        cur = cb >> 5;
-        __syncwarp();
       }
-      accw[cur * 32 + lane] += A;
-      accw[(cur + 1) * 32 + lane] += B;
-      __syncwarp();
-      // add the tile's bins into the output accumulator and clear them
-      float* o = a.acc_out + (((size_t)g * a.V + v) * a.C) * a.Spad + i0 + lane;
-      for (int r = 0; r < nb; ++r) {
-        const int c = lo + r;
-        const float val = accw[r * 32 + lane];
-        accw[r * 32 + lane] = 0.f;
-        if (c >= 0 && c < a.C) o[(size_t)c * a.Spad] += val;
-      }
+      put(lo + cb, make_float2(r0.x + (cin.x + av.x), r0.y + (cin.y + av.y)));
+      put(lo + cb + 1, make_float2(r1.x + (sx.x - av.x), r1.y + (sx.y - av.y)));
       __syncwarp();
     }
     __syncthreads();
@@ -273,11 +300,15 @@ struct Ax0AdjArgs {
   float* out;         // (S, NJ, NK), or split partials
   const float* views;
   int S, NJ, NK, V, R, C, row_offset;
-  int W;  // staged bins per slice row
   int per_split;
   size_t split_stride;
   int* errflag;
 };
+
+// staged detector columns per slice row of the 16 x 32 adjoint tile:
+// 15|m11| + 31|m12| + 5 <= 51 for |m11|, |m12| <= 1
+constexpr int kAW = (kAdjRows - 1) + 31 + 6;
+constexpr int kAdjStage = (32 * kAW + 255) / 256;  // staging slots per thread
 
 __device__ __forceinline__ float2 ld_shared_f2(uint32_t addr) {
   float2 v;
@@ -285,8 +316,20 @@ __device__ __forceinline__ float2 ld_shared_f2(uint32_t addr) {
   return v;
 }
 
+// Window [lo, lo + nb) of detector columns that the 16x32 tile at (j0, k0)
+// reads in one view (corner bound as tile_bins, two extra columns above).
+__device__ __forceinline__ void adj_window(float m11, float m12, float m13, int j0, int k0,
+                                           int& lo, int& nb) {
+  const float ja = (float)j0 + 0.5f, jb = (float)(j0 + kAdjRows - 1) + 0.5f;
+  const float ka = (float)k0 + 0.5f, kb = (float)(k0 + 31) + 0.5f;
+  const float a0 = fmul(m11, ja), a1 = fmul(m11, jb), b0 = fmul(m12, ka), b1 = fmul(m12, kb);
+  lo = (int)floorf(fadd(fminf(a0, a1) + fminf(b0, b1), m13) - 0.25f) - 1;
+  nb = (int)floorf(fadd(fmaxf(a0, a1) + fmaxf(b0, b1), m13) - 0.25f) + 3 - lo;
+}
+
 __global__ void __launch_bounds__(256, 2) k_p3_ax0_adj(const Ax0AdjArgs a) {
-  extern __shared__ __align__(16) float2 sy[];  // [2][32][W]
+  // [2][32][kAW] pairs (y[c], y[c+1]) of the slice rows, double-buffered
+  __shared__ __align__(16) float2 sy[2 * 32 * kAW];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int k0 = blockIdx.x * 32, j0 = blockIdx.y * kAdjRows;
   const int nsg = (a.S + 31) / 32;
@@ -296,40 +339,55 @@ __global__ void __launch_bounds__(256, 2) k_p3_ax0_adj(const Ax0AdjArgs a) {
   const int jj[2] = {j0 + warp, j0 + warp + 8};
   const int vs = split * a.per_split, ve = min(a.V, vs + a.per_split);
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sy);
+
+  // issue the copies of view v's window into buffer `buf`
+  auto stage = [&](int v, int buf, int lo, int nb) {
+    const float* src = a.proj + (size_t)v * a.R * a.C;
+#pragma unroll
+    for (int it = 0; it < kAdjStage; ++it) {
+      const int e = tid + 256 * it;
+      if (e < 32 * kAW) {
+        const int s = e / kAW, bl = e - s * kAW;
+        const int r = i0 + s + a.row_offset, c = lo + bl;
+        const bool row_ok = bl < nb && i0 + s < a.S && r >= 0 && r < a.R;
+        const float* row = src + (size_t)(row_ok ? r : 0) * a.C;
+        const bool ok0 = row_ok && c >= 0 && c < a.C;
+        const bool ok1 = row_ok && c + 1 >= 0 && c + 1 < a.C;
+        const uint32_t d = sbase + (uint32_t)(buf * 32 * kAW + e) * 8u;
+        cp_async4(d, ok0 ? row + c : a.proj, ok0);
+        cp_async4(d + 4, ok1 ? row + c + 1 : a.proj, ok1);
+      }
+    }
+  };
+
   float acc[2][32];
 #pragma unroll
   for (int q = 0; q < 2; ++q)
 #pragma unroll
     for (int s = 0; s < 32; ++s) acc[q][s] = 0.f;
 
+  int lo = 0, nb = 0;
+  if (vs < ve) {
+    const float* m = a.views + (size_t)vs * kVT;
+    adj_window(m[5], m[6], m[7], j0, k0, lo, nb);
+    stage(vs, 0, lo, min(nb, kAW));
+    cp_async_wait_all();
+  }
+  __syncthreads();
   for (int v = vs; v < ve; ++v) {
     const int buf = (v - vs) & 1;
     const float* m = a.views + (size_t)v * kVT;
     const float m11 = m[5], m12 = m[6], m13 = m[7];
-    // bin window of the 16x32 tile (corner bound, as tile_bins)
-    const float ja = (float)j0 + 0.5f, jb = (float)(j0 + kAdjRows - 1) + 0.5f;
-    const float ka = (float)k0 + 0.5f, kb = (float)(k0 + 31) + 0.5f;
-    const float a0 = fmul(m11, ja), a1 = fmul(m11, jb), b0 = fmul(m12, ka), b1 = fmul(m12, kb);
-    const int lo = (int)floorf(fadd(fminf(a0, a1) + fminf(b0, b1), m13) - 0.25f) - 1;
-    const int hi = (int)floorf(fadd(fmaxf(a0, a1) + fmaxf(b0, b1), m13) - 0.25f) + 3;
-    const int nb = min(hi - lo, a.W);
-    if (hi - lo > a.W && tid == 0) atomicOr(a.errflag, 2);
-    // stage rows i0+s+row_offset, columns lo .. lo+nb-1 as (y[c], y[c+1])
-    float2* dst = sy + (size_t)buf * 32 * a.W;
-    const float* src = a.proj + (size_t)v * a.R * a.C;
-    for (int e = tid; e < 32 * nb; e += 256) {
-      const int s = e / nb, bl = e - s * nb;
-      const int r = i0 + s + a.row_offset, c = lo + bl;
-      float y0 = 0.f, y1 = 0.f;
-      if (i0 + s < a.S && r >= 0 && r < a.R) {
-        const float* row = src + (size_t)r * a.C;
-        if (c >= 0 && c < a.C) y0 = __ldg(row + c);
-        if (c + 1 >= 0 && c + 1 < a.C) y1 = __ldg(row + c + 1);
-      }
-      dst[s * a.W + bl] = make_float2(y0, y1);
+    if (nb > kAW && tid == 0) atomicOr(a.errflag, 2);  // cannot happen for |m| <= 1
+    const int nbc = min(nb, kAW);
+    // next view's copies run while this view is computed
+    int lo_n = 0, nb_n = 0;
+    if (v + 1 < ve) {
+      const float* mn = a.views + (size_t)(v + 1) * kVT;
+      adj_window(mn[5], mn[6], mn[7], j0, k0, lo_n, nb_n);
+      stage(v + 1, buf ^ 1, lo_n, min(nb_n, kAW));
     }
-    __syncthreads();
-    const uint32_t vbase = sbase + (uint32_t)(buf * 32 * a.W) * 8u;
+    const uint32_t vbase = sbase + (uint32_t)(buf * 32 * kAW) * 8u;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const float x1 = (float)jj[q] + 0.5f, x2 = (float)k + 0.5f;
@@ -340,7 +398,7 @@ __global__ void __launch_bounds__(256, 2) k_p3_ax0_adj(const Ax0AdjArgs a) {
       float w0 = (ul >= 0 && ul < a.C) ? fmul(2.0f, t1) : 0.0f;
       float w1 = (ul + 1 >= 0 && ul + 1 < a.C) ? fmul(2.0f, fsub(0.5f, t1)) : 0.0f;
       int rel = ul - lo;
-      if (rel < 0 || rel >= nb - 1) {  // outside the staged window (cannot happen)
+      if (rel < 0 || rel >= nbc - 1) {  // outside the staged window (cannot happen)
         rel = 0;
         w0 = 0.f;
         w1 = 0.f;
@@ -348,11 +406,15 @@ __global__ void __launch_bounds__(256, 2) k_p3_ax0_adj(const Ax0AdjArgs a) {
       const uint32_t addr = vbase + (uint32_t)rel * 8u;
 #pragma unroll
       for (int s = 0; s < 32; ++s) {
-        const float2 y = ld_shared_f2(addr + (uint32_t)(s * a.W) * 8u);
+        const float2 y = ld_shared_f2(addr + (uint32_t)(s * kAW * 8));
         acc[q][s] = fmaf(w0, y.x, acc[q][s]);
         acc[q][s] = fmaf(w1, y.y, acc[q][s]);
       }
     }
+    cp_async_wait_all();
+    __syncthreads();
+    lo = lo_n;
+    nb = nb_n;
   }
   float* out = a.out + (size_t)split * a.split_stride;
 #pragma unroll
@@ -524,11 +586,8 @@ __global__ void k_p3_sum_splits(const float* __restrict__ part, float* __restric
 // ---------------------------------------------------------------------------
 struct Proj3dPlan {
   // AXIS0 forward
-  int Spad = 0, tiles_k = 0, n_tiles = 0, G = 1, vpc = kFwdViewsPerCta, span = 0;
+  int Spad = 0, tiles_k = 0, n_tiles = 0, G = 1, vpc = kFwdViewsPerCta;
   size_t fwd_smem = 0;
-  // AXIS0 adjoint
-  int W = 0;
-  size_t adj_smem = 0;
   // adjoint view splits (both kinds)
   int nsplit = 1, per_split = 0;
   size_t fwd_bytes = 0, adj_bytes = 0;
@@ -560,19 +619,23 @@ Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch) {
   const int C = g->det_shape[1];
   const int sms = std::max(1, sm_count());
   if (g->kind == CT_PROJ3D_AXIS0) {
-    p.Spad = (S + 31) / 32 * 32;
-    p.tiles_k = (NK + kTile - 1) / kTile;
-    p.n_tiles = p.tiles_k * ((NJ + kTile - 1) / kTile);
-    p.span = kAccSpan;
-    const long base = (long)(p.Spad / 32) * ((V + p.vpc - 1) / p.vpc);
-    int G = 1;
-    while (G < 4 && G < p.n_tiles && base * G < 3L * sms) ++G;
-    p.G = G;
-    p.fwd_smem = sizeof(float) * (size_t)kOrd * kSvStride + sizeof(float4) * 8 * kTabChunk +
-                 sizeof(float) * 8 * (size_t)p.span * 32;
+    p.Spad = (S + kFwdSlices - 1) / kFwdSlices * kFwdSlices;
+    p.tiles_k = (NK + kTileK - 1) / kTileK;
+    p.n_tiles = p.tiles_k * ((NJ + kTileJ - 1) / kTileJ);
+    const long base = (long)(p.Spad / kFwdSlices) * ((V + p.vpc - 1) / p.vpc);
+    // tile groups: fill the GPU (two CTAs per SM) with a small last wave
+    const long slots = 2L * sms;
+    double best = -1.0;
+    for (int G = 1; G <= std::min(8, p.n_tiles); ++G) {
+      const double waves = (double)(base * G) / (double)slots;
+      const double score = std::min(1.0, waves) * waves / std::ceil(waves);
+      if (score > best + 1e-9) {
+        best = score;
+        p.G = G;
+      }
+    }
+    p.fwd_smem = sizeof(float) * (size_t)kOrd * kSvStride + sizeof(float2) * 8 * kOrd;
     p.fwd_bytes = round_up(sizeof(float) * (size_t)p.G * V * C * p.Spad, 256);
-    p.W = (kAdjRows - 1) + 31 + 6;
-    p.adj_smem = sizeof(float2) * 2 * 32 * (size_t)p.W;
     const long ctas = (long)((NK + 31) / 32) * ((NJ + kAdjRows - 1) / kAdjRows) * (p.Spad / 32);
     int ns = 1;
     if (ctas < kAdjTargetCtas) ns = (int)((kAdjTargetCtas + ctas - 1) / ctas);
@@ -666,7 +729,7 @@ ct_status ct_proj3d_views(const float* matrices, int32_t n_views, const int32_t*
     for (int v = 0; v < n_views; ++v) {
       const float* m = matrices + (size_t)v * 8;
       for (int p = 0; p < CT_PROJ3D_ORDER; ++p)
-        key[p] = {(double)m[5] * (p >> 5) + (double)m[6] * (p & 31), p};
+        key[p] = {(double)m[5] * (p / ct::kTileK) + (double)m[6] * (p % ct::kTileK), p};
       std::stable_sort(key.begin(), key.end(),
                        [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
                          return a.first < b.first;
@@ -726,10 +789,8 @@ ct_status ct_proj3d_fwd(const ct_geom3d* g, const float* vol, float* proj, int32
       a.n_tiles = p.n_tiles;
       a.G = p.G;
       a.vpc = p.vpc;
-      a.span = p.span;
-      a.vec4 = ((NK & 3) == 0 && aligned(vol, 16)) ? 1 : 0;
       a.errflag = ef;
-      dim3 grid(p.G, p.Spad / 32, (V + p.vpc - 1) / p.vpc);
+      dim3 grid(p.G, p.Spad / kFwdSlices, (V + p.vpc - 1) / p.vpc);
       k_p3_ax0_fwd<<<grid, 256, p.fwd_smem, s>>>(a);
       st = launch_check("k_p3_ax0_fwd");
       if (st != CT_OK) return st;
@@ -768,12 +829,6 @@ ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol, int32
   float* part = static_cast<float*>(workspace);
   int* ef = errflag3_ptr();
   if (!ef) return fail(CT_ERR_CUDA, "proj3d: error-word address unavailable");
-  if (g->kind == CT_PROJ3D_AXIS0) {
-    st = cuda_check(cudaFuncSetAttribute(k_p3_ax0_adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)p.adj_smem),
-                    "k_p3_ax0_adj smem attribute");
-    if (st != CT_OK) return st;
-  }
   for (int b = 0; b < batch; ++b) {
     float* dst = p.nsplit > 1 ? part : vol + b * vol_n;
     if (g->kind == CT_PROJ3D_AXIS0) {
@@ -788,12 +843,11 @@ ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol, int32
       a.R = R;
       a.C = C;
       a.row_offset = g->row_offset;
-      a.W = p.W;
       a.per_split = p.per_split;
       a.split_stride = vol_n;
       a.errflag = ef;
       dim3 grid((NK + 31) / 32, (NJ + kAdjRows - 1) / kAdjRows, (p.Spad / 32) * p.nsplit);
-      k_p3_ax0_adj<<<grid, 256, p.adj_smem, s>>>(a);
+      k_p3_ax0_adj<<<grid, 256, 0, s>>>(a);
       st = launch_check("k_p3_ax0_adj");
     } else {
       dim3 grid((unsigned)((vol_n + 255) / 256), p.nsplit);

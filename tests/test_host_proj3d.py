@@ -61,12 +61,12 @@ def test_classification(shape, det, seq, kind, off):
     d = np.cross(M32[:, 0, :3].astype(np.float64), M32[:, 1, :3].astype(np.float64))
     assert np.array_equal(views[:, 8], np.argmax(np.abs(d), axis=1).astype(np.float32))
     if kind == _lib.CT_PROJ3D_AXIS0:
-        # the walk order of each view is a permutation of the 32x32 tile,
+        # the walk order of each view is a permutation of the 16x16 tile,
         # non-decreasing in the tile's detector coordinate
         for v in range(len(M)):
             p = order[v].astype(np.int64)
-            assert np.array_equal(np.sort(p), np.arange(1024))
-            key = M32[v, 1, 1].astype(np.float64) * (p >> 5) + M32[v, 1, 2].astype(np.float64) * (p & 31)
+            assert np.array_equal(np.sort(p), np.arange(_lib.CT_PROJ3D_ORDER))
+            key = M32[v, 1, 1].astype(np.float64) * (p // 16) + M32[v, 1, 2].astype(np.float64) * (p % 16)
             assert np.all(np.diff(key) >= 0)
         # AXIS0 also needs the slice -> row map of the oracle's weights
         for v in range(len(M)):
@@ -121,7 +121,7 @@ def test_workspace_query_and_checks():
     lib = _lib.load()
     assert lib.ct_proj3d_workspace(ctypes.byref(g), 1, ctypes.byref(fwd), ctypes.byref(adj)) == _lib.CT_OK
     # [groups][views][cols][slices padded to 32] float32
-    assert fwd.value >= 3 * 90 * 64 * 4 and fwd.value % (3 * 90 * 64 * 4) == 0
+    assert fwd.value >= 3 * 90 * 64 * 4 and fwd.value % (3 * 90 * 64 * 4) == 0  # slices padded to 64
     g.order = None
     assert lib.ct_proj3d_workspace(ctypes.byref(g), 1, ctypes.byref(fwd), ctypes.byref(adj)) == \
         _lib.CT_ERR_INVALID_ARG
