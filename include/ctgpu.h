@@ -359,6 +359,35 @@ ct_status ct_admm_tv_solve(const ct_admm_tv_desc* d, const float* y, float* x,
                            double* itstat_dev, int32_t iter0, void* workspace,
                            size_t workspace_bytes, ct_stream_t stream);
 
+/*
+ * The same solver for 3D parallel-beam CT (XRayTransform3D,
+ * scico/linop/xray/_xray3d.py), as in scico's ct_3d_tv_* examples:
+ * D = FiniteDifference(append=0) over the three volume axes, stacked
+ * (3, n0, n1, n2); z_i/u_i are n_terms x 3 x n0 x n1 x n2.  Fields and
+ * semantics as ct_admm_tv_desc.
+ */
+typedef struct ct_admm_tv3d_desc {
+  ct_geom3d geom;
+  int32_t maxiter;
+  int32_t cg_maxiter;
+  double cg_tol;
+  double cg_atol;
+  double lam_l21;
+  double lam_l1;
+  double rho;
+  double loss_scale;
+  double alpha;
+  int32_t use_graph;
+} ct_admm_tv3d_desc;
+
+ct_status ct_admm_tv3d_workspace(const ct_admm_tv3d_desc* d, size_t* bytes);
+ct_status ct_admm_tv3d_state(const ct_admm_tv3d_desc* d, size_t* z_offset,
+                             size_t* u_offset, int32_t* n_terms);
+/* y: projections (n_views x rows x cols); x: volume (n0 x n1 x n2). */
+ct_status ct_admm_tv3d_solve(const ct_admm_tv3d_desc* d, const float* y, float* x,
+                             double* itstat_dev, int32_t iter0, void* workspace,
+                             size_t workspace_bytes, ct_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -214,34 +214,44 @@ def xray3d_calc_weights(input_shape, matrix, det_shape, dtype=np.float32):
     return ul, ul_w, ur_w, ll_w, lr_w
 
 
-def xray3d_project(im: np.ndarray, matrices: np.ndarray, det_shape, dtype=np.float32) -> np.ndarray:
-    """(views, *det_shape) projections (_xray3d.py:110-159), 4 scatter-adds per view."""
-    im = np.asarray(im, dtype=dtype)
+def xray3d_project(im: np.ndarray, matrices: np.ndarray, det_shape, dtype=np.float32, acc_dtype=None) -> np.ndarray:
+    """(views, *det_shape) projections (_xray3d.py:110-159), 4 scatter-adds per view.
+
+    Weights are computed in `dtype`; acc_dtype (default `dtype`) is the
+    precision of the voxel values and the sums.  The weight model is
+    discontinuous where left is an exact integer, so float64 weights move
+    different voxels than the reference's float32 ones: use dtype=float32,
+    acc_dtype=float64 for a float32-model reference with exact sums."""
+    acc = np.dtype(dtype if acc_dtype is None else acc_dtype).type
+    im = np.asarray(im, dtype=acc)
     nv = len(matrices)
-    out = np.zeros((nv,) + tuple(det_shape), dtype=dtype)
+    out = np.zeros((nv,) + tuple(det_shape), dtype=acc)
     for v in range(nv):
         ul, w00, w10, w01, w11 = xray3d_calc_weights(im.shape, matrices[v], det_shape, dtype)
-        proj = np.zeros(det_shape, dtype=dtype)
+        proj = np.zeros(det_shape, dtype=acc)
         for (d0, d1), w in (((0, 0), w00), ((1, 0), w10), ((0, 1), w01), ((1, 1), w11)):
             a, b = ul[0] + d0, ul[1] + d1
             ok = (a >= 0) & (a < det_shape[0]) & (b >= 0) & (b < det_shape[1])  # mode="drop"
-            np.add.at(proj, (a[ok], b[ok]), (w * im)[ok])
+            np.add.at(proj, (a[ok], b[ok]), (w.astype(acc) * im)[ok])
         out[v] = proj
     return out
 
 
-def xray3d_back_project(proj: np.ndarray, matrices: np.ndarray, input_shape, dtype=np.float32) -> np.ndarray:
-    """Back projection (_xray3d.py:161-204): view-sequential scan of 4 gathers."""
-    proj = np.asarray(proj, dtype=dtype)
+def xray3d_back_project(proj: np.ndarray, matrices: np.ndarray, input_shape, dtype=np.float32,
+                        acc_dtype=None) -> np.ndarray:
+    """Back projection (_xray3d.py:161-204): view-sequential scan of 4 gathers
+    (weights in `dtype`, values and sums in acc_dtype, as xray3d_project)."""
+    acc = np.dtype(dtype if acc_dtype is None else acc_dtype).type
+    proj = np.asarray(proj, dtype=acc)
     det_shape = proj.shape[1:]
-    HTy = np.zeros(input_shape, dtype=dtype)
+    HTy = np.zeros(input_shape, dtype=acc)
     for v in range(len(matrices)):
         ul, w00, w10, w01, w11 = xray3d_calc_weights(input_shape, matrices[v], det_shape, dtype)
         y = proj[v]
         for (d0, d1), w in (((0, 0), w00), ((1, 0), w10), ((0, 1), w01), ((1, 1), w11)):
             a = np.clip(ul[0] + d0, 0, det_shape[0] - 1)
             b = np.clip(ul[1] + d1, 0, det_shape[1] - 1)
-            HTy = HTy + y[a, b] * w  # :200-203 (weights are 0 out of range)
+            HTy = HTy + y[a, b] * w.astype(acc)  # :200-203 (weights are 0 out of range)
     return HTy
 
 

@@ -121,6 +121,22 @@ class AdmmTvDesc(ctypes.Structure):
     ]
 
 
+class AdmmTv3dDesc(ctypes.Structure):
+    _fields_ = [
+        ("geom", Geom3D),
+        ("maxiter", c_int32),
+        ("cg_maxiter", c_int32),
+        ("cg_tol", c_double),
+        ("cg_atol", c_double),
+        ("lam_l21", c_double),
+        ("lam_l1", c_double),
+        ("rho", c_double),
+        ("loss_scale", c_double),
+        ("alpha", c_double),
+        ("use_graph", c_int32),
+    ]
+
+
 P = c_void_p
 _SIGNATURES = {
     "ct_version": (c_char_p, []),
@@ -149,6 +165,9 @@ _SIGNATURES = {
     "ct_admm_tv_workspace": (ctypes.c_int, [P, P]),
     "ct_admm_tv_state": (ctypes.c_int, [P, P, P, P]),
     "ct_admm_tv_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),
+    "ct_admm_tv3d_workspace": (ctypes.c_int, [P, P]),
+    "ct_admm_tv3d_state": (ctypes.c_int, [P, P, P, P]),
+    "ct_admm_tv3d_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),
 }
 
 _lock = threading.Lock()

@@ -1,10 +1,13 @@
-// Fused ADMM-TV solver for 2D parallel-beam CT.
+// Fused ADMM-TV solver for 2D and 3D parallel-beam CT.
 //
 // Solves  min_x scale ||A x - y||^2 + lam21 ||D x||_{2,1} + lam1 ||D x||_1
 // with scico's ADMM + LinearSubproblemSolver (scico/optimize/_admm.py:334-378,
 // _admmaux.py:205-269, scico/solver.py:326-405), D = FiniteDifference over
-// both axes with append=0 (stacked (2, rows, cols)).  One g_i per non-zero
-// lambda, L2,1 first, each with its own z_i and u_i, all sharing D and rho.
+// all image axes with append=0 (stacked (ND, *shape), ND = 2 for a slice
+// with XRayTransform2D, 3 for a volume with XRayTransform3D).  One g_i per
+// non-zero lambda, L2,1 first, each with its own z_i and u_i, all sharing D
+// and rho.  The elementwise kernels are templated on ND; A is whichever
+// projector the descriptor names.
 //
 // Per outer iteration (each kernel below is one launch; the whole iteration
 // is captured once into a CUDA graph and replayed):
@@ -67,60 +70,102 @@ struct TermParams {
   float c;         // 2 * loss scale
 };
 
-__device__ __forceinline__ int pix_i(size_t e, int C) { return (int)(e / (size_t)C); }
+// Image shape (n[0..ND-1], C order) of the fused kernels: ND = 2 for 2D
+// slices, 3 for volumes.
+struct Shape3 {
+  int n[3];
+};
 
-// D^T applied at (i, j) to a stacked (2, R, C) field f = a - b (b may be null).
+template <int ND>
+__device__ __forceinline__ void coords(size_t e, const Shape3& sh, int (&c)[ND]) {
+  if (ND == 2) {
+    c[0] = (int)(e / (size_t)sh.n[1]);
+    c[ND - 1] = (int)(e % (size_t)sh.n[1]);
+  } else {
+    const size_t r = e / (size_t)sh.n[ND - 1];
+    c[ND - 1] = (int)(e - r * (size_t)sh.n[ND - 1]);
+    c[1] = (int)(r % (size_t)sh.n[1]);
+    c[0] = (int)(r / (size_t)sh.n[1]);
+  }
+}
+
+// C-order element stride of axis k.
+template <int ND>
+__device__ __forceinline__ size_t axis_stride(const Shape3& sh, int k) {
+  size_t st = 1;
+  for (int q = ND - 1; q > k; --q) st *= (size_t)sh.n[q];
+  return st;
+}
+
+// D^T applied at element e to a stacked (ND, *shape) field f = a - b (b may
+// be null): sum over axes of (f_k[e - st_k] - f_k[e]) with the append=0
+// boundaries, axes added in order (linop/_stack.py:71-72).
+template <int ND>
 __device__ __forceinline__ float dT_at(const float* __restrict__ a, const float* __restrict__ b,
-                                       int i, int j, int R, int C) {
-  const size_t N = (size_t)R * C;
-  const size_t e = (size_t)i * C + j;
+                                       const int (&c)[ND], size_t e, const Shape3& sh, size_t N) {
   auto f = [&](int comp, size_t idx) -> float {
     const float av = a[comp * N + idx];
     return b ? ct::fsub(av, b[comp * N + idx]) : av;
   };
-  const float lo0 = i >= 1 ? f(0, e - C) : 0.0f;
-  const float hi0 = i <= R - 2 ? f(0, e) : 0.0f;
-  const float lo1 = j >= 1 ? f(1, e - 1) : 0.0f;
-  const float hi1 = j <= C - 2 ? f(1, e) : 0.0f;
-  return ct::fadd(ct::fsub(lo0, hi0), ct::fsub(lo1, hi1));
+  float tot = 0.0f;
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    const size_t st = axis_stride<ND>(sh, k);
+    const float lo = c[k] >= 1 ? f(k, e - st) : 0.0f;
+    const float hi = c[k] <= sh.n[k] - 2 ? f(k, e) : 0.0f;
+    const float term = ct::fsub(lo, hi);
+    tot = k == 0 ? term : ct::fadd(tot, term);
+  }
+  return tot;
 }
 
-// (D^T D q) at (i, j), append=0 differences over both axes.
-__device__ __forceinline__ float dtd_at(const float* __restrict__ q, int i, int j, int R, int C) {
-  const size_t e = (size_t)i * C + j;
+// (D^T D q) at element e, append=0 differences over all axes.
+template <int ND>
+__device__ __forceinline__ float dtd_at(const float* __restrict__ q, const int (&c)[ND], size_t e,
+                                        const Shape3& sh) {
   const float qc = q[e];
-  const float lo0 = i >= 1 ? ct::fsub(qc, q[e - C]) : 0.0f;
-  const float hi0 = i <= R - 2 ? ct::fsub(q[e + C], qc) : 0.0f;
-  const float lo1 = j >= 1 ? ct::fsub(qc, q[e - 1]) : 0.0f;
-  const float hi1 = j <= C - 2 ? ct::fsub(q[e + 1], qc) : 0.0f;
-  return ct::fadd(ct::fsub(lo0, hi0), ct::fsub(lo1, hi1));
+  float tot = 0.0f;
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    const size_t st = axis_stride<ND>(sh, k);
+    const float lo = c[k] >= 1 ? ct::fsub(qc, q[e - st]) : 0.0f;
+    const float hi = c[k] <= sh.n[k] - 2 ? ct::fsub(q[e + st], qc) : 0.0f;
+    const float term = ct::fsub(lo, hi);
+    tot = k == 0 ? term : ct::fadd(tot, term);
+  }
+  return tot;
 }
 
-// D x at (i, j): (x[i+1,j]-x[i,j], x[i,j+1]-x[i,j]); the appended last
+// D x at element e: x[e + st_k] - x[e] per axis; the appended last
 // difference along an axis is x - x.
-__device__ __forceinline__ void d_at(const float* __restrict__ x, int i, int j, int R, int C,
-                                     float& d0, float& d1) {
-  const size_t e = (size_t)i * C + j;
+template <int ND>
+__device__ __forceinline__ void d_at(const float* __restrict__ x, const int (&c)[ND], size_t e,
+                                     const Shape3& sh, float (&d)[ND]) {
   const float xc = x[e];
-  d0 = ct::fsub(i <= R - 2 ? x[e + C] : xc, xc);
-  d1 = ct::fsub(j <= C - 2 ? x[e + 1] : xc, xc);
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    const size_t st = axis_stride<ND>(sh, k);
+    d[k] = ct::fsub(c[k] <= sh.n[k] - 2 ? x[e + st] : xc, xc);
+  }
 }
 
+template <int ND>
 __global__ void __launch_bounds__(NT) k_init_state(const float* __restrict__ x, float* __restrict__ z,
                                                    float* __restrict__ u, float* __restrict__ dz,
-                                                   int R, int C, int ng) {
-  const size_t N = (size_t)R * C;
+                                                   Shape3 sh, size_t N, int ng) {
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-    float d0, d1;
-    d_at(x, pix_i(e, C), (int)(e % C), R, C, d0, d1);
+    int c[ND];
+    coords<ND>(e, sh, c);
+    float d[ND];
+    d_at<ND>(x, c, e, sh, d);
     for (int t = 0; t < ng; ++t) {
-      float* zt = z + (size_t)t * 2 * N;
-      zt[e] = d0;
-      zt[N + e] = d1;
-      u[(size_t)t * 2 * N + e] = 0.0f;
-      u[(size_t)t * 2 * N + N + e] = 0.0f;
-      dz[(size_t)t * 2 * N + e] = 0.0f;
-      dz[(size_t)t * 2 * N + N + e] = 0.0f;
+      const size_t o = (size_t)t * ND * N;
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        z[o + k * N + e] = d[k];
+        u[o + k * N + e] = 0.0f;
+        dz[o + k * N + e] = 0.0f;
+      }
     }
   }
 }
@@ -135,20 +180,21 @@ __global__ void __launch_bounds__(NT) k_scale_splits(const float* __restrict__ s
   }
 }
 
+template <int ND>
 __global__ void __launch_bounds__(NT)
     k_rhs(const float* __restrict__ atyc, const float* __restrict__ z, const float* __restrict__ u,
-          const float* __restrict__ dz, float* __restrict__ rhs, int R, int C, TermParams tp,
+          const float* __restrict__ dz, float* __restrict__ rhs, Shape3 sh, size_t N, TermParams tp,
           double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
-  const size_t N = (size_t)R * C;
   double acc[1] = {0.0};
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-    const int i = pix_i(e, C), j = (int)(e % C);
+    int c[ND];
+    coords<ND>(e, sh, c);
     float val = atyc[e];
     float dv = 0.0f;
     for (int t = 0; t < tp.ng; ++t) {
-      const size_t o = (size_t)t * 2 * N;
-      val = ct::fadd(val, ct::fmul(tp.rho, dT_at(z + o, u + o, i, j, R, C)));
-      const float w = ct::fmul(tp.rho, dT_at(dz + o, nullptr, i, j, R, C));
+      const size_t o = (size_t)t * ND * N;
+      val = ct::fadd(val, ct::fmul(tp.rho, dT_at<ND>(z + o, u + o, c, e, sh, N)));
+      const float w = ct::fmul(tp.rho, dT_at<ND>(dz + o, nullptr, c, e, sh, N));
       dv = (t == 0) ? w : ct::fadd(dv, w);
     }
     rhs[e] = val;
@@ -199,17 +245,16 @@ __global__ void k_itstat(double* __restrict__ itstat, double* __restrict__ slots
 // scalars; lhs(x) is stored in lhsx, or read from it while x is unchanged
 // (slots[S_XCLEAN]).  PAP: Ap = lhs(q) and <q, Ap>.  In a graph with a
 // conditional CG loop, INIT sets the loop condition.
-template <bool INIT>
+template <int ND, bool INIT>
 __global__ void __launch_bounds__(NT)
-    k_lhs_finish(const float* __restrict__ adj, int nsplit, const float* __restrict__ q, int R, int C,
-                 TermParams tp, float* __restrict__ out, const float* __restrict__ rhs,
+    k_lhs_finish(const float* __restrict__ adj, int nsplit, const float* __restrict__ q, Shape3 sh,
+                 size_t N, TermParams tp, float* __restrict__ out, const float* __restrict__ rhs,
                  float* __restrict__ p, float* __restrict__ lhsx, double* __restrict__ slots,
                  double* __restrict__ cg, double tol, double atol, int maxiter,
                  double* __restrict__ partials, unsigned int* __restrict__ ticket,
                  cudaGraphConditionalHandle cond, int use_cond) {
   if (!INIT && cg[CT_CG_DONE] != 0.0) return;
   const bool cached = INIT && slots[S_XCLEAN] != 0.0;
-  const size_t N = (size_t)R * C;
   double acc[2] = {0.0, 0.0};
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     float v;
@@ -218,7 +263,9 @@ __global__ void __launch_bounds__(NT)
     } else {
       float a = adj[e];
       for (int k = 1; k < nsplit; ++k) a = ct::fadd(a, adj[(size_t)k * N + e]);
-      const float g = dtd_at(q, pix_i(e, C), (int)(e % C), R, C);
+      int c[ND];
+      coords<ND>(e, sh, c);
+      const float g = dtd_at<ND>(q, c, e, sh);
       v = ct::fmul(tp.rho, g);
       for (int t = 1; t < tp.ng; ++t) v = ct::fadd(v, ct::fmul(tp.rho, g));
       v = ct::fadd(v, ct::fmul(tp.c, a));
@@ -260,59 +307,77 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-__device__ __forceinline__ void prox_pair(int kind, float thr, float v0, float v1, float& z0, float& z1) {
-  if (kind == 0) {  // L2,1 over the two difference components
-    const float len = __fsqrt_rn(ct::fadd(ct::fmul(v0, v0), ct::fmul(v1, v1)));
+// prox of one g term over the ND difference components of one element
+// (L21Norm._prox / L1Norm.prox, scico/functional/_norm.py; threshold
+// lam/rho in float32, _functional.py:198).
+template <int ND>
+__device__ __forceinline__ void prox_nd(int kind, float thr, const float (&v)[ND], float (&z)[ND]) {
+  if (kind == 0) {  // L2,1 over the difference components
+    float s2 = ct::fmul(v[0], v[0]);
+#pragma unroll
+    for (int k = 1; k < ND; ++k) s2 = ct::fadd(s2, ct::fmul(v[k], v[k]));
+    const float len = __fsqrt_rn(s2);
     float nl = ct::fsub(len, thr);
     nl = ct::fmul(0.5f, ct::fadd(nl, fabsf(nl)));
-    z0 = ct::fmul(nl, len != 0.0f ? __fdiv_rn(v0, len) : 0.0f);
-    z1 = ct::fmul(nl, len != 0.0f ? __fdiv_rn(v1, len) : 0.0f);
+#pragma unroll
+    for (int k = 0; k < ND; ++k) z[k] = ct::fmul(nl, len != 0.0f ? __fdiv_rn(v[k], len) : 0.0f);
   } else {  // L1
-    auto soft = [&](float v) {
-      float t = ct::fsub(fabsf(v), thr);
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      float t = ct::fsub(fabsf(v[k]), thr);
       t = ct::fmul(0.5f, ct::fadd(t, fabsf(t)));
-      const float sg = v > 0.0f ? 1.0f : (v < 0.0f ? -1.0f : (v == 0.0f ? 0.0f : v));
-      return ct::fmul(sg, t);
-    };
-    z0 = soft(v0);
-    z1 = soft(v1);
+      const float sg = v[k] > 0.0f ? 1.0f : (v[k] < 0.0f ? -1.0f : (v[k] == 0.0f ? 0.0f : v[k]));
+      z[k] = ct::fmul(sg, t);
+    }
   }
 }
 
+template <int ND>
 __global__ void __launch_bounds__(NT)
     k_zu(const float* __restrict__ x, float* __restrict__ z, float* __restrict__ u, float* __restrict__ dz,
-         int R, int C, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
+         Shape3 sh, size_t N, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
          unsigned int* __restrict__ ticket) {
-  const size_t N = (size_t)R * C;
   double acc[3] = {0.0, 0.0, 0.0};  // primal, g21, g1
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-    float d0, d1;
-    d_at(x, pix_i(e, C), (int)(e % C), R, C, d0, d1);
+    int c[ND];
+    coords<ND>(e, sh, c);
+    float d[ND];
+    d_at<ND>(x, c, e, sh, d);
     for (int t = 0; t < tp.ng; ++t) {
-      const size_t o = (size_t)t * 2 * N;
-      const float zo0 = z[o + e], zo1 = z[o + N + e];
-      float c0 = d0, c1 = d1;
-      if (tp.alpha != 1.0f) {
-        const float om = ct::fsub(1.0f, tp.alpha);
-        c0 = ct::fadd(ct::fmul(tp.alpha, d0), ct::fmul(om, zo0));
-        c1 = ct::fadd(ct::fmul(tp.alpha, d1), ct::fmul(om, zo1));
+      const size_t o = (size_t)t * ND * N;
+      float zo[ND], v[ND], zn[ND];
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        zo[k] = z[o + k * N + e];
+        float ck = d[k];
+        if (tp.alpha != 1.0f) {
+          const float om = ct::fsub(1.0f, tp.alpha);
+          ck = ct::fadd(ct::fmul(tp.alpha, d[k]), ct::fmul(om, zo[k]));
+        }
+        v[k] = ct::fadd(ck, u[o + k * N + e]);
       }
-      const float v0 = ct::fadd(c0, u[o + e]);
-      const float v1 = ct::fadd(c1, u[o + N + e]);
-      float z0, z1;
-      prox_pair(tp.kind[t], tp.thr[t], v0, v1, z0, z1);
-      z[o + e] = z0;
-      z[o + N + e] = z1;
-      u[o + e] = ct::fsub(v0, z0);
-      u[o + N + e] = ct::fsub(v1, z1);
-      dz[o + e] = ct::fsub(z0, zo0);
-      dz[o + N + e] = ct::fsub(z1, zo1);
-      const double p0 = (double)d0 - (double)z0, p1 = (double)d1 - (double)z1;
-      acc[0] += (double)tp.rho * (p0 * p0 + p1 * p1);
-      if (tp.kind[t] == 0)
-        acc[1] += (double)__fsqrt_rn(ct::fadd(ct::fmul(z0, z0), ct::fmul(z1, z1)));
-      else
-        acc[2] += fabs((double)z0) + fabs((double)z1);
+      prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
+      double pr = 0.0;
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        z[o + k * N + e] = zn[k];
+        u[o + k * N + e] = ct::fsub(v[k], zn[k]);
+        dz[o + k * N + e] = ct::fsub(zn[k], zo[k]);
+        const double pk = (double)d[k] - (double)zn[k];
+        pr = k == 0 ? pk * pk : pr + pk * pk;
+      }
+      acc[0] += (double)tp.rho * pr;
+      if (tp.kind[t] == 0) {
+        float s2 = ct::fmul(zn[0], zn[0]);
+#pragma unroll
+        for (int k = 1; k < ND; ++k) s2 = ct::fadd(s2, ct::fmul(zn[k], zn[k]));
+        acc[1] += (double)__fsqrt_rn(s2);
+      } else {
+        double a1 = fabs((double)zn[0]);
+#pragma unroll
+        for (int k = 1; k < ND; ++k) a1 += fabs((double)zn[k]);
+        acc[2] += a1;
+      }
     }
   }
   double tot[3];
@@ -333,61 +398,146 @@ __global__ void k_reset_call(double* __restrict__ slots) {
 
 // ---------------------------------------------------------------------------
 
+// Solver parameters common to the 2D and 3D descriptors.
+struct Params {
+  int maxiter, cg_maxiter;
+  double cg_tol, cg_atol, lam_l21, lam_l1, rho, loss_scale, alpha;
+  int use_graph;
+};
+
+template <class D>
+Params params_of(const D* d) {
+  return Params{d->maxiter, d->cg_maxiter, d->cg_tol,     d->cg_atol,
+                d->lam_l21, d->lam_l1,     d->rho,        d->loss_scale,
+                d->alpha,   d->use_graph};
+}
+
+// The forward/adjoint pair behind A: the 2D or the 3D projector.
+struct Projector {
+  int nd = 2;
+  const ct_geom2d* g2 = nullptr;
+  const ct_geom3d* g3 = nullptr;
+  ct::Proj2dPlan p2{};
+  ct::Proj3dPlan p3{};
+  size_t fwd_bytes() const { return nd == 2 ? p2.fwd_bytes : p3.fwd_bytes; }
+  size_t adj_bytes() const { return nd == 2 ? p2.adj_bytes : p3.adj_bytes; }
+  int nsplit() const { return nd == 2 ? p2.nsplit : p3.nsplit; }
+  ct_status prepare() const { return nd == 2 ? ct::proj2d_prepare(p2) : ct::proj3d_prepare(g3, p3); }
+  ct_status fwd(const float* img, float* sino, void* ws, cudaStream_t s, const double* skip) const {
+    return nd == 2 ? ct::proj2d_fwd_launch(g2, p2, img, sino, 1, static_cast<float*>(ws), s, skip)
+                   : ct::proj3d_fwd_launch(g3, p3, img, sino, ws, s, skip);
+  }
+  ct_status adj(const float* sino, float* out, float* part, cudaStream_t s, const double* skip) const {
+    return nd == 2 ? ct::proj2d_adj_launch(g2, p2, sino, out, part, 1, s, skip)
+                   : ct::proj3d_adj_launch(g3, p3, sino, out, part, s, skip);
+  }
+};
+
+// One problem: descriptor bytes (for the graph cache key), parameters,
+// image shape and projector.
+struct Problem {
+  const void* desc = nullptr;
+  size_t desc_size = 0;
+  Params prm{};
+  Shape3 sh{};
+  int nd = 2;
+  size_t N = 0, S = 0;
+  Projector proj;
+};
+
+Problem problem_of(const ct_admm_tv_desc* d) {
+  Problem P;
+  P.desc = d;
+  P.desc_size = sizeof(*d);
+  P.prm = params_of(d);
+  P.nd = 2;
+  P.sh.n[0] = d->geom.rows;
+  P.sh.n[1] = d->geom.cols;
+  P.sh.n[2] = 1;
+  P.N = (size_t)d->geom.rows * d->geom.cols;
+  P.S = (size_t)d->geom.n_views * d->geom.det_count;
+  P.proj.nd = 2;
+  P.proj.g2 = &d->geom;
+  P.proj.p2 = ct::proj2d_plan(&d->geom, 1);
+  return P;
+}
+
+Problem problem_of(const ct_admm_tv3d_desc* d) {
+  Problem P;
+  P.desc = d;
+  P.desc_size = sizeof(*d);
+  P.prm = params_of(d);
+  P.nd = 3;
+  for (int k = 0; k < 3; ++k) P.sh.n[k] = d->geom.shape[k];
+  P.N = (size_t)d->geom.shape[0] * d->geom.shape[1] * d->geom.shape[2];
+  P.S = (size_t)d->geom.n_views * d->geom.det_shape[0] * d->geom.det_shape[1];
+  P.proj.nd = 3;
+  P.proj.g3 = &d->geom;
+  P.proj.p3 = ct::proj3d_plan(&d->geom, 1);
+  return P;
+}
+
 struct Layout {
-  size_t N, S;
   int ng;
-  ct::Proj2dPlan plan;
   size_t off_slots, off_red, off_atyc, off_rhs, off_r, off_p, off_ap, off_adj, off_sino, off_z, off_u,
       off_dz, off_fwd, off_adjpart, off_lhsx, off_sinox, total;
 };
 
-Layout layout(const ct_admm_tv_desc* d) {
+Layout layout(const Problem& P) {
   Layout L;
-  const ct_geom2d* g = &d->geom;
-  L.N = (size_t)g->rows * g->cols;
-  L.S = (size_t)g->n_views * g->det_count;
-  L.ng = (d->lam_l21 != 0.0) + (d->lam_l1 != 0.0);
-  L.plan = ct::proj2d_plan(g, 1);
+  L.ng = (P.prm.lam_l21 != 0.0) + (P.prm.lam_l1 != 0.0);
   size_t o = 0;
   auto take = [&](size_t bytes) {
     const size_t at = o;
     o += ct::round_up(bytes, 256);
     return at;
   };
+  const size_t zbytes = P.N * 4 * (size_t)P.nd * (size_t)(L.ng > 0 ? L.ng : 1);
   L.off_slots = take(S_COUNT * sizeof(double));
   L.off_red = take(ct::kReduceWorkspace);
-  L.off_atyc = take(L.N * 4);
-  L.off_rhs = take(L.N * 4);
-  L.off_r = take(L.N * 4);
-  L.off_p = take(L.N * 4);
-  L.off_ap = take(L.N * 4);
-  L.off_adj = take(L.N * 4);
-  L.off_sino = take(L.S * 4);
-  L.off_z = take(L.N * 8 * (size_t)(L.ng > 0 ? L.ng : 1));
-  L.off_u = take(L.N * 8 * (size_t)(L.ng > 0 ? L.ng : 1));
-  L.off_dz = take(L.N * 8 * (size_t)(L.ng > 0 ? L.ng : 1));
-  L.off_fwd = take(L.plan.fwd_bytes);
-  L.off_adjpart = take(L.plan.adj_bytes > 0 ? L.plan.adj_bytes : 256);
-  L.off_lhsx = take(L.N * 4);
-  L.off_sinox = take(L.S * 4);
+  L.off_atyc = take(P.N * 4);
+  L.off_rhs = take(P.N * 4);
+  L.off_r = take(P.N * 4);
+  L.off_p = take(P.N * 4);
+  L.off_ap = take(P.N * 4);
+  L.off_adj = take(P.N * 4);
+  L.off_sino = take(P.S * 4);
+  L.off_z = take(zbytes);
+  L.off_u = take(zbytes);
+  L.off_dz = take(zbytes);
+  L.off_fwd = take(P.proj.fwd_bytes() > 0 ? P.proj.fwd_bytes() : 256);
+  L.off_adjpart = take(P.proj.adj_bytes() > 0 ? P.proj.adj_bytes() : 256);
+  L.off_lhsx = take(P.N * 4);
+  L.off_sinox = take(P.S * 4);
   L.total = o;
   return L;
+}
+
+ct_status check_params(const Params& p, const char* who) {
+  if (p.maxiter < 0 || p.cg_maxiter < 0)
+    return ct::fail(CT_ERR_INVALID_ARG, "%s: maxiter=%d cg_maxiter=%d", who, p.maxiter, p.cg_maxiter);
+  if ((p.lam_l21 != 0.0) + (p.lam_l1 != 0.0) == 0)
+    return ct::fail(CT_ERR_INVALID_ARG, "%s: at least one of lam_l21, lam_l1 must be non-zero", who);
+  if (!(p.rho > 0.0)) return ct::fail(CT_ERR_INVALID_ARG, "%s: rho must be > 0", who);
+  return CT_OK;
 }
 
 ct_status check_desc(const ct_admm_tv_desc* d, const char* who) {
   if (!d) return ct::fail(CT_ERR_INVALID_ARG, "%s: null descriptor", who);
   ct_status st = ct::proj2d_check(&d->geom, who);
   if (st != CT_OK) return st;
-  if (d->maxiter < 0 || d->cg_maxiter < 0)
-    return ct::fail(CT_ERR_INVALID_ARG, "%s: maxiter=%d cg_maxiter=%d", who, d->maxiter, d->cg_maxiter);
-  if ((d->lam_l21 != 0.0) + (d->lam_l1 != 0.0) == 0)
-    return ct::fail(CT_ERR_INVALID_ARG, "%s: at least one of lam_l21, lam_l1 must be non-zero", who);
-  if (!(d->rho > 0.0)) return ct::fail(CT_ERR_INVALID_ARG, "%s: rho must be > 0", who);
-  return CT_OK;
+  return check_params(params_of(d), who);
+}
+
+ct_status check_desc(const ct_admm_tv3d_desc* d, const char* who) {
+  if (!d) return ct::fail(CT_ERR_INVALID_ARG, "%s: null descriptor", who);
+  ct_status st = ct::proj3d_check(&d->geom, who);
+  if (st != CT_OK) return st;
+  return check_params(params_of(d), who);
 }
 
 struct Ctx {
-  const ct_admm_tv_desc* d;
+  Problem P;
   Layout L;
   char* ws;
   const float* y;
@@ -408,8 +558,17 @@ struct Ctx {
     if (_st != CT_OK) return _st;    \
   } while (0)
 
+// Launch the ND instance of a templated kernel for the problem's dimension.
+#define CT_LAUNCH_ND(nd, kernel, grid, block, stream, ...)                 \
+  do {                                                                     \
+    if ((nd) == 2)                                                         \
+      kernel<2><<<(grid), (block), 0, (stream)>>>(__VA_ARGS__);            \
+    else                                                                   \
+      kernel<3><<<(grid), (block), 0, (stream)>>>(__VA_ARGS__);            \
+  } while (0)
+
 ct_status project(const Ctx& c, const float* img, float* sino, cudaStream_t s, const double* skip) {
-  return ct::proj2d_fwd_launch(&c.d->geom, c.L.plan, img, sino, 1, c.at<float>(c.L.off_fwd), s, skip);
+  return c.P.proj.fwd(img, sino, c.at<float>(c.L.off_fwd), s, skip);
 }
 
 // A^T of a sinogram into the adjoint buffer (or its view splits); returns
@@ -417,38 +576,48 @@ ct_status project(const Ctx& c, const float* img, float* sino, cudaStream_t s, c
 const float* backproject(const Ctx& c, const float* sino, cudaStream_t s, const double* skip, ct_status& st) {
   float* adj = c.at<float>(c.L.off_adj);
   float* part = c.at<float>(c.L.off_adjpart);
-  st = ct::proj2d_adj_launch(&c.d->geom, c.L.plan, sino, adj, part, 1, s, skip);
-  return c.L.plan.nsplit > 1 ? part : adj;
+  st = c.P.proj.adj(sino, adj, part, s, skip);
+  return c.P.proj.nsplit() > 1 ? part : adj;
 }
 
 // The three phases of one ADMM iteration.  cond/use_cond: the conditional
 // handle of the graph's CG loop (use_cond = 0 outside such a graph).
 ct_status enqueue_pre(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
-  const int R = c.d->geom.rows, C = c.d->geom.cols;
+  const int nd = c.P.nd;
+  const size_t N = c.P.N;
   float* r = c.at<float>(c.L.off_r);
   float* p = c.at<float>(c.L.off_p);
   float* rhs = c.at<float>(c.L.off_rhs);
   float* sinox = c.at<float>(c.L.off_sinox);
   const double* clean = c.slots() + S_XCLEAN;
-  k_rhs<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-                          c.at<float>(c.L.off_dz), rhs, R, C, c.tp, c.slots(), c.partials(), c.ticket());
+  CT_LAUNCH_ND(nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
+               c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), rhs, c.P.sh, N, c.tp, c.slots(),
+               c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_rhs"));
   CT_TRY(project(c, c.x, sinox, s, clean));
-  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.L.S, c.slots(), c.partials(), c.ticket());
+  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_resid2"));
-  k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.d->maxiter, c.d->loss_scale, c.d->lam_l21, c.d->lam_l1, 0);
+  k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21,
+                            c.P.prm.lam_l1, 0);
   CT_TRY(ct::launch_check("k_itstat"));
   ct_status st;
   const float* adj = backproject(c, sinox, s, clean, st);
   CT_TRY(st);
-  k_lhs_finish<true><<<NB, NT, 0, s>>>(adj, c.L.plan.nsplit, c.x, R, C, c.tp, r, rhs, p,
-                                       c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.d->cg_tol,
-                                       c.d->cg_atol, c.d->cg_maxiter, c.partials(), c.ticket(), cond, use_cond);
+  if (nd == 2)
+    k_lhs_finish<2, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
+                                            c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
+                                            c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
+                                            cond, use_cond);
+  else
+    k_lhs_finish<3, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
+                                            c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
+                                            c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
+                                            cond, use_cond);
   return ct::launch_check("k_lhs_finish<init>");
 }
 
 ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
-  const int R = c.d->geom.rows, C = c.d->geom.cols;
+  const size_t N = c.P.N;
   float* r = c.at<float>(c.L.off_r);
   float* p = c.at<float>(c.L.off_p);
   float* ap = c.at<float>(c.L.off_ap);
@@ -458,18 +627,22 @@ ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHand
   ct_status st;
   const float* adj = backproject(c, sino, s, done, st);
   CT_TRY(st);
-  k_lhs_finish<false><<<NB, NT, 0, s>>>(adj, c.L.plan.nsplit, p, R, C, c.tp, ap, nullptr, nullptr, nullptr,
-                                        c.slots(), c.cg(), 0.0, 0.0, c.d->cg_maxiter, c.partials(), c.ticket(),
-                                        0, 0);
+  if (c.P.nd == 2)
+    k_lhs_finish<2, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
+                                             nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
+                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0);
+  else
+    k_lhs_finish<3, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
+                                             nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
+                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0);
   CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
-  CT_TRY(ct::cg_update_launch(c.x, r, p, ap, c.L.N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond));
-  return ct::cg_direction_launch(p, r, c.L.N, c.cg(), c.ws + c.L.off_red, s);
+  CT_TRY(ct::cg_update_launch(c.x, r, p, ap, N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond));
+  return ct::cg_direction_launch(p, r, N, c.cg(), c.ws + c.L.off_red, s);
 }
 
 ct_status enqueue_post(const Ctx& c, cudaStream_t s) {
-  const int R = c.d->geom.rows, C = c.d->geom.cols;
-  k_zu<<<NB, NT, 0, s>>>(c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), R, C,
-                         c.tp, c.slots(), c.partials(), c.ticket());
+  CT_LAUNCH_ND(c.P.nd, k_zu, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
+               c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp, c.slots(), c.partials(), c.ticket());
   return ct::launch_check("k_zu");
 }
 
@@ -477,22 +650,22 @@ ct_status enqueue_post(const Ctx& c, cudaStream_t s) {
 // into no-ops once CG has converged.
 ct_status enqueue_iteration(const Ctx& c, cudaStream_t s) {
   CT_TRY(enqueue_pre(c, s, 0, 0));
-  for (int it = 0; it < c.d->cg_maxiter; ++it) CT_TRY(enqueue_cg_step(c, s, 0, 0));
+  for (int it = 0; it < c.P.prm.cg_maxiter; ++it) CT_TRY(enqueue_cg_step(c, s, 0, 0));
   return enqueue_post(c, s);
 }
 
 // Statistics of the last iteration: dual residual (k_rhs), objective.
 ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
-  const int R = c.d->geom.rows, C = c.d->geom.cols;
   float* sinox = c.at<float>(c.L.off_sinox);
-  k_rhs<<<NB, NT, 0, s>>>(c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-                          c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), R, C, c.tp, c.slots(),
-                          c.partials(), c.ticket());
+  CT_LAUNCH_ND(c.P.nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
+               c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N,
+               c.tp, c.slots(), c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_rhs"));
   CT_TRY(project(c, c.x, sinox, s, c.slots() + S_XCLEAN));
-  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.L.S, c.slots(), c.partials(), c.ticket());
+  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket());
   CT_TRY(ct::launch_check("k_resid2"));
-  k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.d->maxiter, c.d->loss_scale, c.d->lam_l21, c.d->lam_l1, 1);
+  k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21,
+                            c.P.prm.lam_l1, 1);
   return ct::launch_check("k_itstat");
 }
 
@@ -514,7 +687,8 @@ size_t make_key(const Ctx& c, unsigned char* key) {
     memcpy(key + n, p, b);
     n += b;
   };
-  put(c.d, sizeof(ct_admm_tv_desc));
+  put(&c.P.nd, sizeof(c.P.nd));
+  put(c.P.desc, c.P.desc_size);
   put(&c.ws, sizeof(c.ws));
   put(&c.y, sizeof(c.y));
   put(&c.x, sizeof(c.x));
@@ -609,10 +783,87 @@ ct_status run_graph(const Ctx& c, cudaStream_t caller) {
   }
   CT_TRY(ct::cuda_check(cudaEventRecord(g_cache.ev_in, caller), "event record"));
   CT_TRY(ct::cuda_check(cudaStreamWaitEvent(g_cache.cs, g_cache.ev_in, 0), "stream wait"));
-  for (int k = 0; k < c.d->maxiter; ++k)
+  for (int k = 0; k < c.P.prm.maxiter; ++k)
     CT_TRY(ct::cuda_check(cudaGraphLaunch(g_cache.exec, g_cache.cs), "graph launch"));
   CT_TRY(ct::cuda_check(cudaEventRecord(g_cache.ev_out, g_cache.cs), "event record"));
   return ct::cuda_check(cudaStreamWaitEvent(caller, g_cache.ev_out, 0), "stream wait");
+}
+
+// Solve for either descriptor kind.
+template <class D>
+ct_status solve(const D* d, const char* who, const float* y, float* x, double* itstat_dev, int32_t iter0,
+                void* workspace, size_t workspace_bytes, ct_stream_t stream) {
+  CT_TRY(check_desc(d, who));
+  if (!y || !x) return ct::fail(CT_ERR_INVALID_ARG, "%s: null array", who);
+  Ctx c;
+  c.P = problem_of(d);
+  c.L = layout(c.P);
+  if (!workspace || workspace_bytes < c.L.total || !ct::aligned(workspace, 256))
+    return ct::fail(CT_ERR_WORKSPACE, "%s: need %zu bytes (256-B aligned), got %zu", who, c.L.total,
+                    workspace_bytes);
+  c.ws = static_cast<char*>(workspace);
+  c.y = y;
+  c.x = x;
+  c.itstat = itstat_dev;
+  const Params& prm = c.P.prm;
+  TermParams& tp = c.tp;
+  tp.ng = 0;
+  // The reference's prox parameter is (1/rho) * lam in float64, then float32.
+  if (prm.lam_l21 != 0.0) {
+    tp.kind[tp.ng] = 0;
+    tp.thr[tp.ng] = (float)((1.0 / prm.rho) * prm.lam_l21);
+    ++tp.ng;
+  }
+  if (prm.lam_l1 != 0.0) {
+    tp.kind[tp.ng] = 1;
+    tp.thr[tp.ng] = (float)((1.0 / prm.rho) * prm.lam_l1);
+    ++tp.ng;
+  }
+  tp.rho = (float)prm.rho;
+  tp.alpha = (float)prm.alpha;
+  tp.c = (float)(2.0 * prm.loss_scale);
+  cudaStream_t s = ct::as_stream(stream);
+  CT_TRY(c.P.proj.prepare());
+
+  if (iter0 == 0) {
+    CT_TRY(ct::cuda_check(cudaMemsetAsync(c.ws, 0, c.L.off_atyc, s), "memset state"));
+    // A^T y, scaled by 2*scale (hoisted out of the loop: y is constant).
+    CT_TRY(c.P.proj.adj(y, c.at<float>(c.L.off_adj), c.at<float>(c.L.off_adjpart), s, nullptr));
+    const int ns = c.P.proj.nsplit();
+    const float* src = ns > 1 ? c.at<float>(c.L.off_adjpart) : c.at<float>(c.L.off_adj);
+    k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.P.N, ns, tp.c);
+    CT_TRY(ct::launch_check("k_scale_splits"));
+    CT_LAUNCH_ND(c.P.nd, k_init_state, NB, NT, s, x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
+                 c.at<float>(c.L.off_dz), c.P.sh, c.P.N, tp.ng);
+    CT_TRY(ct::launch_check("k_init_state"));
+  }
+  k_reset_call<<<1, 1, 0, s>>>(c.slots());
+  CT_TRY(ct::launch_check("k_reset_call"));
+  if (prm.maxiter == 0) return CT_OK;
+  if (prm.use_graph) {
+    CT_TRY(run_graph(c, s));
+  } else {
+    for (int k = 0; k < prm.maxiter; ++k) CT_TRY(enqueue_iteration(c, s));
+  }
+  return enqueue_epilogue(c, s);
+}
+
+template <class D>
+ct_status workspace_of(const D* d, const char* who, size_t* bytes) {
+  CT_TRY(check_desc(d, who));
+  if (!bytes) return ct::fail(CT_ERR_INVALID_ARG, "%s: null bytes", who);
+  *bytes = layout(problem_of(d)).total;
+  return CT_OK;
+}
+
+template <class D>
+ct_status state_of(const D* d, const char* who, size_t* z_offset, size_t* u_offset, int32_t* n_terms) {
+  CT_TRY(check_desc(d, who));
+  const Layout L = layout(problem_of(d));
+  if (z_offset) *z_offset = L.off_z;
+  if (u_offset) *u_offset = L.off_u;
+  if (n_terms) *n_terms = L.ng;
+  return CT_OK;
 }
 
 }  // namespace
@@ -620,77 +871,31 @@ ct_status run_graph(const Ctx& c, cudaStream_t caller) {
 extern "C" {
 
 ct_status ct_admm_tv_workspace(const ct_admm_tv_desc* d, size_t* bytes) {
-  CT_TRY(check_desc(d, "ct_admm_tv_workspace"));
-  if (!bytes) return ct::fail(CT_ERR_INVALID_ARG, "ct_admm_tv_workspace: null bytes");
-  *bytes = layout(d).total;
-  return CT_OK;
+  return workspace_of(d, "ct_admm_tv_workspace", bytes);
 }
 
 ct_status ct_admm_tv_state(const ct_admm_tv_desc* d, size_t* z_offset, size_t* u_offset,
                            int32_t* n_terms) {
-  CT_TRY(check_desc(d, "ct_admm_tv_state"));
-  const Layout L = layout(d);
-  if (z_offset) *z_offset = L.off_z;
-  if (u_offset) *u_offset = L.off_u;
-  if (n_terms) *n_terms = L.ng;
-  return CT_OK;
+  return state_of(d, "ct_admm_tv_state", z_offset, u_offset, n_terms);
 }
 
 ct_status ct_admm_tv_solve(const ct_admm_tv_desc* d, const float* y, float* x, double* itstat_dev,
                            int32_t iter0, void* workspace, size_t workspace_bytes, ct_stream_t stream) {
-  CT_TRY(check_desc(d, "ct_admm_tv_solve"));
-  if (!y || !x) return ct::fail(CT_ERR_INVALID_ARG, "ct_admm_tv_solve: null array");
-  Ctx c;
-  c.d = d;
-  c.L = layout(d);
-  if (!workspace || workspace_bytes < c.L.total || !ct::aligned(workspace, 256))
-    return ct::fail(CT_ERR_WORKSPACE, "ct_admm_tv_solve: need %zu bytes (256-B aligned), got %zu",
-                    c.L.total, workspace_bytes);
-  c.ws = static_cast<char*>(workspace);
-  c.y = y;
-  c.x = x;
-  c.itstat = itstat_dev;
-  TermParams& tp = c.tp;
-  tp.ng = 0;
-  // The reference's prox parameter is (1/rho) * lam in float64, then float32.
-  if (d->lam_l21 != 0.0) {
-    tp.kind[tp.ng] = 0;
-    tp.thr[tp.ng] = (float)((1.0 / d->rho) * d->lam_l21);
-    ++tp.ng;
-  }
-  if (d->lam_l1 != 0.0) {
-    tp.kind[tp.ng] = 1;
-    tp.thr[tp.ng] = (float)((1.0 / d->rho) * d->lam_l1);
-    ++tp.ng;
-  }
-  tp.rho = (float)d->rho;
-  tp.alpha = (float)d->alpha;
-  tp.c = (float)(2.0 * d->loss_scale);
-  cudaStream_t s = ct::as_stream(stream);
-  CT_TRY(ct::proj2d_prepare(c.L.plan));
-  const int R = d->geom.rows, C = d->geom.cols;
+  return solve(d, "ct_admm_tv_solve", y, x, itstat_dev, iter0, workspace, workspace_bytes, stream);
+}
 
-  if (iter0 == 0) {
-    CT_TRY(ct::cuda_check(cudaMemsetAsync(c.ws, 0, c.L.off_atyc, s), "memset state"));
-    // A^T y, scaled by 2*scale (hoisted out of the loop: y is constant).
-    CT_TRY(ct::proj2d_adj_launch(&d->geom, c.L.plan, y, c.at<float>(c.L.off_adj),
-                                 c.at<float>(c.L.off_adjpart), 1, s, nullptr));
-    const float* src = c.L.plan.nsplit > 1 ? c.at<float>(c.L.off_adjpart) : c.at<float>(c.L.off_adj);
-    k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.L.N, c.L.plan.nsplit, tp.c);
-    CT_TRY(ct::launch_check("k_scale_splits"));
-    k_init_state<<<NB, NT, 0, s>>>(x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-                                   c.at<float>(c.L.off_dz), R, C, tp.ng);
-    CT_TRY(ct::launch_check("k_init_state"));
-  }
-  k_reset_call<<<1, 1, 0, s>>>(c.slots());
-  CT_TRY(ct::launch_check("k_reset_call"));
-  if (d->maxiter == 0) return CT_OK;
-  if (d->use_graph) {
-    CT_TRY(run_graph(c, s));
-  } else {
-    for (int k = 0; k < d->maxiter; ++k) CT_TRY(enqueue_iteration(c, s));
-  }
-  return enqueue_epilogue(c, s);
+ct_status ct_admm_tv3d_workspace(const ct_admm_tv3d_desc* d, size_t* bytes) {
+  return workspace_of(d, "ct_admm_tv3d_workspace", bytes);
+}
+
+ct_status ct_admm_tv3d_state(const ct_admm_tv3d_desc* d, size_t* z_offset, size_t* u_offset,
+                             int32_t* n_terms) {
+  return state_of(d, "ct_admm_tv3d_state", z_offset, u_offset, n_terms);
+}
+
+ct_status ct_admm_tv3d_solve(const ct_admm_tv3d_desc* d, const float* y, float* x, double* itstat_dev,
+                             int32_t iter0, void* workspace, size_t workspace_bytes, ct_stream_t stream) {
+  return solve(d, "ct_admm_tv3d_solve", y, x, itstat_dev, iter0, workspace, workspace_bytes, stream);
 }
 
 }  // extern "C"

@@ -32,6 +32,29 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
 ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* sino, float* out,
                             float* part, int batch, cudaStream_t s, const double* skip);
 
+// ---- 3D projector (proj3d.cu) ---------------------------------------------
+struct Proj3dPlan {
+  // AXIS0 forward: slices padded to the CTA's 64, tiles, tile groups, views per CTA
+  int Spad = 0, tiles_k = 0, n_tiles = 0, G = 1, vpc = 16;
+  size_t fwd_smem = 0;
+  // adjoint view splits (both kinds)
+  int nsplit = 1, per_split = 0;
+  size_t fwd_bytes = 0, adj_bytes = 0;
+};
+
+ct_status proj3d_check(const ct_geom3d* g, const char* who);
+Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch);
+// One-time per-process function attributes; must run before any stream capture.
+ct_status proj3d_prepare(const ct_geom3d* g, const Proj3dPlan& p);
+// proj = A vol for one volume; `ws` holds p.fwd_bytes.  `skip` as for 2D.
+ct_status proj3d_fwd_launch(const ct_geom3d* g, const Proj3dPlan& p, const float* vol, float* proj,
+                            void* ws, cudaStream_t s, const double* skip);
+// A^T proj for one projection set.  With p.nsplit == 1 the result goes to
+// `out`; otherwise view split k goes to part + k * (volume size) and the
+// caller sums the splits in order.
+ct_status proj3d_adj_launch(const ct_geom3d* g, const Proj3dPlan& p, const float* proj, float* out,
+                            float* part, cudaStream_t s, const double* skip);
+
 // ---- CG vector steps (vec.cu) ----------------------------------------------
 // cond/use_cond: in a graph with a conditional WHILE CG loop, the update sets
 // the loop condition to "not converged".

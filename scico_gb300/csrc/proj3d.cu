@@ -39,7 +39,7 @@
 #include <cmath>
 #include <vector>
 
-#include "common.cuh"
+#include "kernels.cuh"
 
 namespace ct {
 namespace {
@@ -113,6 +113,7 @@ struct Ax0FwdArgs {
   int tiles_k, n_tiles, G;
   int vpc;   // views per CTA
   int* errflag;
+  const double* skip;  // device flag: return at once when non-zero (may be null)
 };
 
 // Bin range of one 16x32 tile for one view.  Every operation of the rounded
@@ -132,6 +133,7 @@ __device__ __forceinline__ void tile_bins(float m11, float m12, float m13, int j
 }
 
 __global__ void __launch_bounds__(256, 2) k_p3_ax0_fwd(const Ax0FwdArgs a) {
+  if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) float smem[];
   float* sv = smem;                                           // [kOrd][kSvStride]
   float2* tab = reinterpret_cast<float2*>(sv + kOrd * kSvStride);  // [8][kOrd]
@@ -272,7 +274,9 @@ __global__ void __launch_bounds__(256, 2) k_p3_ax0_fwd(const Ax0FwdArgs a) {
 // proj[v][r][c] = sum_g acc_out[g][v][c][r - row_offset] (0 where no slice
 // lands on row r).  32x32 (col, row) tiles through shared memory.
 __global__ void k_p3_ax0_rows(const float* __restrict__ acc, float* __restrict__ proj, int V,
-                              int R, int C, int S, int Spad, int G, int row_offset) {
+                              int R, int C, int S, int Spad, int G, int row_offset,
+                              const double* skip) {
+  if (skip && *skip != 0.0) return;
   __shared__ float t[32][33];
   const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32, v = blockIdx.z;
   const int lx = threadIdx.x, ly = threadIdx.y;  // 32 x 8
@@ -303,6 +307,7 @@ struct Ax0AdjArgs {
   int per_split;
   size_t split_stride;
   int* errflag;
+  const double* skip;
 };
 
 // staged detector columns per slice row of the 16 x 32 adjoint tile:
@@ -328,6 +333,7 @@ __device__ __forceinline__ void adj_window(float m11, float m12, float m13, int 
 }
 
 __global__ void __launch_bounds__(256, 2) k_p3_ax0_adj(const Ax0AdjArgs a) {
+  if (a.skip && *a.skip != 0.0) return;
   // [2][32][kAW] pairs (y[c], y[c+1]) of the slice rows, double-buffered
   __shared__ __align__(16) float2 sy[2 * 32 * kAW];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -435,7 +441,9 @@ __global__ void __launch_bounds__(256) k_p3_gen_adj(const float* __restrict__ pr
                                                     float* __restrict__ out,
                                                     const float* __restrict__ views, int n0,
                                                     int n1, int n2, int V, int R, int C,
-                                                    int per_split, size_t split_stride) {
+                                                    int per_split, size_t split_stride,
+                                                    const double* skip) {
+  if (skip && *skip != 0.0) return;
   __shared__ float sm[kGenViewChunk * 8];
   const size_t n = (size_t)n0 * n1 * n2;
   const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -497,7 +505,9 @@ __device__ __forceinline__ void narrow(float beta, float mq, float wlo, float wh
 __global__ void __launch_bounds__(256) k_p3_gen_fwd(const float* __restrict__ vol,
                                                     float* __restrict__ proj,
                                                     const float* __restrict__ views, int n0,
-                                                    int n1, int n2, int V, int R, int C) {
+                                                    int n1, int n2, int V, int R, int C,
+                                                    const double* skip) {
+  if (skip && *skip != 0.0) return;
   const int v = blockIdx.y;
   const int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= R * C) return;
@@ -581,17 +591,11 @@ __global__ void k_p3_sum_splits(const float* __restrict__ part, float* __restric
   }
 }
 
+}  // namespace
+
 // ---------------------------------------------------------------------------
-// Host planning
+// Host planning and launchers
 // ---------------------------------------------------------------------------
-struct Proj3dPlan {
-  // AXIS0 forward
-  int Spad = 0, tiles_k = 0, n_tiles = 0, G = 1, vpc = kFwdViewsPerCta;
-  size_t fwd_smem = 0;
-  // adjoint view splits (both kinds)
-  int nsplit = 1, per_split = 0;
-  size_t fwd_bytes = 0, adj_bytes = 0;
-};
 
 ct_status proj3d_check(const ct_geom3d* g, const char* who) {
   if (!g) return fail(CT_ERR_INVALID_ARG, "%s: null geometry", who);
@@ -663,7 +667,82 @@ ct_status need_ws(const char* who, size_t need, void* ws, size_t bytes) {
   return CT_OK;
 }
 
-}  // namespace
+ct_status proj3d_prepare(const ct_geom3d* g, const Proj3dPlan& p) {
+  if (!errflag3_ptr()) return fail(CT_ERR_CUDA, "proj3d: error-word address unavailable");
+  if (g->kind != CT_PROJ3D_AXIS0) return CT_OK;
+  return cuda_check(cudaFuncSetAttribute(k_p3_ax0_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p.fwd_smem),
+                    "k_p3_ax0_fwd smem attribute");
+}
+
+ct_status proj3d_fwd_launch(const ct_geom3d* g, const Proj3dPlan& p, const float* vol, float* proj,
+                            void* ws, cudaStream_t s, const double* skip) {
+  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
+  const int R = g->det_shape[0], C = g->det_shape[1];
+  if (g->kind == CT_PROJ3D_AXIS0) {
+    Ax0FwdArgs a;
+    a.vol = vol;
+    a.acc_out = static_cast<float*>(ws);
+    a.views = g->views;
+    a.order = g->order;
+    a.S = S;
+    a.NJ = NJ;
+    a.NK = NK;
+    a.V = V;
+    a.C = C;
+    a.Spad = p.Spad;
+    a.tiles_k = p.tiles_k;
+    a.n_tiles = p.n_tiles;
+    a.G = p.G;
+    a.vpc = p.vpc;
+    a.errflag = errflag3_ptr();
+    a.skip = skip;
+    dim3 grid(p.G, p.Spad / kFwdSlices, (V + p.vpc - 1) / p.vpc);
+    k_p3_ax0_fwd<<<grid, 256, p.fwd_smem, s>>>(a);
+    ct_status st = launch_check("k_p3_ax0_fwd");
+    if (st != CT_OK) return st;
+    dim3 g2((C + 31) / 32, (R + 31) / 32, V);
+    k_p3_ax0_rows<<<g2, dim3(32, 8), 0, s>>>(a.acc_out, proj, V, R, C, S, p.Spad, p.G,
+                                             g->row_offset, skip);
+    return launch_check("k_p3_ax0_rows");
+  }
+  dim3 grid((R * C + 255) / 256, V);
+  k_p3_gen_fwd<<<grid, 256, 0, s>>>(vol, proj, g->views, S, NJ, NK, V, R, C, skip);
+  return launch_check("k_p3_gen_fwd");
+}
+
+ct_status proj3d_adj_launch(const ct_geom3d* g, const Proj3dPlan& p, const float* proj, float* out,
+                            float* part, cudaStream_t s, const double* skip) {
+  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
+  const int R = g->det_shape[0], C = g->det_shape[1];
+  const size_t vol_n = (size_t)S * NJ * NK;
+  float* dst = p.nsplit > 1 ? part : out;
+  if (g->kind == CT_PROJ3D_AXIS0) {
+    Ax0AdjArgs a;
+    a.proj = proj;
+    a.out = dst;
+    a.views = g->views;
+    a.S = S;
+    a.NJ = NJ;
+    a.NK = NK;
+    a.V = V;
+    a.R = R;
+    a.C = C;
+    a.row_offset = g->row_offset;
+    a.per_split = p.per_split;
+    a.split_stride = vol_n;
+    a.errflag = errflag3_ptr();
+    a.skip = skip;
+    dim3 grid((NK + 31) / 32, (NJ + kAdjRows - 1) / kAdjRows, ((S + 31) / 32) * p.nsplit);
+    k_p3_ax0_adj<<<grid, 256, 0, s>>>(a);
+    return launch_check("k_p3_ax0_adj");
+  }
+  dim3 grid((unsigned)((vol_n + 255) / 256), p.nsplit);
+  k_p3_gen_adj<<<grid, 256, 0, s>>>(proj, dst, g->views, S, NJ, NK, V, R, C, p.per_split, vol_n,
+                                    skip);
+  return launch_check("k_p3_gen_adj");
+}
+
 }  // namespace ct
 
 extern "C" {
@@ -762,51 +841,13 @@ ct_status ct_proj3d_fwd(const ct_geom3d* g, const float* vol, float* proj, int32
   const Proj3dPlan p = proj3d_plan(g, batch);
   st = need_ws("ct_proj3d_fwd", p.fwd_bytes, workspace, workspace_bytes);
   if (st != CT_OK) return st;
-  cudaStream_t s = as_stream(stream);
-  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
-  const int R = g->det_shape[0], C = g->det_shape[1];
-  const size_t vol_n = (size_t)S * NJ * NK, proj_n = (size_t)V * R * C;
-  if (g->kind == CT_PROJ3D_AXIS0) {
-    int* ef = errflag3_ptr();
-    if (!ef) return fail(CT_ERR_CUDA, "proj3d: error-word address unavailable");
-    st = cuda_check(cudaFuncSetAttribute(k_p3_ax0_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)p.fwd_smem),
-                    "k_p3_ax0_fwd smem attribute");
-    if (st != CT_OK) return st;
-    for (int b = 0; b < batch; ++b) {
-      Ax0FwdArgs a;
-      a.vol = vol + b * vol_n;
-      a.acc_out = static_cast<float*>(workspace);
-      a.views = g->views;
-      a.order = g->order;
-      a.S = S;
-      a.NJ = NJ;
-      a.NK = NK;
-      a.V = V;
-      a.C = C;
-      a.Spad = p.Spad;
-      a.tiles_k = p.tiles_k;
-      a.n_tiles = p.n_tiles;
-      a.G = p.G;
-      a.vpc = p.vpc;
-      a.errflag = ef;
-      dim3 grid(p.G, p.Spad / kFwdSlices, (V + p.vpc - 1) / p.vpc);
-      k_p3_ax0_fwd<<<grid, 256, p.fwd_smem, s>>>(a);
-      st = launch_check("k_p3_ax0_fwd");
-      if (st != CT_OK) return st;
-      dim3 g2((C + 31) / 32, (R + 31) / 32, V);
-      k_p3_ax0_rows<<<g2, dim3(32, 8), 0, s>>>(a.acc_out, proj + b * proj_n, V, R, C, S, p.Spad,
-                                               p.G, g->row_offset);
-      st = launch_check("k_p3_ax0_rows");
-      if (st != CT_OK) return st;
-    }
-    return CT_OK;
-  }
+  st = proj3d_prepare(g, p);
+  if (st != CT_OK) return st;
+  const size_t vol_n = (size_t)g->shape[0] * g->shape[1] * g->shape[2];
+  const size_t proj_n = (size_t)g->n_views * g->det_shape[0] * g->det_shape[1];
   for (int b = 0; b < batch; ++b) {
-    dim3 grid((R * C + 255) / 256, V);
-    k_p3_gen_fwd<<<grid, 256, 0, s>>>(vol + b * vol_n, proj + b * proj_n, g->views, S, NJ, NK, V,
-                                      R, C);
-    st = launch_check("k_p3_gen_fwd");
+    st = proj3d_fwd_launch(g, p, vol + b * vol_n, proj + b * proj_n, workspace, as_stream(stream),
+                           nullptr);
     if (st != CT_OK) return st;
   }
   return CT_OK;
@@ -822,39 +863,14 @@ ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol, int32
   const Proj3dPlan p = proj3d_plan(g, batch);
   st = need_ws("ct_proj3d_adj", p.adj_bytes, workspace, workspace_bytes);
   if (st != CT_OK) return st;
+  st = proj3d_prepare(g, p);
+  if (st != CT_OK) return st;
   cudaStream_t s = as_stream(stream);
-  const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
-  const int R = g->det_shape[0], C = g->det_shape[1];
-  const size_t vol_n = (size_t)S * NJ * NK, proj_n = (size_t)V * R * C;
+  const size_t vol_n = (size_t)g->shape[0] * g->shape[1] * g->shape[2];
+  const size_t proj_n = (size_t)g->n_views * g->det_shape[0] * g->det_shape[1];
   float* part = static_cast<float*>(workspace);
-  int* ef = errflag3_ptr();
-  if (!ef) return fail(CT_ERR_CUDA, "proj3d: error-word address unavailable");
   for (int b = 0; b < batch; ++b) {
-    float* dst = p.nsplit > 1 ? part : vol + b * vol_n;
-    if (g->kind == CT_PROJ3D_AXIS0) {
-      Ax0AdjArgs a;
-      a.proj = proj + b * proj_n;
-      a.out = dst;
-      a.views = g->views;
-      a.S = S;
-      a.NJ = NJ;
-      a.NK = NK;
-      a.V = V;
-      a.R = R;
-      a.C = C;
-      a.row_offset = g->row_offset;
-      a.per_split = p.per_split;
-      a.split_stride = vol_n;
-      a.errflag = ef;
-      dim3 grid((NK + 31) / 32, (NJ + kAdjRows - 1) / kAdjRows, (p.Spad / 32) * p.nsplit);
-      k_p3_ax0_adj<<<grid, 256, 0, s>>>(a);
-      st = launch_check("k_p3_ax0_adj");
-    } else {
-      dim3 grid((unsigned)((vol_n + 255) / 256), p.nsplit);
-      k_p3_gen_adj<<<grid, 256, 0, s>>>(proj + b * proj_n, dst, g->views, S, NJ, NK, V, R, C,
-                                        p.per_split, vol_n);
-      st = launch_check("k_p3_gen_adj");
-    }
+    st = proj3d_adj_launch(g, p, proj + b * proj_n, vol + b * vol_n, part, s, nullptr);
     if (st != CT_OK) return st;
     if (p.nsplit > 1) {
       const int blocks = (int)std::min<size_t>((vol_n + 255) / 256, 4096);

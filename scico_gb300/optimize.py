@@ -10,11 +10,13 @@ Two execution paths, same results (within float32 rounding):
 * generic: ``ADMM.step`` composes the operators exactly as the reference
   does (every operator application is a ctgpu kernel launch);
 * fused: when the problem is the CT TV pattern -- ``f = SquaredL2Loss(y,
-  A=XRayTransform2D)``, every ``C_i`` a 2D ``FiniteDifference(append=0)``,
-  ``g_i`` a scaled ``L21Norm()`` and/or ``L1Norm()``, equal ``rho_i``,
-  ``LinearSubproblemSolver`` -- ``solve()`` runs ``ct_admm_tv_solve``: the
-  whole outer iteration (x-update CG with device-side stopping test, z/u
-  updates, iteration statistics) replayed as one CUDA graph.
+  A=XRayTransform2D or XRayTransform3D)``, every ``C_i`` a
+  ``FiniteDifference(append=0)`` over all image axes, ``g_i`` a scaled
+  ``L21Norm()`` and/or ``L1Norm()``, equal ``rho_i``,
+  ``LinearSubproblemSolver`` -- ``solve()`` runs ``ct_admm_tv_solve`` (2D)
+  or ``ct_admm_tv3d_solve`` (3D): the whole outer iteration (x-update CG
+  with device-side stopping test, z/u updates, iteration statistics)
+  replayed as one CUDA graph.
 """
 
 from __future__ import annotations
@@ -222,7 +224,7 @@ class ADMM:
     # -- fused native path ------------------------------------------------------
     def _fused_plan(self):
         f = self.f
-        if not isinstance(f, SquaredL2Loss) or not isinstance(f.A, linop.XRayTransform2D):
+        if not isinstance(f, SquaredL2Loss) or not isinstance(f.A, (linop.XRayTransform2D, linop.XRayTransform3D)):
             return None
         if not isinstance(self.subproblem_solver, LinearSubproblemSolver):
             return None
@@ -232,7 +234,7 @@ class ADMM:
         for C in self.C_list:
             if not isinstance(C, linop.FiniteDifference) or C.input_shape != shape:
                 return None
-            if C.axes != (0, 1) or C.append != 0 or C.prepend is not None or C.circular:
+            if C.axes != tuple(range(len(shape))) or C.append != 0 or C.prepend is not None or C.circular:
                 return None
         kinds = [_g_kind(g) for g in self.g_list]
         if any(k is None for k in kinds) or len({k[0] for k in kinds}) != len(kinds):
@@ -250,32 +252,35 @@ class ADMM:
         A = self.f.A
         cgk = self.subproblem_solver.cg_kwargs
         g = A.geometry()
-        desc = _lib.AdmmTvDesc(g, int(self.maxiter), int(cgk.get("maxiter", 100)), float(cgk.get("tol", 1e-4)),
-                               float(cgk.get("atol", 0.0)), float(plan["lam21"]), float(plan["lam1"]),
-                               float(self.rho_list[0]), float(self.f.scale), float(self.alpha), 1)
+        three = isinstance(A, linop.XRayTransform3D)
+        Desc, fn = (_lib.AdmmTv3dDesc, "ct_admm_tv3d") if three else (_lib.AdmmTvDesc, "ct_admm_tv")
+        desc = Desc(g, int(self.maxiter), int(cgk.get("maxiter", 100)), float(cgk.get("tol", 1e-4)),
+                    float(cgk.get("atol", 0.0)), float(plan["lam21"]), float(plan["lam1"]),
+                    float(self.rho_list[0]), float(self.f.scale), float(self.alpha), 1)
         st = self._fused_state
         first = st is None
         if first:
             nbytes = _lib.c_size_t()
-            _lib.call("ct_admm_tv_workspace", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(nbytes))
+            _lib.call(fn + "_workspace", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(nbytes))
             ws = _device.workspace(nbytes.value)
             zoff, uoff, nt = _lib.c_size_t(), _lib.c_size_t(), _lib.c_int32()
-            _lib.call("ct_admm_tv_state", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(zoff),
+            _lib.call(fn + "_state", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(zoff),
                       _lib.ctypes.addressof(uoff), _lib.ctypes.addressof(nt))
             st = self._fused_state = dict(ws=ws, zoff=zoff.value, uoff=uoff.value, nt=nt.value, y=self.f.y)
         itstat = _device.zeros((max(1, self.maxiter), _lib.CT_ITSTAT_FIELDS), dtype=torch.float64)
         x = self.x.contiguous()
         t0 = time.perf_counter()
-        _lib.call("ct_admm_tv_solve", _lib.ctypes.addressof(desc), st["y"].data_ptr(), x.data_ptr(),
+        _lib.call(fn + "_solve", _lib.ctypes.addressof(desc), st["y"].data_ptr(), x.data_ptr(),
                   itstat.data_ptr(), 0 if first else 1, st["ws"].data_ptr(), st["ws"].numel(), _device.stream())
         torch.cuda.current_stream().synchronize()
         dt = time.perf_counter() - t0
         self.x = x
         # expose z_list / u_list as views of the solver state (in g_list order)
         N = int(np.prod(A.input_shape))
+        nd = len(A.input_shape)
         ws = st["ws"]
-        zs = ws[st["zoff"]:st["zoff"] + st["nt"] * 2 * N * 4].view(torch.float32).view(st["nt"], 2, *A.input_shape)
-        us = ws[st["uoff"]:st["uoff"] + st["nt"] * 2 * N * 4].view(torch.float32).view(st["nt"], 2, *A.input_shape)
+        zs = ws[st["zoff"]:st["zoff"] + st["nt"] * nd * N * 4].view(torch.float32).view(st["nt"], nd, *A.input_shape)
+        us = ws[st["uoff"]:st["uoff"] + st["nt"] * nd * N * 4].view(torch.float32).view(st["nt"], nd, *A.input_shape)
         self.z_list = [zs[k] for k in plan["order"]]
         self.u_list = [us[k] for k in plan["order"]]
         rec = itstat.cpu().numpy()
