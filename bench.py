@@ -349,8 +349,15 @@ def run_gpu(args):
         except Exception as exc:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
-    K = c.cg_maxiter
-    launches_per_step = 4 + c.maxiter * (8 + 7 * K) + 5
+    # Kernel launches of one solve: A^T y, its split sum, z/u init and the
+    # call reset (4); per iteration the pre phase (rhs, forward strips and
+    # gather, residual, itstat, adjoint, CG start = 7), the CG loop body (the
+    # graph's WHILE node runs it exactly CG_It times: forward strips and
+    # gather, adjoint, lhs, CG update, direction = 6) and the z/u update (1);
+    # the itstat epilogue (rhs, forward strips and gather, residual, itstat =
+    # 5).  CG_It comes from the solve's own itstat records.
+    cg_its = [int(v) for v in itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()]
+    launches_per_step = 4 + sum(7 + 6 * k + 1 for k in cg_its) + 5
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -5,7 +5,8 @@
 Ops: proj2d_fwd, proj2d_adj (one C-ABI call each, CUDA events per call),
 admm (one fused ADMM-TV solve of --iters iterations), proj3d_fwd and
 proj3d_adj (the 256^3, 360-view workload; --views N takes the first N views,
---general runs the GENERAL kernels on it).  Prints one JSON line
+--general runs the GENERAL kernels on it), admm3d (one fused 3D ADMM-TV
+solve of --iters iterations on that workload).  Prints one JSON line
 with the median time, interactions/s and the algorithmic-byte bandwidth
 (4 B per pixel-view interaction + the output write).  Used for ncu captures
 of single kernels.
@@ -26,7 +27,7 @@ from . import _device, _lib, linop, workloads
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--op", default="proj2d_fwd",
-                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj"])
+                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
     ap.add_argument("--general", action="store_true",
@@ -41,6 +42,8 @@ def main(argv=None):
     dev = _device.require_cuda()
     if a.op.startswith("proj3d"):
         return _proj3d(a, dev)
+    if a.op == "admm3d":
+        return _admm3d(a, dev)
     c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
     A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
     g = A.geometry()
@@ -137,6 +140,36 @@ def _proj3d(a, dev):
     print(json.dumps({"op": a.op, "config": "c5", "views": nv, "kind": "general" if a.general else A.kind,
                       "median_s": t, "min_s": tmin, "interactions_per_s": inter / t,
                       "alg_gbs": (4.0 * inter + out_bytes) / t / 1e9}))
+
+
+def _admm3d(a, dev):
+    """--iters fused 3D ADMM-TV iterations on the 256^3, 360-view workload
+    (L1 + L2,1 on one FD, rho 1, CG <= 8).  Reports seconds per iteration and
+    the CG steps taken."""
+    c = workloads.C5
+    A = linop.XRayTransform3D(c.shape, c.matrices(), c.det_shape)
+    x_gt = torch.from_numpy(workloads.random_ellipsoids(c.n, c.n_ellipsoids, c.phantom_seed)).to(dev)
+    y = A(x_gt)
+    y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.noise_seed)).to(dev)
+    g = A.geometry()
+    desc = _lib.AdmmTv3dDesc(g, a.iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam_l21, c.lam_l1, c.rho, 0.5, 1.0, a.graph)
+    n = _lib.c_size_t()
+    _lib.call("ct_admm_tv3d_workspace", ctypes.addressof(desc), ctypes.addressof(n))
+    ws = _device.workspace(n.value)
+    x = torch.zeros(c.shape, device=dev)
+    itstat = torch.zeros((a.iters, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev)
+    s = torch.cuda.current_stream()
+
+    def fn():
+        x.zero_()
+        _lib.call("ct_admm_tv3d_solve", ctypes.addressof(desc), y.data_ptr(), x.data_ptr(), itstat.data_ptr(), 0,
+                  ws.data_ptr(), ws.numel(), s.cuda_stream)
+
+    t, tmin = _time(fn, s, a.warmup, a.reps)
+    cg = itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()
+    print(json.dumps({"op": "admm3d", "config": "c5", "iters": a.iters, "graph": a.graph, "median_s": t,
+                      "s_per_iter": t / a.iters, "cg_steps": [int(v) for v in cg],
+                      "objective": [float(v) for v in itstat[:, _lib.CT_ITSTAT_OBJECTIVE].cpu().numpy()]}))
 
 
 if __name__ == "__main__":
