@@ -404,6 +404,31 @@ def cg(A: Callable, b: np.ndarray, x0: np.ndarray, tol=1e-5, atol=0.0, maxiter=1
 # ---------------------------------------------------------------------------
 
 
+def cg_fixed(A: Callable, b: np.ndarray, x0=None, maxiter: int = 50, dot_dtype=None) -> np.ndarray:
+    """Fixed-iteration CG of scico.flax.inverse.cg_solver (flax/inverse.py:
+    113-158): r0 = b - A(x0), p0 = r0, then exactly maxiter steps of
+    alpha = num / <p, Ap>, x += alpha p, r -= alpha Ap, beta = num' / num,
+    p = r + beta p (no stopping test)."""
+    dt = b.dtype
+    dd = np.dtype(dot_dtype if dot_dtype is not None else dt).type
+
+    def dot(u, v):
+        return dd(np.sum(u.astype(dd) * v.astype(dd)))
+
+    x = np.zeros_like(b) if x0 is None else np.asarray(x0, dtype=dt).copy()
+    r = b - A(x)
+    num = dot(r, r)
+    p = r
+    for _ in range(maxiter):
+        Ap = A(p)
+        alpha = num / dot(p, Ap)
+        x = x + dt.type(alpha) * p
+        r = r - dt.type(alpha) * Ap
+        num_old, num = num, dot(r, r)
+        p = r + dt.type(num / num_old) * p
+    return x
+
+
 def admm_tv(fwd: Callable, adj: Callable, y: np.ndarray, shape, lam_l21: float = 0.0, lam_l1: float = 0.0,
             rho: float = 1.0, maxiter: int = 10, cg_tol: float = 1e-4, cg_maxiter: int = 10, x0=None,
             scale: float = 0.5, alpha: float = 1.0, dtype=np.float32, dot_dtype=None):

@@ -6,7 +6,8 @@ Ops: proj2d_fwd, proj2d_adj (one C-ABI call each, CUDA events per call),
 admm (one fused ADMM-TV solve of --iters iterations), proj3d_fwd and
 proj3d_adj (the 256^3, 360-view workload; --views N takes the first N views,
 --general runs the GENERAL kernels on it), admm3d (one fused 3D ADMM-TV
-solve of --iters iterations on that workload).  Prints one JSON line
+solve of --iters iterations on that workload), modl (one MoDL training
+step, forward and backward, on the 16-slice batch).  Prints one JSON line
 with the median time, interactions/s and the algorithmic-byte bandwidth
 (4 B per pixel-view interaction + the output write).  Used for ncu captures
 of single kernels.
@@ -27,9 +28,10 @@ from . import _device, _lib, linop, workloads
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--op", default="proj2d_fwd",
-                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d"])
+                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d", "modl"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
+    ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
     ap.add_argument("--general", action="store_true",
                     help="proj3d: run the GENERAL kernels on the workload's geometry")
     ap.add_argument("--reps", type=int, default=20)
@@ -44,6 +46,8 @@ def main(argv=None):
         return _proj3d(a, dev)
     if a.op == "admm3d":
         return _admm3d(a, dev)
+    if a.op == "modl":
+        return _modl(a, dev)
     c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
     A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
     g = A.geometry()
@@ -170,6 +174,45 @@ def _admm3d(a, dev):
     print(json.dumps({"op": "admm3d", "config": "c5", "iters": a.iters, "graph": a.graph, "median_s": t,
                       "s_per_iter": t / a.iters, "cg_steps": [int(v) for v in cg],
                       "objective": [float(v) for v in itstat[:, _lib.CT_ITSTAT_OBJECTIVE].cpu().numpy()]}))
+
+
+def _modl(a, dev):
+    """One MoDL training step on the C4 batch (16 x 256^2, 180 views; 5
+    blocks of CG(10) on A^T A + lmbda I, 3-layer 32-filter ResNet): forward
+    with the MSE loss, then backward, each timed with CUDA events.
+    Convolutions in full float32 (TF32 off)."""
+    from . import inverse
+
+    torch.backends.cudnn.allow_tf32 = False
+    torch.backends.cuda.matmul.allow_tf32 = False
+    c = workloads.C4
+    H = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+    x_gt = torch.from_numpy(c.phantoms()).to(dev)
+    y = H.project(x_gt)
+    y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.phantom_seed)).to(dev)
+    torch.manual_seed(c.weight_seed)
+    net = inverse.MoDLNet(H, depth=c.depth, channels=1, num_filters=c.num_filters, block_depth=c.block_depth,
+                          lmbda_ini=c.lmbda_ini, cg_iter=c.cg_iter, cg_recompute=a.recompute).to(dev)
+    s = torch.cuda.current_stream()
+    fts, bts = [], []
+    for k in range(a.warmup + a.reps):
+        net.zero_grad(set_to_none=True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(s)
+        loss = ((net(y) - x_gt) ** 2).mean()
+        e1.record(s)
+        loss.backward()
+        e2.record(s)
+        e2.synchronize()
+        if k >= a.warmup:
+            fts.append(e0.elapsed_time(e1) / 1e3)
+            bts.append(e1.elapsed_time(e2) / 1e3)
+    tf, tb = statistics.median(fts), statistics.median(bts)
+    n_proj = c.batch * (c.depth * (c.cg_iter + 1) * 2 + 1)  # A and A^T applications per image in the forward
+    print(json.dumps({"op": "modl", "config": "c4", "batch": c.batch, "recompute": a.recompute,
+                      "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
+                      "images_per_s_train": c.batch / (tf + tb), "projector_applications_forward": n_proj,
+                      "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach())}))
 
 
 if __name__ == "__main__":

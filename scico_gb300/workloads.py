@@ -152,6 +152,40 @@ class Volume3D:
 C5 = Volume3D(256, 360, (256, 363), 0.005, 0.005, 1.0, 30, 8, 1e-4, 6, 30, 0.01, 7)
 
 
+@dataclasses.dataclass
+class MoDLWorkload:
+    """Unrolled MoDL reconstruction of a batch of 2D slices: MoDLNet(depth,
+    ResNet(block_depth, num_filters)) with cg_iter CG steps on A^T A + lmbda I
+    per block, trained with an MSE loss."""
+
+    batch: int
+    n: int
+    n_views: int
+    det_count: int
+    depth: int
+    block_depth: int
+    num_filters: int
+    cg_iter: int
+    lmbda_ini: float
+    phantom_seed: int
+    n_ellipses: int
+    noise: float
+    weight_seed: int
+
+    @property
+    def angles(self) -> np.ndarray:
+        return np.linspace(0, np.pi, self.n_views, endpoint=False)
+
+    def phantoms(self) -> np.ndarray:
+        return np.stack([random_ellipses(self.n, self.n_ellipses, self.phantom_seed * 1000 + k)
+                         for k in range(self.batch)])
+
+
+# C4: 16 x 256^2 slices, 180 views, 363 bins, 5 blocks of CG(10) on
+# A^T A + 0.1 I with a 3-layer, 32-filter ResNet denoiser
+C4 = MoDLWorkload(16, 256, 180, 363, 5, 3, 32, 10, 0.1, 4, 10, 0.01, 5)
+
+
 def batched_configs(count: int = 64, seed: int = 3) -> List[Slice2D]:
     """C3: `count` scans with N from {128..768}, views from {90..720}, det = ceil(sqrt2 N)+1."""
     rng = np.random.default_rng(seed)
