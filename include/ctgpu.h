@@ -303,7 +303,7 @@ ct_status ct_cg_init(const float* b, const float* Ax, float* r, float* p,
                      ct_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
-/* Fused ADMM-TV solver (2D)                                                */
+/* Fused ADMM-TV solver (2D, batches of 2D scans, 3D)                      */
 /* ------------------------------------------------------------------------ */
 
 /*
@@ -358,6 +358,24 @@ ct_status ct_admm_tv_state(const ct_admm_tv_desc* d, size_t* z_offset,
 ct_status ct_admm_tv_solve(const ct_admm_tv_desc* d, const float* y, float* x,
                            double* itstat_dev, int32_t iter0, void* workspace,
                            size_t workspace_bytes, ct_stream_t stream);
+
+/*
+ * Run n independent 2D solves concurrently, each exactly as
+ * ct_admm_tv_solve would: scan k uses descs[k], y[k], x[k], itstat_dev[k]
+ * (itstat_dev itself may be NULL) and its own workspace workspace[k] of
+ * workspace_bytes[k] bytes (ct_admm_tv_workspace of descs[k]).  For many
+ * scans of different sizes (no counterpart in the reference, whose scripts
+ * solve one scan after another): each scan replays its own iteration graph
+ * on one of n_streams internal streams (0 = min(n, 16), at most 32), scans
+ * assigned longest-estimated-first to the least-loaded stream.  All work
+ * starts after prior work on `stream`, and `stream` waits for all of it.
+ */
+ct_status ct_admm_tv_solve_batch(const ct_admm_tv_desc* descs, int32_t n,
+                                 const float* const* y, float* const* x,
+                                 double* const* itstat_dev, int32_t iter0,
+                                 void* const* workspace,
+                                 const size_t* workspace_bytes,
+                                 int32_t n_streams, ct_stream_t stream);
 
 /*
  * The same solver for 3D parallel-beam CT (XRayTransform3D,

@@ -165,6 +165,7 @@ _SIGNATURES = {
     "ct_admm_tv_workspace": (ctypes.c_int, [P, P]),
     "ct_admm_tv_state": (ctypes.c_int, [P, P, P, P]),
     "ct_admm_tv_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),
+    "ct_admm_tv_solve_batch": (ctypes.c_int, [P, c_int32, P, P, P, c_int32, P, P, c_int32, P]),
     "ct_admm_tv3d_workspace": (ctypes.c_int, [P, P]),
     "ct_admm_tv3d_state": (ctypes.c_int, [P, P, P, P]),
     "ct_admm_tv3d_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),

@@ -38,7 +38,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -669,15 +671,24 @@ ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
   return ct::launch_check("k_itstat");
 }
 
-// One cached executable graph of the iteration body (per process).
-struct GraphCache {
-  std::mutex m;
+// Executable iteration graphs, one per problem (key: dimension, descriptor
+// bytes and the state/data pointers), least recently used evicted.  One
+// capture stream per device; graphs are launched on the solve's stream.
+constexpr int kMaxGraphs = 256;
+
+struct GraphEntry {
   unsigned char key[512];
   size_t key_len = 0;
   int device = -1;
   cudaGraphExec_t exec = nullptr;
-  cudaStream_t cs = nullptr;
-  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  unsigned long long last_use = 0;
+};
+
+struct GraphCache {
+  std::mutex m;
+  GraphEntry e[kMaxGraphs];
+  unsigned long long clock = 0;
+  cudaStream_t capture[64] = {nullptr};
 };
 GraphCache g_cache;
 
@@ -749,53 +760,65 @@ ct_status build_iteration_graph(const Ctx& c, cudaStream_t cs, cudaGraph_t& grap
   return ct::cuda_check(ce2, "end capture post");
 }
 
-ct_status run_graph(const Ctx& c, cudaStream_t caller) {
-  std::lock_guard<std::mutex> lock(g_cache.m);
+// The executable iteration graph of a problem (built on first use).
+// Caller holds g_cache.m.
+ct_status graph_for(const Ctx& c, cudaGraphExec_t& exec) {
   int dev = 0;
   CT_TRY(ct::cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
-  if (g_cache.device != dev) {
-    if (g_cache.exec) cudaGraphExecDestroy(g_cache.exec);
-    g_cache.exec = nullptr;
-    g_cache.key_len = 0;
-    CT_TRY(ct::cuda_check(cudaStreamCreateWithFlags(&g_cache.cs, cudaStreamNonBlocking), "stream"));
-    CT_TRY(ct::cuda_check(cudaEventCreateWithFlags(&g_cache.ev_in, cudaEventDisableTiming), "event"));
-    CT_TRY(ct::cuda_check(cudaEventCreateWithFlags(&g_cache.ev_out, cudaEventDisableTiming), "event"));
-    g_cache.device = dev;
-  }
+  if (dev < 0 || dev >= 64) return ct::fail(CT_ERR_UNSUPPORTED, "device %d", dev);
+  if (!g_cache.capture[dev])
+    CT_TRY(ct::cuda_check(cudaStreamCreateWithFlags(&g_cache.capture[dev], cudaStreamNonBlocking),
+                          "capture stream"));
   unsigned char key[512];
   const size_t kl = make_key(c, key);
-  if (!g_cache.exec || kl != g_cache.key_len || memcmp(key, g_cache.key, kl) != 0) {
-    if (g_cache.exec) {
-      cudaGraphExecDestroy(g_cache.exec);
-      g_cache.exec = nullptr;
+  GraphEntry* slot = nullptr;
+  for (GraphEntry& e : g_cache.e) {
+    if (e.exec && e.device == dev && e.key_len == kl && memcmp(e.key, key, kl) == 0) {
+      e.last_use = ++g_cache.clock;
+      exec = e.exec;
+      return CT_OK;
     }
-    cudaGraph_t graph = nullptr;
-    ct_status st = build_iteration_graph(c, g_cache.cs, graph);
-    if (st != CT_OK) {
-      if (graph) cudaGraphDestroy(graph);
-      return st;
-    }
-    cudaError_t ce = cudaGraphInstantiate(&g_cache.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    CT_TRY(ct::cuda_check(ce, "graph instantiate"));
-    memcpy(g_cache.key, key, kl);
-    g_cache.key_len = kl;
+    if (!slot || !e.exec || (slot->exec && e.last_use < slot->last_use)) slot = &e;
   }
-  CT_TRY(ct::cuda_check(cudaEventRecord(g_cache.ev_in, caller), "event record"));
-  CT_TRY(ct::cuda_check(cudaStreamWaitEvent(g_cache.cs, g_cache.ev_in, 0), "stream wait"));
-  for (int k = 0; k < c.P.prm.maxiter; ++k)
-    CT_TRY(ct::cuda_check(cudaGraphLaunch(g_cache.exec, g_cache.cs), "graph launch"));
-  CT_TRY(ct::cuda_check(cudaEventRecord(g_cache.ev_out, g_cache.cs), "event record"));
-  return ct::cuda_check(cudaStreamWaitEvent(caller, g_cache.ev_out, 0), "stream wait");
+  if (slot->exec) {
+    cudaGraphExecDestroy(slot->exec);
+    slot->exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  ct_status st = build_iteration_graph(c, g_cache.capture[dev], graph);
+  if (st != CT_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  cudaError_t ce = cudaGraphInstantiate(&slot->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) slot->exec = nullptr;
+  CT_TRY(ct::cuda_check(ce, "graph instantiate"));
+  memcpy(slot->key, key, kl);
+  slot->key_len = kl;
+  slot->device = dev;
+  slot->last_use = ++g_cache.clock;
+  exec = slot->exec;
+  return CT_OK;
 }
 
-// Solve for either descriptor kind.
+ct_status run_graph(const Ctx& c, cudaStream_t s) {
+  cudaGraphExec_t exec = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_cache.m);
+    CT_TRY(graph_for(c, exec));
+  }
+  for (int k = 0; k < c.P.prm.maxiter; ++k)
+    CT_TRY(ct::cuda_check(cudaGraphLaunch(exec, s), "graph launch"));
+  return CT_OK;
+}
+
+// Validate one problem and fill its solver context.
 template <class D>
-ct_status solve(const D* d, const char* who, const float* y, float* x, double* itstat_dev, int32_t iter0,
-                void* workspace, size_t workspace_bytes, ct_stream_t stream) {
+ct_status make_ctx(const D* d, const char* who, const float* y, float* x, double* itstat_dev,
+                   void* workspace, size_t workspace_bytes, Ctx& c) {
   CT_TRY(check_desc(d, who));
   if (!y || !x) return ct::fail(CT_ERR_INVALID_ARG, "%s: null array", who);
-  Ctx c;
   c.P = problem_of(d);
   c.L = layout(c.P);
   if (!workspace || workspace_bytes < c.L.total || !ct::aligned(workspace, 256))
@@ -822,19 +845,22 @@ ct_status solve(const D* d, const char* who, const float* y, float* x, double* i
   tp.rho = (float)prm.rho;
   tp.alpha = (float)prm.alpha;
   tp.c = (float)(2.0 * prm.loss_scale);
-  cudaStream_t s = ct::as_stream(stream);
-  CT_TRY(c.P.proj.prepare());
+  return c.P.proj.prepare();
+}
 
+// Enqueue one solve on stream s.
+ct_status run_solve(const Ctx& c, int32_t iter0, cudaStream_t s) {
+  const Params& prm = c.P.prm;
   if (iter0 == 0) {
     CT_TRY(ct::cuda_check(cudaMemsetAsync(c.ws, 0, c.L.off_atyc, s), "memset state"));
     // A^T y, scaled by 2*scale (hoisted out of the loop: y is constant).
-    CT_TRY(c.P.proj.adj(y, c.at<float>(c.L.off_adj), c.at<float>(c.L.off_adjpart), s, nullptr));
+    CT_TRY(c.P.proj.adj(c.y, c.at<float>(c.L.off_adj), c.at<float>(c.L.off_adjpart), s, nullptr));
     const int ns = c.P.proj.nsplit();
     const float* src = ns > 1 ? c.at<float>(c.L.off_adjpart) : c.at<float>(c.L.off_adj);
-    k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.P.N, ns, tp.c);
+    k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.P.N, ns, c.tp.c);
     CT_TRY(ct::launch_check("k_scale_splits"));
-    CT_LAUNCH_ND(c.P.nd, k_init_state, NB, NT, s, x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-                 c.at<float>(c.L.off_dz), c.P.sh, c.P.N, tp.ng);
+    CT_LAUNCH_ND(c.P.nd, k_init_state, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
+                 c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp.ng);
     CT_TRY(ct::launch_check("k_init_state"));
   }
   k_reset_call<<<1, 1, 0, s>>>(c.slots());
@@ -846,6 +872,35 @@ ct_status solve(const D* d, const char* who, const float* y, float* x, double* i
     for (int k = 0; k < prm.maxiter; ++k) CT_TRY(enqueue_iteration(c, s));
   }
   return enqueue_epilogue(c, s);
+}
+
+// Solve for either descriptor kind.
+template <class D>
+ct_status solve(const D* d, const char* who, const float* y, float* x, double* itstat_dev, int32_t iter0,
+                void* workspace, size_t workspace_bytes, ct_stream_t stream) {
+  Ctx c;
+  CT_TRY(make_ctx(d, who, y, x, itstat_dev, workspace, workspace_bytes, c));
+  return run_solve(c, iter0, ct::as_stream(stream));
+}
+
+// Internal streams for concurrent solves (per device, created once) and the
+// events that fork them from, and join them back to, the caller's stream.
+constexpr int kMaxBatchStreams = 32;
+
+struct StreamPool {
+  std::mutex m;
+  cudaStream_t s[64][kMaxBatchStreams] = {};
+  cudaEvent_t fork[64] = {};
+  cudaEvent_t join[64][kMaxBatchStreams] = {};
+};
+StreamPool g_pool;
+
+// Estimated device work of one solve: projector interactions per ADMM
+// iteration (at most cg_maxiter + 2 forward/adjoint pairs) plus the
+// elementwise work, times the iterations.
+double solve_cost(const Ctx& c) {
+  const double inter = (double)c.P.N * (c.P.nd == 2 ? c.P.proj.g2->n_views : c.P.proj.g3->n_views);
+  return (double)c.P.prm.maxiter * ((c.P.prm.cg_maxiter + 2) * 2.0 * inter + 40.0 * (double)c.P.N);
 }
 
 template <class D>
@@ -882,6 +937,61 @@ ct_status ct_admm_tv_state(const ct_admm_tv_desc* d, size_t* z_offset, size_t* u
 ct_status ct_admm_tv_solve(const ct_admm_tv_desc* d, const float* y, float* x, double* itstat_dev,
                            int32_t iter0, void* workspace, size_t workspace_bytes, ct_stream_t stream) {
   return solve(d, "ct_admm_tv_solve", y, x, itstat_dev, iter0, workspace, workspace_bytes, stream);
+}
+
+ct_status ct_admm_tv_solve_batch(const ct_admm_tv_desc* descs, int32_t n, const float* const* y,
+                                 float* const* x, double* const* itstat_dev, int32_t iter0,
+                                 void* const* workspace, const size_t* workspace_bytes, int32_t n_streams,
+                                 ct_stream_t stream) {
+  const char* who = "ct_admm_tv_solve_batch";
+  if (n < 0) return ct::fail(CT_ERR_INVALID_ARG, "%s: n=%d", who, n);
+  if (n == 0) return CT_OK;
+  if (!descs || !y || !x || !workspace || !workspace_bytes)
+    return ct::fail(CT_ERR_INVALID_ARG, "%s: null array of per-scan arguments", who);
+  if (n_streams < 0 || n_streams > kMaxBatchStreams)
+    return ct::fail(CT_ERR_INVALID_ARG, "%s: n_streams=%d (0..%d)", who, n_streams, kMaxBatchStreams);
+  std::vector<Ctx> cs((size_t)n);
+  for (int k = 0; k < n; ++k)
+    CT_TRY(make_ctx(&descs[k], who, y[k], x[k], itstat_dev ? itstat_dev[k] : nullptr, workspace[k],
+                    workspace_bytes[k], cs[k]));
+  const int ns = n_streams > 0 ? std::min(n_streams, n) : std::min(n, 16);
+  // longest-processing-time-first assignment to the least-loaded stream
+  std::vector<int> order((size_t)n);
+  for (int k = 0; k < n; ++k) order[k] = k;
+  std::vector<double> cost((size_t)n);
+  for (int k = 0; k < n; ++k) cost[k] = solve_cost(cs[k]);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<double> load((size_t)ns, 0.0);
+  std::vector<int> lane((size_t)n);
+  for (int k : order) {
+    int best = 0;
+    for (int q = 1; q < ns; ++q)
+      if (load[q] < load[best]) best = q;
+    lane[k] = best;
+    load[best] += cost[k];
+  }
+  int dev = 0;
+  CT_TRY(ct::cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  if (dev < 0 || dev >= 64) return ct::fail(CT_ERR_UNSUPPORTED, "%s: device %d", who, dev);
+  std::lock_guard<std::mutex> lock(g_pool.m);
+  if (!g_pool.fork[dev]) {
+    CT_TRY(ct::cuda_check(cudaEventCreateWithFlags(&g_pool.fork[dev], cudaEventDisableTiming), "event"));
+    for (int q = 0; q < kMaxBatchStreams; ++q) {
+      CT_TRY(ct::cuda_check(cudaStreamCreateWithFlags(&g_pool.s[dev][q], cudaStreamNonBlocking), "stream"));
+      CT_TRY(ct::cuda_check(cudaEventCreateWithFlags(&g_pool.join[dev][q], cudaEventDisableTiming), "event"));
+    }
+  }
+  cudaStream_t caller = ct::as_stream(stream);
+  CT_TRY(ct::cuda_check(cudaEventRecord(g_pool.fork[dev], caller), "event record"));
+  for (int q = 0; q < ns; ++q)
+    CT_TRY(ct::cuda_check(cudaStreamWaitEvent(g_pool.s[dev][q], g_pool.fork[dev], 0), "stream wait"));
+  // enqueue in assignment order so each stream starts with its longest scan
+  for (int k : order) CT_TRY(run_solve(cs[k], iter0, g_pool.s[dev][lane[k]]));
+  for (int q = 0; q < ns; ++q) {
+    CT_TRY(ct::cuda_check(cudaEventRecord(g_pool.join[dev][q], g_pool.s[dev][q]), "event record"));
+    CT_TRY(ct::cuda_check(cudaStreamWaitEvent(caller, g_pool.join[dev][q], 0), "stream wait"));
+  }
+  return CT_OK;
 }
 
 ct_status ct_admm_tv3d_workspace(const ct_admm_tv3d_desc* d, size_t* bytes) {

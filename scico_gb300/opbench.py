@@ -7,7 +7,8 @@ admm (one fused ADMM-TV solve of --iters iterations), proj3d_fwd and
 proj3d_adj (the 256^3, 360-view workload; --views N takes the first N views,
 --general runs the GENERAL kernels on it), admm3d (one fused 3D ADMM-TV
 solve of --iters iterations on that workload), modl (one MoDL training
-step, forward and backward, on the 16-slice batch).  Prints one JSON line
+step, forward and backward, on the 16-slice batch), c3 (the 64 uneven scans
+solved in one batch call and in a loop).  Prints one JSON line
 with the median time, interactions/s and the algorithmic-byte bandwidth
 (4 B per pixel-view interaction + the output write).  Used for ncu captures
 of single kernels.
@@ -28,10 +29,12 @@ from . import _device, _lib, linop, workloads
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--op", default="proj2d_fwd",
-                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d", "modl"])
+                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d", "modl",
+                             "c3"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
     ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
+    ap.add_argument("--streams", type=int, default=0, help="c3: internal streams of the batch solve (0 = auto)")
     ap.add_argument("--general", action="store_true",
                     help="proj3d: run the GENERAL kernels on the workload's geometry")
     ap.add_argument("--reps", type=int, default=20)
@@ -48,6 +51,8 @@ def main(argv=None):
         return _admm3d(a, dev)
     if a.op == "modl":
         return _modl(a, dev)
+    if a.op == "c3":
+        return _c3(a, dev)
     c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
     A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
     g = A.geometry()
@@ -213,6 +218,58 @@ def _modl(a, dev):
                       "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
                       "images_per_s_train": c.batch / (tf + tb), "projector_applications_forward": n_proj,
                       "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach())}))
+
+
+def _c3(a, dev):
+    """The 64 uneven scans (N 128..768, 90..720 views), --iters ADMM-TV
+    iterations each: one ct_admm_tv_solve_batch call against the same scans
+    solved one after another with ct_admm_tv_solve (the reference's loop),
+    both from device-resident data, CUDA events."""
+    cfgs = workloads.batched_configs()
+    n = len(cfgs)
+    ys, xs, wss, descs, its, keep = [], [], [], [], [], []
+    for c in cfgs:
+        A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+        x_gt = torch.from_numpy(c.phantom()).to(dev)
+        y = A(x_gt)
+        y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.noise_seed)).to(dev)
+        g = A.geometry()
+        d = _lib.AdmmTvDesc(g, a.iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam, 0.0, c.rho, 0.5, 1.0, 1)
+        nb = _lib.c_size_t()
+        _lib.call("ct_admm_tv_workspace", ctypes.addressof(d), ctypes.addressof(nb))
+        keep.append(A)
+        ys.append(y)
+        xs.append(torch.zeros((c.n, c.n), device=dev))
+        wss.append(_device.workspace(nb.value))
+        its.append(torch.zeros((a.iters, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev))
+        descs.append(d)
+    P = ctypes.c_void_p
+    D = (_lib.AdmmTvDesc * n)(*descs)
+    Y = (P * n)(*[t.data_ptr() for t in ys])
+    X = (P * n)(*[t.data_ptr() for t in xs])
+    I = (P * n)(*[t.data_ptr() for t in its])
+    W = (P * n)(*[t.data_ptr() for t in wss])
+    B = (_lib.c_size_t * n)(*[t.numel() for t in wss])
+    s = torch.cuda.current_stream()
+
+    def batched():
+        for x in xs:
+            x.zero_()
+        _lib.call("ct_admm_tv_solve_batch", ctypes.addressof(D), n, ctypes.addressof(Y), ctypes.addressof(X),
+                  ctypes.addressof(I), 0, ctypes.addressof(W), ctypes.addressof(B), a.streams, s.cuda_stream)
+
+    def looped():
+        for k in range(n):
+            xs[k].zero_()
+            _lib.call("ct_admm_tv_solve", ctypes.addressof(descs[k]), ys[k].data_ptr(), xs[k].data_ptr(),
+                      its[k].data_ptr(), 0, wss[k].data_ptr(), wss[k].numel(), s.cuda_stream)
+
+    tb, _ = _time(batched, s, a.warmup, a.reps)
+    tl, _ = _time(looped, s, a.warmup, a.reps)
+    inter = sum(c.n * c.n * c.n_views for c in cfgs)
+    print(json.dumps({"op": "c3", "scans": n, "iters": a.iters, "streams": a.streams, "batched_s": tb,
+                      "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb,
+                      "interactions_per_application": inter}))
 
 
 if __name__ == "__main__":

@@ -247,7 +247,9 @@ class ADMM:
         order = [native.index(k) for k, _ in kinds]
         return dict(lam21=lam.get("l21", 0.0), lam1=lam.get("l1", 0.0), order=order)
 
-    def _solve_fused(self):
+    def _fused_prepare(self):
+        """Descriptor, workspace (kept across calls) and output buffers of one
+        fused solve of ``maxiter`` iterations."""
         plan = self._fused_plan()
         A = self.f.A
         cgk = self.subproblem_solver.cg_kwargs
@@ -269,12 +271,13 @@ class ADMM:
             st = self._fused_state = dict(ws=ws, zoff=zoff.value, uoff=uoff.value, nt=nt.value, y=self.f.y)
         itstat = _device.zeros((max(1, self.maxiter), _lib.CT_ITSTAT_FIELDS), dtype=torch.float64)
         x = self.x.contiguous()
-        t0 = time.perf_counter()
-        _lib.call(fn + "_solve", _lib.ctypes.addressof(desc), st["y"].data_ptr(), x.data_ptr(),
-                  itstat.data_ptr(), 0 if first else 1, st["ws"].data_ptr(), st["ws"].numel(), _device.stream())
-        torch.cuda.current_stream().synchronize()
-        dt = time.perf_counter() - t0
-        self.x = x
+        return dict(plan=plan, desc=desc, fn=fn, st=st, first=first, itstat=itstat, x=x)
+
+    def _fused_finish(self, run, dt):
+        """Take over x, the z/u state and the iteration records of a fused solve."""
+        A = self.f.A
+        plan, st, itstat = run["plan"], run["st"], run["itstat"]
+        self.x = run["x"]
         # expose z_list / u_list as views of the solver state (in g_list order)
         N = int(np.prod(A.input_shape))
         nd = len(A.input_shape)
@@ -294,6 +297,16 @@ class ADMM:
         self.itnum += self.maxiter
         if self.nanstop and not self._working_vars_finite():
             raise ValueError("NaN or Inf value encountered in a working variable during the fused solve.")
+
+    def _solve_fused(self):
+        run = self._fused_prepare()
+        st = run["st"]
+        t0 = time.perf_counter()
+        _lib.call(run["fn"] + "_solve", _lib.ctypes.addressof(run["desc"]), st["y"].data_ptr(), run["x"].data_ptr(),
+                  run["itstat"].data_ptr(), 0 if run["first"] else 1, st["ws"].data_ptr(), st["ws"].numel(),
+                  _device.stream())
+        torch.cuda.current_stream().synchronize()
+        self._fused_finish(run, time.perf_counter() - t0)
 
     # -- state (_common.py:222-258) --------------------------------------------
     def save_state(self, path: str):
@@ -317,6 +330,47 @@ class ADMM:
                            for r in npz["history"]]
         self._fused_state = None
         self.fused = False  # the fused solver state lives in its workspace; continue generically
+
+
+def solve_batch(solvers: List["ADMM"], n_streams: int = 0) -> List[torch.Tensor]:
+    """Run ``solve()`` of many independent 2D CT-TV ADMM problems at once.
+
+    Each solver must be the fused pattern with an XRayTransform2D (see
+    :class:`ADMM`); sizes, view counts, regularization weights and iteration
+    counts may all differ.  The solves run concurrently through
+    ``ct_admm_tv_solve_batch`` (each scan replays its own iteration graph on
+    one of ``n_streams`` internal streams, 0 = automatic) and give the same
+    iterates as calling ``solve()`` on each.  No counterpart in the
+    reference, whose scripts solve one scan after another.  Returns the
+    solutions in order.
+    """
+    if not solvers:
+        return []
+    for s in solvers:
+        if s._fused_plan() is None or not isinstance(s.f.A, linop.XRayTransform2D):
+            raise ValueError("solve_batch needs 2D problems of the fused ADMM-TV pattern")
+        if s.fused is False:
+            raise ValueError("solve_batch runs the fused solver; a solver has fused=False")
+    runs = [s._fused_prepare() for s in solvers]
+    if len({r["first"] for r in runs}) != 1:
+        raise ValueError("solve_batch: all solvers must be fresh, or all continuing")
+    n = len(runs)
+    P = _lib.ctypes.c_void_p
+    descs = (_lib.AdmmTvDesc * n)(*[r["desc"] for r in runs])
+    ys = (P * n)(*[r["st"]["y"].data_ptr() for r in runs])
+    xs = (P * n)(*[r["x"].data_ptr() for r in runs])
+    its = (P * n)(*[r["itstat"].data_ptr() for r in runs])
+    wss = (P * n)(*[r["st"]["ws"].data_ptr() for r in runs])
+    nbs = (_lib.c_size_t * n)(*[r["st"]["ws"].numel() for r in runs])
+    t0 = time.perf_counter()
+    _lib.call("ct_admm_tv_solve_batch", _lib.ctypes.addressof(descs), n, _lib.ctypes.addressof(ys),
+              _lib.ctypes.addressof(xs), _lib.ctypes.addressof(its), 0 if runs[0]["first"] else 1,
+              _lib.ctypes.addressof(wss), _lib.ctypes.addressof(nbs), int(n_streams), _device.stream())
+    torch.cuda.current_stream().synchronize()
+    dt = time.perf_counter() - t0
+    for s, r in zip(solvers, runs):
+        s._fused_finish(r, dt)
+    return [s.x for s in solvers]
 
 
 def _zeros_like(z):
