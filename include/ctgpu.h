@@ -127,6 +127,16 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
                         int32_t batch, void* workspace, size_t workspace_bytes,
                         ct_stream_t stream);
 
+/*
+ * Ramp filter of XRayTransform2D.fbp (_xray2d.py:158-221): every row of
+ * `sino` (n_rows rows of det_count samples, e.g. batch x n_views) convolved
+ * with the Kak & Slaney eq. (61) ramp filter at tau = 1 and cropped to the
+ * input's samples, as the reference's zero-padded FFT product does.  FBP is
+ * then A^T of the filtered rows, masked and scaled (scico_gb300.linop).
+ */
+ct_status ct_fbp_filter(const float* sino, float* out, int32_t n_rows,
+                        int32_t det_count, ct_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* 3D parallel-beam projector (XRayTransform3D)                             */
 /* ------------------------------------------------------------------------ */

@@ -160,6 +160,31 @@ def xray2d_fbp_filter(N: int) -> np.ndarray:
     return out
 
 
+def xray2d_fbp_rows(y: np.ndarray, dtype=np.float64) -> np.ndarray:
+    """Ramp-filtered sinogram rows of XRayTransform2D.fbp (_xray2d.py:191-195):
+    FFT product of each row and the filter, both zero-padded to 2N-1, inverse
+    FFT, real part of samples (N-1)//2 .. (N-1)//2 + N - 1."""
+    y = np.asarray(y, dtype=dtype)
+    N = y.shape[-1]
+    L = 2 * N - 1
+    h = xray2d_fbp_filter(N).astype(dtype)
+    c = np.fft.ifft(np.fft.fft(h, n=L)[None, :] * np.fft.fft(y, n=L, axis=-1), n=L, axis=-1).real
+    off = (N - 1) // 2
+    return c[..., off:off + N].astype(dtype)
+
+
+def xray2d_fbp(y: np.ndarray, g: dict, dtype=np.float64) -> np.ndarray:
+    """XRayTransform2D.fbp (_xray2d.py:158-197): filtered rows back projected,
+    masked to pixels whose footprint stays on the detector in every view
+    (back projection of ones >= views * (1 - 1e-5)) and scaled by
+    pi * dx0 * dx1 / views."""
+    nv = y.shape[0]
+    ones = np.ones(y.shape, dtype=dtype)
+    mask = xray2d_back_project(ones, g, dtype) >= nv * (1.0 - 1e-5)
+    hy = xray2d_fbp_rows(y, dtype)
+    return (np.pi * g["dx"][0] * g["dx"][1] / nv) * mask * xray2d_back_project(hy, g, dtype)
+
+
 # ---------------------------------------------------------------------------
 # 3D parallel-beam projector -- scico/linop/xray/_xray3d.py
 # ---------------------------------------------------------------------------

@@ -147,6 +147,7 @@ _SIGNATURES = {
     "ct_proj2d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_proj2d_fwd_noalloc": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_proj2d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_fbp_filter": (ctypes.c_int, [P, P, c_int32, c_int32, P]),
     "ct_proj3d_views": (ctypes.c_int, [P, c_int32, P, P, P, P, P, P]),
     "ct_proj3d_workspace": (ctypes.c_int, [P, c_int32, P, P]),
     "ct_proj3d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),

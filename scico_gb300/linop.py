@@ -398,6 +398,27 @@ class XRayTransform2D(LinearOperator):
                   ws.data_ptr(), ws.numel(), _device.stream())
         return out
 
+    def fbp(self, y) -> torch.Tensor:
+        r"""Filtered back projection (scico/linop/xray/_xray2d.py:158-197).
+
+        Each sinogram row is ramp filtered (``ct_fbp_filter``, the filter of
+        ``_ramp_filter``), the result back projected, multiplied by the mask of
+        pixels whose back projection of ones reaches ``num_angles * (1 -
+        1e-5)`` (computed once and kept, as the reference keeps
+        ``fbp_mask``) and scaled by ``pi * dx[0] * dx[1] / num_angles``.
+        Angles are assumed evenly spaced in [0, pi).  Accepts a leading batch
+        axis.
+        """
+        t, batch, has_batch = self._batched(y, self.output_shape, "sinogram")
+        nv = self.output_shape[0]
+        hy = torch.empty_like(t)
+        _lib.call("ct_fbp_filter", t.data_ptr(), hy.data_ptr(), batch * nv, self.det_count, _device.stream())
+        if self.fbp_mask is None:
+            ones = _device.to_device(torch.ones(self.output_shape))
+            self.fbp_mask = self.back_project(ones) >= nv * (1.0 - 1e-5)
+        scale = float(np.pi * self.dx[0] * self.dx[1] / nv)
+        return scale * self.fbp_mask.to(torch.float32) * self.back_project(hy)
+
 
 class XRayTransform3D(LinearOperator):
     r"""General-purpose, 3D, parallel ray X-ray projector.

@@ -161,3 +161,15 @@ def test_admm_tv_oracle_decreases():
     obj = [h["Objective"] for h in hist]
     assert obj[-1] < obj[0]
     assert ctref.snr(x_gt, x) > 10
+
+
+def test_fbp_oracle_reference_quality():
+    """The oracle's FBP meets the reference's own criterion
+    (test_xray_2d.py:88-102, one of its four cases): PSNR > 28 dB."""
+    N = 256
+    x_gt = np.zeros((N, N), dtype=np.float32)
+    x_gt[N // 4:-N // 4, N // 4:-N // 4] = 1.0
+    angles = np.linspace(0, np.pi, 360, endpoint=False)
+    g = ctref.xray2d_defaults((N, N), angles, det_count=N, dx=1.0 / np.sqrt(2))
+    y = ctref.xray2d_project(x_gt, g, np.float64)
+    assert ctref.psnr(x_gt, ctref.xray2d_fbp(y, g)) > 28
