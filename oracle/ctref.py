@@ -521,6 +521,41 @@ def admm_tv(fwd: Callable, adj: Callable, y: np.ndarray, shape, lam_l21: float =
     return x, hist, z, u
 
 
+def padmm_tv(fwd: Callable, adj: Callable, y: np.ndarray, shape, lam: float, alpha: float, rho: float, mu: float,
+             nu: float, maxiter: int, dtype=np.float64):
+    """ProximalADMM (_padmm.py:349-363) on the split of the reference's
+    ct_3d_tv_padmm example: f = 0, A = (C, alpha D) stacked, B = -I, c = 0,
+    g = (1/2 ||y - z0||^2, (lam / alpha) ||z1||_{2,1}).  D = FiniteDifference
+    (append=0) over all axes.  Returns (x, list of (primal, dual) residual
+    norms, fast dual residual)."""
+    f = np.dtype(dtype).type
+    shape = tuple(shape)
+    y = np.asarray(y, dtype=dtype)
+    D = lambda v: fd_eval(v, append=0)
+    DT = lambda d: fd_adj(d, shape, append=0)
+    A = lambda v: (fwd(v), f(alpha) * D(v))
+    AT = lambda w: adj(w[0]) + f(alpha) * DT(w[1])
+    x = np.zeros(shape, dtype=dtype)
+    z = (np.zeros(y.shape, dtype=dtype), np.zeros((len(shape),) + shape, dtype=dtype))
+    u = (np.zeros_like(z[0]), np.zeros_like(z[1]))
+    u_old = u
+    lam_p = 1.0 / (rho * nu)
+    c0 = f(2.0 * 0.5 * lam_p)  # SquaredL2Loss.prox, A = I (loss.py:220-226)
+    hist = []
+    for _ in range(maxiter):
+        x = x - f(1.0 / mu) * AT(tuple(f(2.0) * a - b for a, b in zip(u, u_old)))  # f = 0: prox is identity
+        Ax = A(x)
+        pz = tuple(zk + f(1.0 / nu) * (a - zk + uk) for zk, a, uk in zip(z, Ax, u))  # B^T = -I, B z = -z
+        z_old = z
+        z = ((c0 * y + pz[0]) / (c0 + f(1.0)), l21_prox(pz[1], f((lam / alpha) * lam_p)))
+        u_old = u
+        u = tuple(uk + a - zk for uk, a, zk in zip(u, Ax, z))
+        prim = math.sqrt(sum(float(np.sum((a - zk).astype(np.float64) ** 2)) for a, zk in zip(Ax, z)))
+        dual = math.sqrt(sum(float(np.sum((zk - zo).astype(np.float64) ** 2)) for zk, zo in zip(z, z_old)))
+        hist.append((prim, dual))
+    return x, hist
+
+
 def snr(reference: np.ndarray, comparison: np.ndarray) -> float:
     """scico.metric.snr (scico/metric.py:48-62)."""
     reference = np.asarray(reference, dtype=np.float64)

@@ -5,6 +5,8 @@
   parameter, :198).
 * :class:`L21Norm` -- scico/functional/_norm.py:208-296.
 * :class:`L1Norm` -- scico/functional/_norm.py:65-117.
+* :class:`ZeroFunctional`, :class:`SeparableFunctional` --
+  scico/functional/_functional.py:201-290.
 
 Values are returned as Python floats accumulated in float64 on the device;
 proxes run in the ctgpu kernels.
@@ -64,6 +66,41 @@ class ScaledFunctional(Functional):
 
     def prox(self, v, lam: float = 1.0, **kwargs):
         return self.functional.prox(v, lam * self.scale, **kwargs)
+
+
+class ZeroFunctional(Functional):
+    """The zero functional (scico/functional/_functional.py:270-290): value 0,
+    prox the identity."""
+
+    has_eval = True
+    has_prox = True
+
+    def __call__(self, x) -> float:
+        return 0.0
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        return v
+
+
+class SeparableFunctional(Functional):
+    """Sum of functionals of the blocks of a block variable
+    (scico/functional/_functional.py:201-267): value sum_k f_k(x_k), prox
+    blockwise with the same parameter."""
+
+    def __init__(self, functional_list):
+        self.functional_list = list(functional_list)
+        self.has_eval = all(f.has_eval for f in self.functional_list)
+        self.has_prox = all(f.has_prox for f in self.functional_list)
+
+    def __call__(self, x) -> float:
+        if len(x) != len(self.functional_list):
+            raise ValueError("the number of blocks does not match the number of functionals")
+        return sum(f(xk) for f, xk in zip(self.functional_list, x))
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        if len(v) != len(self.functional_list):
+            raise ValueError("the number of blocks does not match the number of functionals")
+        return tuple(f.prox(vk, lam) for f, vk in zip(self.functional_list, v))
 
 
 def _l2_layout(x: torch.Tensor, l2_axis) -> Tuple[torch.Tensor, int, int, tuple]:

@@ -251,6 +251,66 @@ class Identity(LinearOperator):
         return self
 
 
+class VerticalStack(LinearOperator):
+    """Operators stacked vertically (scico/linop/_stack.py:24-120,
+    scico/operator/_stack.py:87-129): ``A x = (A_0 x, A_1 x, ...)``,
+    ``A^T y = sum_k A_k^T y_k`` in block order.  The output is one stacked
+    tensor when every block has the same shape and ``collapse_output`` is
+    true, else a tuple of blocks (a BlockArray)."""
+
+    def __init__(self, ops: Sequence[LinearOperator], collapse_output: bool = True, jit: bool = False):
+        ops = list(ops)
+        if not ops:
+            raise ValueError("VerticalStack needs at least one operator")
+        if any(op.input_shape != ops[0].input_shape for op in ops):
+            raise ValueError("all operators must have the same input_shape")
+        self.ops = ops
+        shapes = [op.output_shape for op in ops]
+        self.collapsed = collapse_output and all(sh == shapes[0] for sh in shapes) and not isinstance(
+            shapes[0][0] if shapes[0] else None, tuple)
+        out_shape = (len(ops),) + tuple(shapes[0]) if self.collapsed else tuple(shapes)
+
+        def ev(x):
+            blocks = [op(x) for op in ops]
+            return torch.stack(blocks) if self.collapsed else tuple(blocks)
+
+        def ad(y):
+            acc = None
+            for k, op in enumerate(ops):
+                t = op.adj(y[k])
+                acc = t if acc is None else _add(acc, t)
+            return acc
+
+        super().__init__(input_shape=ops[0].input_shape, output_shape=out_shape, eval_fn=ev, adj_fn=ad,
+                         input_dtype=ops[0].input_dtype, output_dtype=ops[0].output_dtype)
+
+
+def power_iteration(A: LinearOperator, maxiter: int = 100, seed: Optional[int] = None):
+    """Largest eigenvalue of a diagonalizable operator by power iteration
+    (scico/linop/_util.py:27-76): v normalized random start; per step
+    ``Av = A v``, ``mu = <v, Av> / ||v||^2``, ``v = Av / ||Av||``.  Norms and
+    inner products in float64.  Returns (mu, v)."""
+    gen = torch.Generator().manual_seed(0 if seed is None else int(seed))
+    v = _device.to_device(torch.randn(A.input_shape, generator=gen))
+    v = v / torch.linalg.vector_norm(v.double()).float()
+    mu = 0.0
+    for _ in range(maxiter):
+        Av = A(v)
+        nAv = float(torch.linalg.vector_norm(Av.double()))
+        if nAv == 0.0:  # a zero operator
+            return 0.0, Av
+        mu = float(torch.sum(v.double() * Av.double())) / float(torch.sum(v.double() ** 2))
+        v = Av / nAv
+    return mu, v
+
+
+def operator_norm(A: LinearOperator, maxiter: int = 100, seed: Optional[int] = None) -> float:
+    """||A||_2 = sqrt(largest eigenvalue of A^H A) by power iteration
+    (scico/linop/_util.py:79-110)."""
+    mu, _ = power_iteration(A.gram_op, maxiter=maxiter, seed=seed)
+    return math.sqrt(max(mu, 0.0))
+
+
 # ---------------------------------------------------------------------------
 # 2D X-ray transform
 # ---------------------------------------------------------------------------

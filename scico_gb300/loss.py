@@ -27,7 +27,6 @@ class SquaredL2Loss(Functional):
     """
 
     has_eval = True
-    has_prox = False
 
     def __init__(self, y, A: Optional[linop.LinearOperator] = None, scale: float = 0.5, W=None,
                  prox_kwargs: Optional[dict] = None):
@@ -37,6 +36,16 @@ class SquaredL2Loss(Functional):
         self.A = linop.Identity(tuple(self.y.shape)) if A is None else A
         self.W = linop.Identity(tuple(self.y.shape))
         self.scale = float(scale)
+        # closed-form prox for a diagonal (here: identity) A (scico/loss.py:220-226)
+        self.has_prox = isinstance(self.A, linop.Identity)
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        """``argmin_x 1/2 ||v - x||^2 + lam scale ||y - x||^2`` for A = I:
+        ``(c y + v) / (c + 1)`` with ``c = 2 scale lam`` (scico/loss.py:220-226)."""
+        if not self.has_prox:
+            raise NotImplementedError("prox of SquaredL2Loss is implemented for A = Identity")
+        c = 2.0 * self.scale * lam
+        return (c * self.y + v) / (c + 1.0)
 
     def __call__(self, x) -> float:
         r = self.y - self.A(x)

@@ -395,3 +395,151 @@ def _flat(v):
     if isinstance(v, tuple):
         return torch.cat([t.reshape(-1) for t in v])
     return v.reshape(-1)
+
+
+def _zeros_of(shape):
+    """Zeros of an array shape or of a block shape (tuple of shapes)."""
+    if len(shape) and isinstance(shape[0], tuple):
+        return tuple(_device.zeros(s) for s in shape)
+    return _device.zeros(shape)
+
+
+def _axpy(a: float, x, y):
+    """a * x + y, blockwise."""
+    if isinstance(x, tuple):
+        return tuple(a * u + v for u, v in zip(x, y))
+    return a * x + y
+
+
+def _minus_c(v, c):
+    if isinstance(c, (int, float)):
+        if c == 0:
+            return v
+        return tuple(t - c for t in v) if isinstance(v, tuple) else v - c
+    return _sub(v, c)
+
+
+PADMMRecord = collections.namedtuple("PADMMRecord", ("Iter", "Time", "Objective", "Prml_Rsdl", "Dual_Rsdl"))
+
+
+class ProximalADMM:
+    r"""Proximal ADMM (scico/optimize/_padmm.py:180-411) for
+    ``argmin f(x) + g(z)  s.t.  A x + B z = c``:
+
+        x <- prox_{f / (rho mu)}(x - A^T(2u - u_old) / mu)
+        z <- prox_{g / (rho nu)}(z - B^T(A x + B z - c + u) / nu)
+        u <- u + A x + B z - c
+
+    with ``mu > ||A||^2``, ``nu > ||B||^2`` (:meth:`estimate_parameters`).
+    ``B = None`` means ``-I``, ``c = None`` zero.  Variables may be block
+    variables (tuples of tensors), as with ``VerticalStack`` A and a
+    ``SeparableFunctional`` g -- the CG-free 3D TV reconstruction of the
+    reference's ct_3d_tv_padmm example.  Every operator application runs in
+    the ctgpu kernels; ``A x`` is computed once per step and used for both
+    the z-update and the u-update.
+    """
+
+    def __init__(self, f: Functional, g: Functional, A: linop.LinearOperator, rho: float, mu: float, nu: float,
+                 B: Optional[linop.LinearOperator] = None, c=None, x0=None, z0=None, u0=None,
+                 fast_dual_residual: bool = True, **kwargs):
+        self.f, self.g, self.A = f, g, A
+        self.B = -linop.Identity(A.output_shape) if B is None else B
+        self.c = 0.0 if c is None else c
+        self.rho, self.mu, self.nu = float(rho), float(mu), float(nu)
+        self.fast_dual_residual = bool(fast_dual_residual)
+        self.x = _zeros_of(A.input_shape) if x0 is None else _device.to_device(x0, shape=A.input_shape, name="x0")
+        self.z = _zeros_of(self.B.input_shape) if z0 is None else z0
+        self.z_old = self.z
+        self.u = _zeros_of(A.output_shape) if u0 is None else u0
+        self.u_old = self.u
+        self.itnum = kwargs.pop("iter0", 0)
+        self.maxiter = kwargs.pop("maxiter", 100)
+        self.nanstop = kwargs.pop("nanstop", False)
+        itstat_options = kwargs.pop("itstat_options", None) or {}
+        if kwargs:
+            raise TypeError(f"Unrecognized keyword argument(s) {', '.join(kwargs)}")
+        self.itstat_display = bool(itstat_options.get("display", False))
+        self.itstat_period = int(itstat_options.get("period", 1))
+        self.iterations: List[PADMMRecord] = []
+        self._elapsed = 0.0
+        self._Ax = None
+
+    # -- reference quantities (:121-176, 294-347) -----------------------------
+    def objective(self, x=None, z=None) -> float:
+        if (x is None) != (z is None):
+            raise ValueError("Both or neither of arguments 'x' and 'z' must be supplied")
+        if x is None:
+            x, z = self.x, self.z
+        return self.f(x) + self.g(z)
+
+    def norm_primal_residual(self, x=None, z=None) -> float:
+        if (x is None) != (z is None):
+            raise ValueError("Both or neither of arguments 'x' and 'z' must be supplied")
+        Ax = self.A(self.x) if x is None and self._Ax is None else (self._Ax if x is None else self.A(x))
+        z = self.z if z is None else z
+        return math.sqrt(_sqnorm(_flat(_minus_c(_add(Ax, self.B(z)), self.c))))
+
+    def norm_dual_residual(self) -> float:
+        d = _sub(self.z, self.z_old)
+        if not self.fast_dual_residual:
+            d = self.A.adj(self.B(d))
+        return math.sqrt(_sqnorm(_flat(d)))
+
+    def minimizer(self):
+        return self.x
+
+    def _working_vars_finite(self) -> bool:
+        for v in (self.x, self.z, self.u):
+            for t in (v if isinstance(v, tuple) else (v,)):
+                if not bool(torch.isfinite(t).all()):
+                    return False
+        return True
+
+    # -- iteration (:349-363) ---------------------------------------------------
+    def step(self):
+        proxarg = _axpy(-1.0 / self.mu, self.A.adj(_lin(2.0, self.u, -1.0, self.u_old)), self.x)
+        self.x = self.f.prox(proxarg, 1.0 / (self.rho * self.mu), v0=self.x)
+        Ax = self.A(self.x)
+        proxarg = _axpy(-1.0 / self.nu, self.B.adj(_add(_minus_c(_add(Ax, self.B(self.z)), self.c), self.u)),
+                        self.z)
+        self.z_old = self.z
+        self.z = self.g.prox(proxarg, 1.0 / (self.rho * self.nu), v0=self.z)
+        self.u_old = self.u
+        self.u = _add(self.u, _minus_c(_add(Ax, self.B(self.z)), self.c))
+        self._Ax = Ax
+
+    def solve(self, callback: Optional[Callable] = None):
+        """Run ``maxiter`` iterations (Optimizer.solve, _common.py:287-320)."""
+        t0 = time.perf_counter()
+        evaluatable = getattr(self.f, "has_eval", False) and getattr(self.g, "has_eval", False)
+        for self.itnum in range(self.itnum, self.itnum + self.maxiter):
+            self.step()
+            if self.nanstop and not self._working_vars_finite():
+                raise ValueError(f"NaN or Inf value encountered in working variable in iteration {self.itnum}.")
+            rec = PADMMRecord(self.itnum, self._elapsed + time.perf_counter() - t0,
+                              self.objective() if evaluatable else float("nan"), self.norm_primal_residual(),
+                              self.norm_dual_residual())
+            self.iterations.append(rec)
+            if self.itstat_display and rec.Iter % self.itstat_period == 0:
+                print("  ".join(f"{k}={v:.4g}" if isinstance(v, float) else f"{k}={v}"
+                                for k, v in rec._asdict().items()))
+            if callback:
+                callback(self)
+        self._elapsed += time.perf_counter() - t0
+        self.itnum += 1
+        return self.minimizer()
+
+    def history(self, transpose: bool = False):
+        if transpose:
+            return PADMMRecord(*[list(col) for col in zip(*self.iterations)]) if self.iterations else \
+                PADMMRecord(*[[] for _ in PADMMRecord._fields])
+        return list(self.iterations)
+
+    @staticmethod
+    def estimate_parameters(A: linop.LinearOperator, B: Optional[linop.LinearOperator] = None,
+                            factor: Optional[float] = 1.01, maxiter: int = 100, seed: Optional[int] = None):
+        """(mu, nu) = factor * (||A||^2, ||B||^2) by power iteration, nu = 1
+        for B = -I (:365-411)."""
+        mu = linop.operator_norm(A, maxiter=maxiter, seed=seed) ** 2
+        nu = 1.0 if B is None else linop.operator_norm(B, maxiter=maxiter, seed=seed) ** 2
+        return (mu, nu) if factor is None else (factor * mu, factor * nu)
