@@ -556,6 +556,42 @@ def padmm_tv(fwd: Callable, adj: Callable, y: np.ndarray, shape, lam: float, alp
     return x, hist
 
 
+def haar_fwd(x: np.ndarray, axes) -> np.ndarray:
+    """Single-level shift-invariant Haar transform (_tvnorm.py:458-538):
+    per axis (x + roll(x, -1)) / sqrt2 and (roll(x, -1) - x) / sqrt2."""
+    r = 1.0 / math.sqrt(2.0)
+    return np.stack([np.stack((r * (x + np.roll(x, -1, a)), r * (np.roll(x, -1, a) - x))) for a in axes])
+
+
+def haar_adj(w: np.ndarray, axes) -> np.ndarray:
+    r = 1.0 / math.sqrt(2.0)
+    return sum(r * (w[k, 0] + np.roll(w[k, 0], 1, a)) + r * (np.roll(w[k, 1], 1, a) - w[k, 1])
+               for k, a in enumerate(axes))
+
+
+def tv_prox(v: np.ndarray, lam: float, isotropic: bool, circular: bool, axes=None, dtype=np.float64) -> np.ndarray:
+    """TVNorm.prox (_tvnorm.py:183-237): the base norm's prox, parameter
+    sqrt2 K lam (K = 2 naxes), on the highpass Haar components of v --
+    replicate-padded by one on the differenced axes and restricted to the
+    non-boundary region when not circular -- then 1/K times the adjoint
+    transform, cropped."""
+    v = np.asarray(v, dtype=dtype)
+    nd = v.ndim
+    axes = tuple(range(nd)) if axes is None else tuple(axes)
+    K = 2 * len(axes)
+    thr = math.sqrt(2.0) * K * lam
+    prox = (lambda t: l21_prox(t, thr)) if isotropic else (lambda t: l1_prox(t, thr))
+    if circular:
+        w = haar_fwd(v, axes)
+        w[:, 1] = prox(w[:, 1])
+        return haar_adj(w, axes) / K
+    vp = np.pad(v, [(0, 1) if a in axes else (0, 0) for a in range(nd)], mode="edge")
+    w = haar_fwd(vp, axes)
+    region = (slice(None), 1) + tuple(slice(0, vp.shape[a] - 1) if a in axes else slice(None) for a in range(nd))
+    w[region] = prox(w[region])
+    return (haar_adj(w, axes) / K)[tuple(slice(0, n) for n in v.shape)]
+
+
 def snr(reference: np.ndarray, comparison: np.ndarray) -> float:
     """scico.metric.snr (scico/metric.py:48-62)."""
     reference = np.asarray(reference, dtype=np.float64)

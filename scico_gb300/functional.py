@@ -7,6 +7,9 @@
 * :class:`L1Norm` -- scico/functional/_norm.py:65-117.
 * :class:`ZeroFunctional`, :class:`SeparableFunctional` --
   scico/functional/_functional.py:201-290.
+* :class:`AnisotropicTVNorm`, :class:`IsotropicTVNorm`, :func:`haar_transform`
+  -- scico/functional/_tvnorm.py:33-538 (TV norm with the shift-invariant
+  Haar approximation of its prox).
 
 Values are returned as Python floats accumulated in float64 on the device;
 proxes run in the ctgpu kernels.
@@ -14,6 +17,7 @@ proxes run in the ctgpu kernels.
 
 from __future__ import annotations
 
+import math
 from typing import Tuple, Union
 
 import numpy as np
@@ -183,3 +187,123 @@ class L1Norm(Functional):
         _lib.call("ct_l1_prox", t.data_ptr(), out.data_ptr(), t.numel(), float(np.float32(lam)),
                   _device.stream())
         return out
+
+
+# ---------------------------------------------------------------------------
+# TV norms (scico/functional/_tvnorm.py)
+# ---------------------------------------------------------------------------
+
+_R2 = 1.0 / math.sqrt(2.0)
+
+
+def _haar_fwd(x: torch.Tensor, axes) -> torch.Tensor:
+    """Single-level shift-invariant Haar transform (HaarTransform,
+    _tvnorm.py:458-538): per axis a lowpass (x + x shifted by one, circular)
+    and highpass (x shifted by one - x) component, each / sqrt(2), stacked
+    to (naxes, 2, *shape)."""
+    out = []
+    for a in axes:
+        xs = torch.roll(x, -1, dims=a)
+        out.append(torch.stack((_R2 * (x + xs), _R2 * (xs - x))))
+    return torch.stack(out)
+
+
+def _haar_adj(w: torch.Tensor, axes) -> torch.Tensor:
+    """Adjoint of _haar_fwd: sum over axes of the adjoint of each component."""
+    acc = None
+    for k, a in enumerate(axes):
+        lo, hi = w[k, 0], w[k, 1]
+        t = _R2 * (lo + torch.roll(lo, 1, dims=a)) + _R2 * (torch.roll(hi, 1, dims=a) - hi)
+        acc = t if acc is None else acc + t
+    return acc
+
+
+def haar_transform(x, axes=None, adjoint: bool = False) -> torch.Tensor:
+    """HaarTransform (or its adjoint) of a device tensor over `axes` (all
+    axes if None)."""
+    x = _device.to_device(x)
+    if adjoint:
+        nd = x.ndim - 2
+        axes = tuple(range(nd)) if axes is None else tuple(a % nd for a in ((axes,) if isinstance(axes, int) else axes))
+        return _haar_adj(x, axes)
+    nd = x.ndim
+    axes = tuple(range(nd)) if axes is None else tuple(a % nd for a in ((axes,) if isinstance(axes, int) else axes))
+    return _haar_fwd(x, axes)
+
+
+class TVNorm(Functional):
+    """Total variation norm ``norm(D x)`` with the approximate prox of
+    Kamilov (2016) / Chandler (2024) (scico/functional/_tvnorm.py:33-237):
+    D = FiniteDifference over `axes` (circular, or append=0 otherwise); the
+    prox applies the base norm's prox with parameter sqrt(2) K lam (K = 2
+    naxes) to the highpass part of the single-level shift-invariant Haar
+    transform of v -- edge-padded by one on the differenced axes when not
+    circular, only the non-boundary region shrunk -- and returns 1/K times
+    the adjoint transform, cropped back."""
+
+    has_eval = True
+    has_prox = True
+
+    def __init__(self, norm: Functional, circular: bool = True, axes=None, input_shape=None,
+                 input_dtype=np.float32):
+        self.norm = norm
+        self.circular = bool(circular)
+        self.axes = axes
+        self._G = None
+
+    def _axes_of(self, nd):
+        if self.axes is None:
+            return tuple(range(nd))
+        ax = (self.axes,) if isinstance(self.axes, (int, np.integer)) else tuple(self.axes)
+        return tuple(int(a) % nd for a in ax)
+
+    def __call__(self, x) -> float:
+        from . import linop
+
+        x = _device.to_device(x)
+        shape = tuple(x.shape)
+        if self._G is None or self._G.input_shape != shape:
+            self._G = linop.FiniteDifference(shape, axes=self._axes_of(len(shape)), circular=self.circular,
+                                             append=None if self.circular else 0)
+        return self.norm(self._G(x))
+
+    def prox(self, v, lam: float = 1.0, **kwargs):
+        v = _device.to_device(v)
+        nd = v.ndim
+        axes = self._axes_of(nd)
+        K = 2 * len(axes)
+        if self.circular:
+            w = _haar_fwd(v, axes)
+            hi = w[:, 1].contiguous()
+            w[:, 1] = self.norm.prox(hi, math.sqrt(2.0) * K * lam)
+            return (1.0 / K) * _haar_adj(w, axes)
+        # replicate-pad by one at the end of each differenced axis
+        vp = v
+        for a in axes:
+            last = vp.narrow(a, vp.shape[a] - 1, 1)
+            vp = torch.cat((vp, last), dim=a)
+        w = _haar_fwd(vp, axes)
+        region = [slice(None)] * (nd + 2)
+        region[1] = 1
+        for a in axes:
+            region[2 + a] = slice(0, vp.shape[a] - 1)
+        region = tuple(region)
+        hi = w[region].contiguous()
+        w[region] = self.norm.prox(hi, math.sqrt(2.0) * K * lam)
+        u = _haar_adj(w, axes)
+        crop = tuple(slice(0, v.shape[a]) for a in range(nd))
+        return (1.0 / K) * u[crop]
+
+
+class AnisotropicTVNorm(TVNorm):
+    """Anisotropic TV: ``L1Norm(D x)`` (scico/functional/_tvnorm.py:239-294)."""
+
+    def __init__(self, circular: bool = False, axes=None, input_shape=None, input_dtype=np.float32):
+        super().__init__(L1Norm(), circular=circular, axes=axes, input_shape=input_shape, input_dtype=input_dtype)
+
+
+class IsotropicTVNorm(TVNorm):
+    """Isotropic TV: ``L21Norm(D x)`` (scico/functional/_tvnorm.py:297-352)."""
+
+    def __init__(self, circular: bool = False, axes=None, input_shape=None, input_dtype=np.float32):
+        super().__init__(L21Norm(), circular=circular, axes=axes, input_shape=input_shape, input_dtype=input_dtype)

@@ -51,6 +51,11 @@ class SquaredL2Loss(Functional):
         r = self.y - self.A(x)
         return self.scale * _sqnorm(r)
 
+    def grad(self, x):
+        """Gradient ``2 scale A^T (A x - y)`` (the reference differentiates
+        scale ||y - A x||^2 with jax.grad, scico/loss.py:104)."""
+        return (2.0 * self.scale) * self.A.adj(self.A(x) - self.y)
+
     @property
     def hessian(self) -> linop.LinearOperator:
         """``2 * scale * A^T W A`` (scico/loss.py:245-262)."""

@@ -543,3 +543,108 @@ class ProximalADMM:
         mu = linop.operator_norm(A, maxiter=maxiter, seed=seed) ** 2
         nu = 1.0 if B is None else linop.operator_norm(B, maxiter=maxiter, seed=seed) ** 2
         return (mu, nu) if factor is None else (factor * mu, factor * nu)
+
+
+PGMRecord = collections.namedtuple("PGMRecord", ("Iter", "Time", "Objective", "L", "Residual"))
+
+
+class PGMStepSize:
+    """Constant step size 1/L0 (scico/optimize/_pgmaux.py PGMStepSize)."""
+
+    def internal_init(self, solver):
+        self.solver = solver
+
+    def update(self, v) -> float:
+        return self.solver.L
+
+
+class PGM:
+    r"""Proximal gradient method (scico/optimize/_pgm.py:30-180) for
+    ``f(x) + g(x)``: ``x <- prox_{g/L}(x - grad f(x) / L)``."""
+
+    def __init__(self, f: Functional, g: Functional, L0: float, x0, step_size: Optional[PGMStepSize] = None,
+                 **kwargs):
+        self.f = f
+        if g.has_prox is not True:
+            raise ValueError(f"Functional 'g' ({type(g)}) must have a prox method.")
+        self.g = g
+        self.step_size = PGMStepSize() if step_size is None else step_size
+        self.step_size.internal_init(self)
+        self.L = float(L0)
+        self.fixed_point_residual = float("inf")
+        self.x = _device.to_device(x0, name="x0").clone()
+        self.itnum = kwargs.pop("iter0", 0)
+        self.maxiter = kwargs.pop("maxiter", 100)
+        self.nanstop = kwargs.pop("nanstop", False)
+        itstat_options = kwargs.pop("itstat_options", None) or {}
+        if kwargs:
+            raise TypeError(f"Unrecognized keyword argument(s) {', '.join(kwargs)}")
+        self.itstat_display = bool(itstat_options.get("display", False))
+        self.itstat_period = int(itstat_options.get("period", 1))
+        self.iterations: List[PGMRecord] = []
+        self._elapsed = 0.0
+
+    def x_step(self, v, L: float):
+        return self.g.prox(v - (1.0 / L) * self.f.grad(v), 1.0 / L)
+
+    def objective(self, x=None) -> float:
+        x = self.x if x is None else x
+        return self.f(x) + self.g(x)
+
+    def norm_residual(self) -> float:
+        return self.fixed_point_residual
+
+    def minimizer(self):
+        return self.x
+
+    def step(self):
+        self.L = self.step_size.update(self.x)
+        x = self.x_step(self.x, self.L)
+        self.fixed_point_residual = math.sqrt(_sqnorm((self.x - x).reshape(-1)))
+        self.x = x
+
+    def solve(self, callback: Optional[Callable] = None):
+        t0 = time.perf_counter()
+        evaluatable = getattr(self.f, "has_eval", False) and getattr(self.g, "has_eval", False)
+        for self.itnum in range(self.itnum, self.itnum + self.maxiter):
+            self.step()
+            if self.nanstop and not bool(torch.isfinite(self.x).all()):
+                raise ValueError(f"NaN or Inf value encountered in working variable in iteration {self.itnum}.")
+            rec = PGMRecord(self.itnum, self._elapsed + time.perf_counter() - t0,
+                            self.objective() if evaluatable else float("nan"), self.L, self.norm_residual())
+            self.iterations.append(rec)
+            if self.itstat_display and rec.Iter % self.itstat_period == 0:
+                print("  ".join(f"{k}={v:.4g}" if isinstance(v, float) else f"{k}={v}"
+                                for k, v in rec._asdict().items()))
+            if callback:
+                callback(self)
+        self._elapsed += time.perf_counter() - t0
+        self.itnum += 1
+        return self.minimizer()
+
+    def history(self, transpose: bool = False):
+        if transpose:
+            return PGMRecord(*[list(col) for col in zip(*self.iterations)]) if self.iterations else \
+                PGMRecord(*[[] for _ in PGMRecord._fields])
+        return list(self.iterations)
+
+
+class AcceleratedPGM(PGM):
+    r"""Accelerated PGM / FISTA (scico/optimize/_pgm.py:183-252):
+    ``x <- prox step at v``, ``t' = (1 + sqrt(1 + 4 t^2)) / 2``,
+    ``v <- x + (t - 1)/t' (x - x_old)``."""
+
+    def __init__(self, f: Functional, g: Functional, L0: float, x0, step_size: Optional[PGMStepSize] = None,
+                 **kwargs):
+        super().__init__(f=f, g=g, L0=L0, x0=x0, step_size=step_size, **kwargs)
+        self.v = self.x.clone()
+        self.t = 1.0
+
+    def step(self):
+        x_old = self.x
+        self.L = self.step_size.update(self.v)
+        self.x = self.x_step(self.v, self.L)
+        self.fixed_point_residual = math.sqrt(_sqnorm((self.x - self.v).reshape(-1)))
+        t_old = self.t
+        self.t = 0.5 * (1.0 + math.sqrt(1.0 + 4.0 * t_old ** 2))
+        self.v = self.x + ((t_old - 1.0) / self.t) * (self.x - x_old)

@@ -64,6 +64,17 @@ def random_ellipsoids(n: int, count: int, seed: int, semi=(0.05, 0.35)) -> np.nd
     return np.clip(vol, 0.0, 1.0)
 
 
+def circular_phantom(shape, radii, values) -> np.ndarray:
+    """Concentric discs (or balls) about the array centre: each radius in
+    turn sets the points closer than it to its value (later ones on top)."""
+    grids = np.meshgrid(*[np.arange(n) - (n - 1) / 2 for n in shape], indexing="ij", sparse=True)
+    dist = np.sqrt(sum(g.astype(np.float64) ** 2 for g in grids))
+    out = np.zeros(shape)
+    for r, v in zip(radii, values):
+        out[dist < r] = v
+    return out
+
+
 def noisy(y: np.ndarray, rel_sigma: float, seed: int) -> np.ndarray:
     """y + N(0, (rel_sigma * max|y|)^2), float32."""
     rng = np.random.default_rng(seed)

@@ -173,3 +173,10 @@ def test_fbp_oracle_reference_quality():
     g = ctref.xray2d_defaults((N, N), angles, det_count=N, dx=1.0 / np.sqrt(2))
     y = ctref.xray2d_project(x_gt, g, np.float64)
     assert ctref.psnr(x_gt, ctref.xray2d_fbp(y, g)) > 28
+
+
+def test_haar_oracle_identities():
+    """test_tvnorm.py:13-25: H^T H x = 2 x per axis, 4 x over two axes."""
+    x = np.random.default_rng(1234).standard_normal((3, 4))
+    for axes, k in (((0,), 2), ((1,), 2), ((0, 1), 4)):
+        np.testing.assert_allclose(ctref.haar_adj(ctref.haar_fwd(x, axes), axes), k * x, rtol=1e-12, atol=1e-12)
