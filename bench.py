@@ -19,6 +19,9 @@ synthetic sinogram (20-ellipse phantom, 0.5%-of-peak Gaussian noise).
   cpu_baseline  the C/OpenMP restatement of scico's path (reference float32
             policy) timed on the host cores on a bounded sample.
 
+``--config c5`` runs the 3D workload instead (256^3 volume, 360 views about
+axis 0, L1 + L2,1 TV, 30 iterations, CG <= 8), with the same keys.
+
 ``--impl reference`` times that CPU restatement alone as the reference arm
 (scico itself runs on JAX, which is not installable on these machines).
 Multi-GPU (``--gpus N`` under torchrun): independent replicas, no collective
@@ -54,7 +57,8 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"],
+                    help="c1/c2: 2D ADMM-TV (default c2); c5: 3D ADMM-TV, 256^3 x 360 views")
     ap.add_argument("--cpu-iters", type=int, default=1, help="ADMM iterations per CPU-baseline sample")
     return ap.parse_args()
 
@@ -62,7 +66,7 @@ def _args():
 def _workload(name):
     from scico_gb300 import workloads
 
-    return {"c1": workloads.C1, "c2": workloads.C2}[name]
+    return {"c1": workloads.C1, "c2": workloads.C2, "c5": workloads.C5}[name]
 
 
 def _config_json(c, name):
@@ -159,12 +163,62 @@ def cpu_sample(c, iters: int, threads: int):
     return iters / dt, used, dt
 
 
+def cpu_sample_3d(c, cg_steps: float, threads: int):
+    """CPU estimate of one 3D ADMM-TV iteration: one forward and one adjoint
+    of the C/OpenMP 3D projector on the workload, times the reference's
+    K + 2 forward/adjoint pairs per iteration (K = CG steps).  Returns
+    (iterations/s, threads, seconds timed, seconds per iteration)."""
+    from oracle import ctref_c
+
+    used = ctref_c.set_threads(threads)
+    G = ctref_c.Geometry3D(c.shape, c.matrices().astype(np.float32), c.det_shape)
+    x = c.phantom()
+    t0 = time.perf_counter()
+    y = G.project(x)
+    t1 = time.perf_counter()
+    G.back_project(y)
+    t2 = time.perf_counter()
+    per_iter = (cg_steps + 2.0) * (t2 - t0)
+    return 1.0 / per_iter, used, t2 - t0, per_iter
+
+
+def _config_json_3d(c, name):
+    return {
+        "workload": f"ct_admm_tv_3d_{c.n}^3_{c.n_views}v_{c.det_shape[0]}x{c.det_shape[1]}",
+        "config": name, "volume": c.n, "views": c.n_views, "det_shape": list(c.det_shape),
+        "admm_iters_per_step": c.maxiter, "cg_maxiter": c.cg_maxiter, "lambda_l1": c.lam_l1,
+        "lambda_l21": c.lam_l21, "rho": c.rho, "l2_flush": "inputs (64 MB volume, 134 MB projections) plus a "
+        "256 MB write before every step", "parallelism": "replicas",
+    }
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     from oracle import ctref_c
 
+    if args.config == "c5":
+        c = _workload("c5")
+        threads = ctref_c.default_threads()
+        vals, used, tsum = [], threads, 0.0
+        for k in range(args.warmup + args.steps):
+            v, used, dt, _ = cpu_sample_3d(c, c.cg_maxiter, threads)
+            if k >= args.warmup:
+                vals.append(v)
+                tsum += dt
+        value = statistics.median(vals)
+        sample = (f"one forward and one adjoint of the C/OpenMP 3D projector per step on the {c.n}^3 x "
+                  f"{c.n_views}-view workload, extrapolated to {c.cg_maxiter} + 2 pairs per ADMM iteration "
+                  "(scico runs on JAX, not installable here)")
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tsum / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 30-ellipsoid phantom)", "config": _config_json_3d(c, "c5"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+        return 0
     c = _workload(args.config)
     threads = ctref_c.default_threads()
     for _ in range(args.warmup):
@@ -386,10 +440,163 @@ def run_gpu(args):
     return 0
 
 
+def run_gpu_3d(args):
+    """The 3D workload (C5): value through ct_admm_tv3d_solve, e2e through
+    ADMM(...).solve() with XRayTransform3D, roofline of ct_proj3d_fwd."""
+    import ctypes
+
+    import torch
+
+    from scico_gb300 import _device, _lib, functional, linop, loss, workloads
+    from scico_gb300.optimize import ADMM, LinearSubproblemSolver
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    c = workloads.C5
+    A = linop.XRayTransform3D(c.shape, c.matrices(), c.det_shape)
+    x_gt = torch.from_numpy(c.phantom()).to(dev)
+    y_dev = A(x_gt)
+    gen = torch.Generator().manual_seed(c.noise_seed)
+    y_dev = y_dev + c.noise * y_dev.abs().max() * torch.randn(y_dev.shape, generator=gen).to(dev)
+    y_host = y_dev.cpu().pin_memory()
+    g = A.geometry()
+    desc = _lib.AdmmTv3dDesc(g, c.maxiter, c.cg_maxiter, c.cg_tol, 0.0, c.lam_l21, c.lam_l1, c.rho, 0.5, 1.0, 1)
+    nbytes = _lib.c_size_t()
+    _lib.call("ct_admm_tv3d_workspace", ctypes.addressof(desc), ctypes.addressof(nbytes))
+    ws = _device.workspace(nbytes.value)
+    x = torch.zeros(c.shape, device=dev)
+    itstat = torch.zeros((c.maxiter, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def solve():
+        x.zero_()
+        _lib.call("ct_admm_tv3d_solve", ctypes.addressof(desc), y_dev.data_ptr(), x.data_ptr(), itstat.data_ptr(),
+                  0, ws.data_ptr(), ws.numel(), stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        solve()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    times = []
+    with ClockSampler(dev.index) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solve()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    barrier()
+    t_max = sum(times)
+    if dist is not None:
+        tt = torch.tensor([t_max], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = c.maxiter * args.steps * world / t_max
+    cg_its = [int(v) for v in itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()]
+    x_dev = x.clone()
+
+    def e2e_step():
+        yd = torch.empty(A.output_shape, device=dev)
+        yd.copy_(y_host, non_blocking=True)
+        f = loss.SquaredL2Loss(y=yd, A=A)
+        C = linop.FiniteDifference(c.shape, append=0)
+        s = ADMM(f=f, g_list=[c.lam_l21 * functional.L21Norm(), c.lam_l1 * functional.L1Norm()], C_list=[C, C],
+                 rho_list=[c.rho] * 2, maxiter=c.maxiter,
+                 subproblem_solver=LinearSubproblemSolver(cg_kwargs={"tol": c.cg_tol, "maxiter": c.cg_maxiter}))
+        return s.solve().cpu()
+
+    e2e_step()
+    barrier()
+    e2e_t = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xr = e2e_step()
+        e2e_t += time.perf_counter() - t0
+    barrier()
+    e2e_value = c.maxiter * args.steps * world / e2e_t
+    e2e_diff = float((xr.to(dev) - x_dev).norm() / x_dev.norm())
+
+    # roofline: the 3D forward projector, live CUDA events
+    fwd_b, _ = A.workspace_bytes(1)
+    pws = _device.workspace(fwd_b)
+    proj = torch.empty(A.output_shape, device=dev)
+    for _ in range(3):
+        _lib.call("ct_proj3d_fwd", ctypes.addressof(g), x_dev.data_ptr(), proj.data_ptr(), 1, pws.data_ptr(),
+                  pws.numel(), stream.cuda_stream)
+    ts = []
+    for _ in range(10):
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        _lib.call("ct_proj3d_fwd", ctypes.addressof(g), x_dev.data_ptr(), proj.data_ptr(), 1, pws.data_ptr(),
+                  pws.numel(), stream.cuda_stream)
+        a1.record(stream)
+        a1.synchronize()
+        ts.append(a0.elapsed_time(a1) / 1e3)
+    t_fwd = statistics.median(ts)
+    inter = c.interactions
+    alg = 4.0 * inter + 4.0 * proj.numel()
+    peak, peak_kind = _hbm_peak()
+    achieved = alg / t_fwd / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1:
+        try:
+            from oracle import ctref_c
+
+            k = float(np.mean(cg_its)) if cg_its else c.cg_maxiter
+            v, used, dt, per_iter = cpu_sample_3d(c, k, ctref_c.default_threads())
+            cpu = {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+                   "sample": f"one forward + one adjoint of the C/OpenMP 3D projector ({dt:.1f} s), extrapolated "
+                             f"to {k:.1f} + 2 pairs per ADMM iteration ({per_iter:.1f} s per iteration)"}
+        except Exception as exc:
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+    launches_per_step = 4 + sum(7 + 6 * k + 1 for k in cg_its) + 5  # as the 2D solver; projector = 2 kernels
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 30-ellipsoid phantom, 1% Gaussian noise)",
+            "config": _config_json_3d(c, "c5"),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(proj.numel() * 4),
+                    "d2h_bytes_per_step": int(x.numel() * 4), "api": "scico_gb300.optimize.ADMM(...).solve()",
+                    "rel_diff_vs_value_path": e2e_diff},
+            "roofline": {"bound": "hbm", "kernel": "ct_proj3d_fwd", "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "algorithmic_bytes": alg, "launch_s": t_fwd, "interactions_per_s": inter / t_fwd},
+            "cpu_baseline": cpu, "clocks": clk.result, "gpu_launches": launches_per_step * args.steps,
+            "cg_steps_per_iteration": cg_its,
+        }), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = _args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "c5":
+        return run_gpu_3d(args)
     return run_gpu(args)
 
 

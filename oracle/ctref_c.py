@@ -38,6 +38,8 @@ def lib():
         _lib.ref_admm_tv.restype = ctypes.c_int
         _lib.ref_set_dot64.argtypes = [ctypes.c_int]
         _lib.ref_set_proj64.argtypes = [ctypes.c_int]
+        _lib.ref_proj3d_fwd.argtypes = [P, P, ctypes.c_int, P, P, P]
+        _lib.ref_proj3d_adj.argtypes = [P, P, ctypes.c_int, P, P, P]
     return _lib
 
 
@@ -88,6 +90,33 @@ class Geometry:
         lib().ref_admm_tv(ctypes.addressof(self.cg), y.ctypes.data, lam, rho, scale, maxiter, cg_maxiter, cg_tol,
                           x.ctypes.data, z.ctypes.data, u.ctypes.data, it.ctypes.data)
         return x, z, u, it
+
+
+class Geometry3D:
+    """XRayTransform3D geometry (float32 (V, 2, 4) matrices) for the C
+    restatement of the 3D projector."""
+
+    def __init__(self, input_shape, matrices, det_shape):
+        self.shape = tuple(int(n) for n in input_shape)
+        self.det = tuple(int(n) for n in det_shape)
+        self.mats = np.ascontiguousarray(matrices, dtype=np.float32).reshape(-1, 2, 4)
+        self.nv = len(self.mats)
+        self._shape = np.asarray(self.shape, dtype=np.int32)
+        self._det = np.asarray(self.det, dtype=np.int32)
+
+    def project(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty((self.nv,) + self.det, dtype=np.float32)
+        lib().ref_proj3d_fwd(self._shape.ctypes.data, self._det.ctypes.data, self.nv, self.mats.ctypes.data,
+                             x.ctypes.data, y.ctypes.data)
+        return y
+
+    def back_project(self, y: np.ndarray) -> np.ndarray:
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        x = np.empty(self.shape, dtype=np.float32)
+        lib().ref_proj3d_adj(self._shape.ctypes.data, self._det.ctypes.data, self.nv, self.mats.ctypes.data,
+                             y.ctypes.data, x.ctypes.data)
+        return x
 
 
 def set_threads(n: int) -> int:
