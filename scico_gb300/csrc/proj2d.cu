@@ -62,17 +62,15 @@ __device__ __forceinline__ ViewParams load_view(const float* __restrict__ views,
   return ViewParams{a.x, a.y, a.z, a.w, b.x};
 }
 
-// Extreme Px over the pixel rectangle [i0, i1] x [j0, j1]: px2d is monotone
-// in i and in j separately (each operation is a monotone rounding), so the
-// extremes are at the corners.
+// Extreme Px over the pixel rectangle [i0, i1] x [j0, j1]: px2d is
+// non-decreasing in i where Pdx0 >= 0 and non-increasing where Pdx0 < 0 (each
+// operation is a monotone rounding), and likewise in j, so the extremes are
+// at the two corners the signs select.
 __device__ __forceinline__ void rect_px(const ViewParams& p, int i0, int i1, int j0, int j1, float& lo,
                                         float& hi) {
-  const float a = ct::px2d(p.pxmin, p.pd0, p.pd1, i0, j0);
-  const float b = ct::px2d(p.pxmin, p.pd0, p.pd1, i1, j0);
-  const float c = ct::px2d(p.pxmin, p.pd0, p.pd1, i0, j1);
-  const float d = ct::px2d(p.pxmin, p.pd0, p.pd1, i1, j1);
-  lo = fminf(fminf(a, b), fminf(c, d));
-  hi = fmaxf(fmaxf(a, b), fmaxf(c, d));
+  const bool ui = p.pd0 >= 0.0f, uj = p.pd1 >= 0.0f;
+  lo = ct::px2d(p.pxmin, p.pd0, p.pd1, ui ? i0 : i1, uj ? j0 : j1);
+  hi = ct::px2d(p.pxmin, p.pd0, p.pd1, ui ? i1 : i0, uj ? j1 : j0);
 }
 
 // key = floor(px) - kbias and w = min(1 - (px - floor(px)), width) * inv_width
@@ -108,6 +106,35 @@ __device__ __forceinline__ float2 ld_shared2(uint32_t addr) {
   return r;
 }
 
+// Paired float32 arithmetic (sm_100+ f32x2): each element is rounded exactly
+// as the scalar operation of the same name.  A paired multiply feeding a
+// paired add is contracted into one fused multiply-add by the assembler even
+// with explicit rounding modifiers (measured: identical to fma.rn.f32x2), so
+// products that must be rounded on their own stay scalar (__fmul_rn).
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long fadd2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long fadd2_rd(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("add.rm.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long fsub2(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // Forward
 // ---------------------------------------------------------------------------
@@ -117,31 +144,47 @@ __device__ __forceinline__ float2 ld_shared2(uint32_t addr) {
 // the pixels with key b-1 followed by the w x of the pixels with key b.
 //
 // walk_row_fast: |Pdx1| < 0.999 and |Px| < 2^21, so consecutive keys differ
-// by 0 or 1 (d).  The carry select is done with exact 0/1 mask products on
-// the FMA pipe: a0 = A (1-d) + B d, b0 = B (1-d).  The partial row is
+// by 0 or 1.  The Px, floor, distance and 1 - w steps of two consecutive
+// pixels run as paired instructions (each element rounded as the scalar
+// step: Px's products stay scalar), then the two pixels enter the carry in
+// walk order: when the key advances, the current bin's sum is complete and
+// the next bin's (1-w) x sum becomes the current one.  The partial row is
 // addressed directly from the float bits of kMagic + key:
 // row_addr = mp_addr - 4 (kMagicBits + base).
 template <bool REV>
 __device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, float pd1, float fj0,
                                               float R, float inv_width) {
+  const unsigned long long R2 = pk2(R, R);
+  const unsigned long long M2 = pk2(kMagic, kMagic), M12 = pk2(kMagic - 1.0f, kMagic - 1.0f);
+  const unsigned long long one2 = pk2(1.0f, 1.0f);
   float A = 0.0f, B = 0.0f;
   int tbp = 0;
-#pragma unroll
-  for (int t = 0; t < kT; ++t) {
-    const int jj = REV ? kT - 1 - t : t;
-    const float px = ct::fadd(R, ct::fmul(pd1, fj0 + (float)jj));
-    int tb;
-    float w;
-    weight_fast(px, inv_width, tb, w);
-    const float omw = ct::fsub(1.0f, w);
-    if (t == 0) tbp = tb;
+  auto step = [&](int tb, float w, float omw, float x, bool first) {
+    if (first) tbp = tb;
     const bool next = tb != tbp;  // the key advanced by one bin
     const float a0 = next ? B : A;
     const float b0 = next ? 0.0f : B;
-    A = fmaf(w, xr[jj], a0);
-    B = fmaf(omw, xr[jj], b0);
+    A = fmaf(w, x, a0);
+    B = fmaf(omw, x, b0);
     tbp = tb;
     st_shared(row_addr + 4u * (uint32_t)tb, A);
+  };
+#pragma unroll
+  for (int t = 0; t < kT; t += 2) {
+    const int ja = REV ? kT - 1 - t : t;
+    const int jb = REV ? kT - 2 - t : t + 1;
+    const unsigned long long px2 =
+        fadd2(R2, pk2(ct::fmul(pd1, fj0 + (float)ja), ct::fmul(pd1, fj0 + (float)jb)));
+    const unsigned long long t2 = fadd2_rd(px2, M2);
+    const unsigned long long d2 = fsub2(fsub2(t2, M12), px2);
+    float ta, tb, da, db;
+    upk2(t2, ta, tb);
+    upk2(d2, da, db);
+    const float wa = __saturatef(ct::fmul(da, inv_width)), wb = __saturatef(ct::fmul(db, inv_width));
+    float oa, ob;
+    upk2(fsub2(one2, pk2(wa, wb)), oa, ob);
+    step(__float_as_int(ta), wa, oa, xr[ja], t == 0);
+    step(__float_as_int(tb), wb, ob, xr[jb], false);
   }
   st_shared(row_addr + 4u * (uint32_t)tbp + 4u, B);
 }
@@ -186,18 +229,32 @@ struct FwdArgs {
   const double* skip;
 };
 
+// Strip bins of one view: base = floor(min Px) and span = the bins the strip
+// can touch, floor(max Px) - base + 2 (both kernels use this).
+__device__ __forceinline__ void strip_bins(const ViewParams& p, int i0, int c0, int& base, int& span) {
+  float lo, hi;
+  rect_px(p, i0, i0 + kT - 1, c0, c0 + kCW - 1, lo, hi);
+  base = (int)floorf(lo);
+  span = (int)floorf(hi) - base + 2;
+}
+
+// Shared memory of k_proj2d_fwd_strips: a 16-B header (the copy barrier),
+// then one region used twice: first the 32 x kRS strip, then, once every lane
+// holds its tile row in registers, the partial rows [kFW][32][LS] and two
+// slot buffers [2][kFW][cspan] (one per view parity).
+__host__ __device__ constexpr size_t fwd_region_floats(int LS, int cspan) {
+  return (size_t)kT * kRS > (size_t)kFW * kT * LS + 2u * kFW * cspan ? (size_t)kT * kRS
+                                                                     : (size_t)kFW * kT * LS + 2u * kFW * cspan;
+}
+
 // grid = (n_strips, view groups, batch), block = 256.
 __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs a) {
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* strip = reinterpret_cast<float*>(smem_raw);                 // [32][kRS]
-  float* part = strip + kT * kRS;                                    // [kFW][32][LS]
-  float* slot = part + kFW * kT * a.LS;                              // [kFW][L]
-  int* sbase = reinterpret_cast<int*>(slot + kFW * a.L);             // [kFW]
-  int* sspan = sbase + kFW;                                          // [kFW]
-  int* scb = sspan + kFW;                                            // strip base of the view
-  uint64_t* bar = reinterpret_cast<uint64_t*>(scb + 1);              // 8-B aligned below
-  bar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(bar) + 7) & ~uintptr_t(7));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  float* strip = reinterpret_cast<float*>(smem_raw + 16);            // [32][kRS]
+  float* part = strip;                                               // [kFW][32][LS]
+  float* slots = part + kFW * kT * a.LS;                             // [2][kFW][cspan]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int s = blockIdx.x;
@@ -235,16 +292,11 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       for (int c = lane; c < kRS; c += 32)
         strip[r * kRS + c] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
   }
-  // zero every partial row once; after each tile the reduction re-zeroes
-  // exactly what the walk wrote, so rows stay zero outside a tile's bins
-  for (int e = tid; e < kFW * kT * a.LS; e += kFW * 32) part[e] = 0.0f;
   __syncthreads();
 
   const int tj = ch * (kCW / kT) + warp;  // this warp's tile column
   const int j0 = tj * kT;
   const bool tile_live = (j0 < a.cols) && (i0 < a.rows);
-  float* wpart = part + warp * kT * a.LS;
-  float* mp = wpart + lane * a.LS;
   const float fi = (float)(i0 + lane);
   const float fj0 = (float)j0;
   const int vbeg = blockIdx.y * a.vpc;
@@ -262,18 +314,40 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       xr[4 * q + 3] = f.w;
     }
   }
+  __syncthreads();  // the strip is dead from here: its bytes become rows and slots
+  {
+    const int nz = kFW * kT * a.LS + 2 * kFW * a.cspan;
+    for (int e = tid; e < nz; e += kFW * 32) part[e] = 0.0f;
+  }
+  __syncthreads();
 
+  float* wpart = part + warp * kT * a.LS;
+  float* mp = wpart + lane * a.LS;
+  // Slot rows hold each tile's bins at strip-relative offsets and zeros
+  // elsewhere, so the tile combine needs no range checks.  A warp clears what
+  // it wrote into a slot buffer when it reuses that buffer two views later
+  // (after the barrier that ends the combine reading it).
+  int zoff0 = 0, zspan0 = 0, zoff1 = 0, zspan1 = 0;
   for (int v = vbeg; v < vend; ++v) {
+    const int par = (v - vbeg) & 1;
     const ViewParams p = load_view(a.views, v);
+    int cb, ssp;
+    strip_bins(p, i0, c0, cb, ssp);
+    float* slot = slots + (par * kFW + warp) * a.cspan;
+    {
+      const int zo = par ? zoff1 : zoff0, zs = par ? zspan1 : zspan0;
+      for (int k = lane; k < zs; k += 32) slot[zo + k] = 0.0f;
+    }
     // ---- this warp's tile --------------------------------------------------
-    int base = 0, span = 0;
+    int off = 0, span = 0;
     if (tile_live) {
       float lo, hi;
       rect_px(p, i0, i0 + kT - 1, j0, j0 + kT - 1, lo, hi);
-      base = (int)floorf(lo);
+      const int base = (int)floorf(lo);
       span = (int)floorf(hi) - base + 2;
+      off = base - cb;
       const bool fast = fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit && fabsf(p.pd1) < 0.999f;
-      if (span > a.L) {  // cannot happen for a table from ct_proj2d_views
+      if (span > a.L || off < 0 || off + span > a.cspan) {  // cannot happen for a table from ct_proj2d_views
         if (lane == 0) atomicOr(a.errflag, 1);
         span = 0;
       } else {
@@ -300,51 +374,48 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
             acc += q[r * a.LS];
             q[r * a.LS] = 0.0f;
           }
-          slot[warp * a.L + k] = acc;
+          slot[off + k] = acc;
         }
       }
     }
-    if (lane == 0) {
-      sbase[warp] = base;
-      sspan[warp] = span;
-    }
-    if (tid == 32) {
-      float lo, hi;
-      rect_px(p, i0, i0 + kT - 1, c0, c0 + kCW - 1, lo, hi);
-      *scb = (int)floorf(lo);
+    if (par) {
+      zoff1 = off;
+      zspan1 = span;
+    } else {
+      zoff0 = off;
+      zspan0 = span;
     }
     __syncthreads();
     // ---- combine the 8 tiles in tile order into the strip's bins ----------
-    const int cb = *scb;
+    const float* s0 = slots + par * kFW * a.cspan;
     float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + v) * a.cspan;
-    for (int k = tid; k < a.cspan; k += kFW * 32) {
-      float acc = 0.0f;
+    const int n = min(ssp, a.cspan);
+    for (int k = tid; k < n; k += kFW * 32) {
+      float acc = s0[k];
 #pragma unroll
-      for (int w = 0; w < kFW; ++w) {
-        const int off = cb + k - sbase[w];
-        if ((unsigned)off < (unsigned)sspan[w]) acc += slot[w * a.L + off];
-      }
+      for (int w = 1; w < kFW; ++w) acc += s0[w * a.cspan + k];
       po[k] = acc;
     }
-    __syncthreads();
   }
 }
 
 // sino[b, v, bin] = sum over strips (strip order) of the strip bins covering
-// bin.  grid = (n_views, batch), block = 256, dynamic smem = n_strips ints.
+// bin.  grid = (n_views, batch), block = 256, dynamic smem = 2 n_strips ints.
 __global__ void __launch_bounds__(256)
     k_proj2d_fwd_gather(const float* __restrict__ part, float* __restrict__ sino,
                         const float* __restrict__ views, int nv, int det, int cspan, int n_chunks,
                         int n_strips, const double* __restrict__ skip) {
   if (skip && *skip != 0.0) return;
   extern __shared__ int sb[];
+  int* ss = sb + n_strips;
   const int v = blockIdx.x, b = blockIdx.y;
   const ViewParams p = load_view(views, v);
   for (int s = threadIdx.x; s < n_strips; s += blockDim.x) {
     const int ti = s / n_chunks, ch = s - ti * n_chunks;
-    float lo, hi;
-    rect_px(p, ti * kT, ti * kT + kT - 1, ch * kCW, ch * kCW + kCW - 1, lo, hi);
-    sb[s] = (int)floorf(lo);
+    int base, span;
+    strip_bins(p, ti * kT, ch * kCW, base, span);
+    sb[s] = base;
+    ss[s] = min(span, cspan);
   }
   __syncthreads();
   const float* pb = part + ((size_t)b * n_strips * nv + v) * cspan;
@@ -355,9 +426,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll 8
     for (int s = 0; s < n_strips; ++s) {
       const int off = bin - sb[s];
-      const bool in = (unsigned)off < (unsigned)cspan;
-      const float v = __ldg(pb + s * sstride + (in ? off : 0));
-      acc += in ? v : 0.0f;
+      if ((unsigned)off < (unsigned)ss[s]) acc += __ldg(pb + s * sstride + off);
     }
     out[bin] = acc;
   }
@@ -382,35 +451,6 @@ struct AdjArgs {
 // One view's contribution to this thread's pixels.  Fast path: the window
 // pair of key k lives at shared address off + 8 (kMagicBits + k) for the
 // float bits kMagicBits + k of kMagic + k.
-
-// Paired float32 arithmetic (sm_100+ f32x2): each element is rounded exactly
-// as the scalar operation of the same name.  A paired multiply feeding a
-// paired add is contracted into one fused multiply-add by the assembler even
-// with explicit rounding modifiers (measured: identical to fma.rn.f32x2), so
-// products that must be rounded on their own stay scalar (__fmul_rn).
-__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void upk2(unsigned long long v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long fadd2(unsigned long long a, unsigned long long b) {
-  unsigned long long r;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ unsigned long long fadd2_rd(unsigned long long a, unsigned long long b) {
-  unsigned long long r;
-  asm("add.rm.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ unsigned long long fsub2(unsigned long long a, unsigned long long b) {
-  unsigned long long r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
 
 // adj_view_fast with the Px, floor and distance steps of two pixels per
 // paired instruction (bit-identical to the scalar form).
@@ -558,10 +598,7 @@ int* errflag_ptr() {
   return cached[dev];
 }
 
-size_t fwd_smem_bytes(int L, int LS) {
-  return sizeof(float) * ((size_t)kT * kRS + (size_t)kFW * kT * LS + (size_t)kFW * L) +
-         sizeof(int) * (2 * kFW + 1) + 24;
-}
+size_t fwd_smem_bytes(int LS, int cspan) { return 16 + sizeof(float) * fwd_region_floats(LS, cspan); }
 
 size_t adj_smem_bytes(int W) {
   return sizeof(float2) * (size_t)kAVC * W + sizeof(float4) * kAVC + sizeof(float) * kAVC +
@@ -587,7 +624,7 @@ ct_status proj2d_check(const ct_geom2d* g, const char* who) {
   const Proj2dPlan p = proj2d_plan(g, 1);
   if (p.fwd_smem > 200 * 1024 || p.adj_smem > 200 * 1024)
     return fail(CT_ERR_UNSUPPORTED, "%s: tile spans of %d / %d bins too large", who, p.L, p.W);
-  if ((size_t)p.n_strips * sizeof(int) > 48 * 1024)
+  if (2 * (size_t)p.n_strips * sizeof(int) > 48 * 1024)
     return fail(CT_ERR_UNSUPPORTED, "%s: %d image strips too many", who, p.n_strips);
   return CT_OK;
 }
@@ -608,7 +645,7 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   p.vpc = (int)std::min<long>(16, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
   p.fwd_groups = (g->n_views + p.vpc - 1) / p.vpc;
   p.fwd_bytes = round_up((size_t)batch * p.n_strips * g->n_views * p.cspan * sizeof(float), 256);
-  p.fwd_smem = fwd_smem_bytes(p.L, p.LS);
+  p.fwd_smem = fwd_smem_bytes(p.LS, p.cspan);
   p.W = (int)floorf((float)(kAJ - 1) * mw + 1.01f) + 3;
   p.adj_smem = adj_smem_bytes(p.W);
   p.adj_gx = (g->cols + kAJ - 1) / kAJ;
@@ -659,7 +696,7 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   ct_status st = launch_check("k_proj2d_fwd_strips");
   if (st != CT_OK) return st;
   dim3 g2(g->n_views, batch);
-  k_proj2d_fwd_gather<<<g2, 256, (size_t)p.n_strips * sizeof(int), s>>>(
+  k_proj2d_fwd_gather<<<g2, 256, 2 * (size_t)p.n_strips * sizeof(int), s>>>(
       part, sino, g->views, g->n_views, g->det_count, p.cspan, p.n_chunks, p.n_strips, skip);
   return launch_check("k_proj2d_fwd_gather");
 }
