@@ -40,6 +40,8 @@ constexpr int kCW = 256;        // forward strip width (8 tiles)
 constexpr int kFW = 8;          // warps of a forward CTA (one tile each)
 constexpr int kRS = kCW + 4;    // strip row stride in floats: 16-B rows, conflict-free LDS.128
 constexpr int kFwdTargetCtas = 1824;
+constexpr int kLSDefault = 35;  // partial-row stride when projected pixels are at most one bin wide
+constexpr int kGL = 8;          // strips read per round by a forward gather warp
 constexpr int kAI = 16;         // adjoint tile rows
 constexpr int kAJ = 64;         // adjoint tile columns
 constexpr int kAPX = 4;         // pixels per adjoint thread
@@ -247,14 +249,18 @@ __host__ __device__ constexpr size_t fwd_region_floats(int LS, int cspan) {
                                                                      : (size_t)kFW * kT * LS + 2u * kFW * cspan;
 }
 
-// grid = (n_strips, view groups, batch), block = 256.
+// grid = (n_strips, view groups, batch), block = 256.  LSC: the partial-row
+// stride as a compile-time constant (its default-geometry value, so the row
+// sums address with immediates), or 0 for a.LS.
+template <int LSC>
 __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs a) {
+  const int LS = LSC ? LSC : a.LS;
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* strip = reinterpret_cast<float*>(smem_raw + 16);            // [32][kRS]
   float* part = strip;                                               // [kFW][32][LS]
-  float* slots = part + kFW * kT * a.LS;                             // [2][kFW][cspan]
+  float* slots = part + kFW * kT * LS;                             // [2][kFW][cspan]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int s = blockIdx.x;
@@ -316,13 +322,13 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   }
   __syncthreads();  // the strip is dead from here: its bytes become rows and slots
   {
-    const int nz = kFW * kT * a.LS + 2 * kFW * a.cspan;
+    const int nz = kFW * kT * LS + 2 * kFW * a.cspan;
     for (int e = tid; e < nz; e += kFW * 32) part[e] = 0.0f;
   }
   __syncthreads();
 
-  float* wpart = part + warp * kT * a.LS;
-  float* mp = wpart + lane * a.LS;
+  float* wpart = part + warp * kT * LS;
+  float* mp = wpart + lane * LS;
   // Slot rows hold each tile's bins at strip-relative offsets and zeros
   // elsewhere, so the tile combine needs no range checks.  A warp clears what
   // it wrote into a slot buffer when it reuses that buffer two views later
@@ -369,10 +375,10 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
         for (int k = lane; k < span; k += 32) {
           float acc = 0.0f;
           float* q = wpart + k;
-#pragma unroll 8
+#pragma unroll
           for (int r = 0; r < kT; ++r) {
-            acc += q[r * a.LS];
-            q[r * a.LS] = 0.0f;
+            acc += q[r * LS];
+            q[r * LS] = 0.0f;
           }
           slot[off + k] = acc;
         }
@@ -400,36 +406,53 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
 }
 
 // sino[b, v, bin] = sum over strips (strip order) of the strip bins covering
-// bin.  grid = (n_views, batch), block = 256, dynamic smem = 2 n_strips ints.
+// bin.  A warp takes 32 consecutive bins of one view: its lanes compute the
+// strips' bin ranges (lane = strip), a ballot lists the strips that meet the
+// warp's bins, and the listed strips are read kGL at a time (loads first,
+// then the sums in strip order, zero where a strip misses the bin).
+// grid = (n_views, ceil(det / 256), batch), block = 256.
 __global__ void __launch_bounds__(256)
     k_proj2d_fwd_gather(const float* __restrict__ part, float* __restrict__ sino,
                         const float* __restrict__ views, int nv, int det, int cspan, int n_chunks,
                         int n_strips, const double* __restrict__ skip) {
   if (skip && *skip != 0.0) return;
-  extern __shared__ int sb[];
-  int* ss = sb + n_strips;
-  const int v = blockIdx.x, b = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int v = blockIdx.x, b = blockIdx.z;
+  const int k0 = blockIdx.y * 256 + warp * 32;
+  if (k0 >= det) return;  // whole warp
   const ViewParams p = load_view(views, v);
-  for (int s = threadIdx.x; s < n_strips; s += blockDim.x) {
-    const int ti = s / n_chunks, ch = s - ti * n_chunks;
-    int base, span;
-    strip_bins(p, ti * kT, ch * kCW, base, span);
-    sb[s] = base;
-    ss[s] = min(span, cspan);
-  }
-  __syncthreads();
+  const int bin = k0 + lane;
   const float* pb = part + ((size_t)b * n_strips * nv + v) * cspan;
   const size_t sstride = (size_t)nv * cspan;
-  float* out = sino + ((size_t)b * nv + v) * det;
-  for (int bin = threadIdx.x; bin < det; bin += blockDim.x) {
-    float acc = 0.0f;
-#pragma unroll 8
-    for (int s = 0; s < n_strips; ++s) {
-      const int off = bin - sb[s];
-      if ((unsigned)off < (unsigned)ss[s]) acc += __ldg(pb + s * sstride + off);
+  float acc = 0.0f;
+  for (int c = 0; c < n_strips; c += 32) {
+    const int s = c + lane;
+    int base = 0, span = 0;
+    if (s < n_strips) {
+      const int ti = s / n_chunks, ch = s - ti * n_chunks;
+      strip_bins(p, ti * kT, ch * kCW, base, span);
+      span = min(span, cspan);
     }
-    out[bin] = acc;
+    unsigned mask = __ballot_sync(0xffffffffu, s < n_strips && base < k0 + 32 && base + span > k0);
+    while (mask) {
+      float val[kGL];
+#pragma unroll
+      for (int u = 0; u < kGL; ++u) {
+        val[u] = 0.0f;
+        if (mask) {
+          const int sl = __ffs(mask) - 1;
+          mask &= mask - 1u;
+          const int bs = __shfl_sync(0xffffffffu, base, sl);
+          const int sp = __shfl_sync(0xffffffffu, span, sl);
+          const int off = bin - bs;
+          if ((unsigned)off < (unsigned)sp) val[u] = __ldg(pb + (size_t)(c + sl) * sstride + off);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kGL; ++u) acc += val[u];
+    }
   }
+  if (bin < det) sino[((size_t)b * nv + v) * det + bin] = acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -624,8 +647,6 @@ ct_status proj2d_check(const ct_geom2d* g, const char* who) {
   const Proj2dPlan p = proj2d_plan(g, 1);
   if (p.fwd_smem > 200 * 1024 || p.adj_smem > 200 * 1024)
     return fail(CT_ERR_UNSUPPORTED, "%s: tile spans of %d / %d bins too large", who, p.L, p.W);
-  if (2 * (size_t)p.n_strips * sizeof(int) > 48 * 1024)
-    return fail(CT_ERR_UNSUPPORTED, "%s: %d image strips too many", who, p.n_strips);
   return CT_OK;
 }
 
@@ -663,10 +684,14 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
 
 ct_status proj2d_prepare(const Proj2dPlan& p) {
   if (!errflag_ptr()) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
-  ct_status st = cuda_check(cudaFuncSetAttribute(k_proj2d_fwd_strips,
+  ct_status st = cuda_check(cudaFuncSetAttribute(k_proj2d_fwd_strips<kLSDefault>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)p.fwd_smem),
                             "fwd smem attribute");
+  if (st != CT_OK) return st;
+  st = cuda_check(cudaFuncSetAttribute(k_proj2d_fwd_strips<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)p.fwd_smem),
+                  "fwd smem attribute");
   if (st != CT_OK) return st;
   return cuda_check(cudaFuncSetAttribute(k_proj2d_adj, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)p.adj_smem),
@@ -692,11 +717,14 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   a.skip = skip;
   if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
   dim3 g1(p.n_strips, p.fwd_groups, batch);
-  k_proj2d_fwd_strips<<<g1, kFW * 32, p.fwd_smem, s>>>(a);
+  if (p.LS == kLSDefault)
+    k_proj2d_fwd_strips<kLSDefault><<<g1, kFW * 32, p.fwd_smem, s>>>(a);
+  else
+    k_proj2d_fwd_strips<0><<<g1, kFW * 32, p.fwd_smem, s>>>(a);
   ct_status st = launch_check("k_proj2d_fwd_strips");
   if (st != CT_OK) return st;
-  dim3 g2(g->n_views, batch);
-  k_proj2d_fwd_gather<<<g2, 256, 2 * (size_t)p.n_strips * sizeof(int), s>>>(
+  dim3 g2(g->n_views, (g->det_count + 255) / 256, batch);
+  k_proj2d_fwd_gather<<<g2, 256, 0, s>>>(
       part, sino, g->views, g->n_views, g->det_count, p.cspan, p.n_chunks, p.n_strips, skip);
   return launch_check("k_proj2d_fwd_gather");
 }
