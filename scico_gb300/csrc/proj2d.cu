@@ -150,14 +150,17 @@ __device__ __forceinline__ unsigned long long fsub2(unsigned long long a, unsign
 // pixels run as paired instructions (each element rounded as the scalar
 // step: Px's products stay scalar), then the two pixels enter the carry in
 // walk order: when the key advances, the current bin's sum is complete and
-// the next bin's (1-w) x sum becomes the current one.  The partial row is
-// addressed directly from the float bits of kMagic + key:
-// row_addr = mp_addr - 4 (kMagicBits + base).
+// the next bin's (1-w) x sum becomes the current one.  The floor uses the
+// lane's own magic number kMagic + lane LS (an integer below 2^24, so
+// t = magic + floor(px) is still exact), which makes the float bits of t the
+// lane's partial-row index plus a constant: the store address is
+// row_addr + 4 bits(t) with row_addr = warp_rows_addr - 4 (kMagicBits + base),
+// the same for every lane of the warp.
 template <bool REV>
-__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, float pd1, float fj0,
-                                              float R, float inv_width) {
+__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, float magic, float pd1,
+                                              float fj0, float R, float inv_width) {
   const unsigned long long R2 = pk2(R, R);
-  const unsigned long long M2 = pk2(kMagic, kMagic), M12 = pk2(kMagic - 1.0f, kMagic - 1.0f);
+  const unsigned long long M2 = pk2(magic, magic), M12 = pk2(magic - 1.0f, magic - 1.0f);
   const unsigned long long one2 = pk2(1.0f, 1.0f);
   float A = 0.0f, B = 0.0f;
   int tbp = 0;
@@ -329,6 +332,7 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
 
   float* wpart = part + warp * kT * LS;
   float* mp = wpart + lane * LS;
+  const float magic = kMagic + (float)(lane * LS);  // exact: an integer below 2^24
   // Slot rows hold each tile's bins at strip-relative offsets and zeros
   // elsewhere, so the tile combine needs no range checks.  A warp clears what
   // it wrote into a slot buffer when it reuses that buffer two views later
@@ -359,11 +363,11 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       } else {
         const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, fi));
         if (fast) {
-          const uint32_t row_addr = ct::smem_u32(mp) - 4u * (uint32_t)(kMagicBits + base);
+          const uint32_t row_addr = ct::smem_u32(wpart) - 4u * (uint32_t)(kMagicBits + base);
           if (p.pd1 >= 0.0f)
-            walk_row_fast<false>(xr, row_addr, p.pd1, fj0, R, p.inv_width);
+            walk_row_fast<false>(xr, row_addr, magic, p.pd1, fj0, R, p.inv_width);
           else
-            walk_row_fast<true>(xr, row_addr, p.pd1, fj0, R, p.inv_width);
+            walk_row_fast<true>(xr, row_addr, magic, p.pd1, fj0, R, p.inv_width);
         } else {
           if (p.pd1 >= 0.0f)
             walk_row_gen<false>(xr, mp, p, R, fj0, base);
@@ -371,16 +375,44 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
             walk_row_gen<true>(xr, mp, p, R, fj0, base);
         }
         __syncwarp();
-        // rows summed in row order; the read entries are zeroed again
-        for (int k = lane; k < span; k += 32) {
+        // Bins 0..31 of the tile: lane = bin, rows summed in row order; the
+        // read entries are zeroed again.
+        if (lane < span) {
           float acc = 0.0f;
-          float* q = wpart + k;
+          float* q = wpart + lane;
 #pragma unroll
           for (int r = 0; r < kT; ++r) {
             acc += q[r * LS];
             q[r * LS] = 0.0f;
           }
-          slot[off + k] = acc;
+          slot[off + lane] = acc;
+        }
+        if (span > 32) {
+          if (LSC != 0 && LSC - 32 <= 3) {
+            // at most 3 more bins: lane = row, then a fixed butterfly over rows
+            float* q = mp + 32;
+#pragma unroll
+            for (int e = 0; e < (LSC != 0 ? LSC - 32 : 1); ++e) {
+              if (32 + e < span) {  // warp-uniform
+                float t = q[e];
+                q[e] = 0.0f;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
+                if (lane == 0) slot[off + 32 + e] = t;
+              }
+            }
+          } else {
+            for (int k = 32 + lane; k < span; k += 32) {
+              float acc = 0.0f;
+              float* q = wpart + k;
+#pragma unroll 8
+              for (int r = 0; r < kT; ++r) {
+                acc += q[r * LS];
+                q[r * LS] = 0.0f;
+              }
+              slot[off + k] = acc;
+            }
+          }
         }
       }
     }
