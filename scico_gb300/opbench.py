@@ -23,7 +23,8 @@ import statistics
 
 import torch
 
-from . import _device, _lib, linop, workloads
+from . import _device, _lib, functional, linop, loss, workloads
+from .optimize import ADMM, LinearSubproblemSolver
 
 
 def main(argv=None):
@@ -35,6 +36,9 @@ def main(argv=None):
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
     ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
     ap.add_argument("--streams", type=int, default=0, help="c3: internal streams of the batch solve (0 = auto)")
+    ap.add_argument("--plain", action="store_true",
+                    help="c3: also time the per-scan loops without graphs (fused solver with plain launches, "
+                         "and scico_gb300.optimize.ADMM on the drop-in operators)")
     ap.add_argument("--general", action="store_true",
                     help="proj3d: run the GENERAL kernels on the workload's geometry")
     ap.add_argument("--reps", type=int, default=20)
@@ -267,9 +271,30 @@ def _c3(a, dev):
     tb, _ = _time(batched, s, a.warmup, a.reps)
     tl, _ = _time(looped, s, a.warmup, a.reps)
     inter = sum(c.n * c.n * c.n_views for c in cfgs)
-    print(json.dumps({"op": "c3", "scans": n, "iters": a.iters, "streams": a.streams, "batched_s": tb,
-                      "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb,
-                      "interactions_per_application": inter}))
+    out = {"op": "c3", "scans": n, "iters": a.iters, "streams": a.streams, "batched_s": tb,
+           "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb, "interactions_per_application": inter}
+    if a.plain:
+        # the fused per-scan solver with every launch issued from the host
+        for d in descs:
+            d.use_graph = 0
+        tn, _ = _time(looped, s, 1, max(1, a.reps // 2))
+        for d in descs:
+            d.use_graph = 1
+
+        # the plain drop-in: scico's ADMM loop on the GPU operators, one scan
+        # after another (CG convergence tested on the host every step)
+        def generic():
+            for k, c in enumerate(cfgs):
+                f = loss.SquaredL2Loss(y=ys[k], A=keep[k])
+                C = linop.FiniteDifference((c.n, c.n), append=0)
+                ADMM(f=f, g_list=[c.lam * functional.L21Norm()], C_list=[C], rho_list=[c.rho], maxiter=a.iters,
+                     subproblem_solver=LinearSubproblemSolver(cg_kwargs={"tol": c.cg_tol, "maxiter": c.cg_maxiter}),
+                     fused=False).solve()
+
+        tg, _ = _time(generic, s, 0, 1)
+        out.update({"looped_plain_launch_s": tn, "speedup_vs_plain_launch": tn / tb,
+                    "looped_generic_s": tg, "speedup_vs_generic": tg / tb})
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":
