@@ -271,8 +271,17 @@ def _c3(a, dev):
     tb, _ = _time(batched, s, a.warmup, a.reps)
     tl, _ = _time(looped, s, a.warmup, a.reps)
     inter = sum(c.n * c.n * c.n_views for c in cfgs)
+    batched()
+    torch.cuda.synchronize()
+    cg = torch.stack([t[:, _lib.CT_ITSTAT_CG_ITERS] for t in its]).cpu()
+    # projector work actually run: one forward/adjoint pair per CG step plus
+    # the pair of each iteration's start (A x, A^T A x), skipped only when x
+    # did not change
+    pairs = sum(float(cg[k].sum() + a.iters) * cfgs[k].n ** 2 * cfgs[k].n_views for k in range(n))
     out = {"op": "c3", "scans": n, "iters": a.iters, "streams": a.streams, "batched_s": tb,
-           "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb, "interactions_per_application": inter}
+           "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb, "interactions_per_application": inter,
+           "mean_cg_iters": float(cg.mean()),
+           "projection_pair_interactions": pairs}
     if a.plain:
         # the fused per-scan solver with every launch issued from the host
         for d in descs:
