@@ -46,7 +46,7 @@ constexpr int kAI = 16;         // adjoint tile rows
 constexpr int kAJ = 64;         // adjoint tile columns
 constexpr int kAPX = 4;         // pixels per adjoint thread
 constexpr int kAVC = 32;        // views staged per adjoint run
-constexpr int kAdjTargetCtas = 304;
+constexpr int kAdjTargetCtas = 1216;  // 152 SMs x 8: view splits until the CTAs balance over the SMs
 constexpr int kAdjMinViewsPerSplit = 16;
 constexpr uint32_t kMaxPolls = 1u << 24;
 
