@@ -151,10 +151,165 @@ __device__ __forceinline__ void d_at(const float* __restrict__ x, const int (&c)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Quad path: a thread takes four consecutive elements e0..e0+3 along the
+// last axis (used when n[ND-1] % 4 == 0 and every array is 16-B aligned, so
+// the quad shares its row and each axis' neighbours are quads too).  The
+// per-element arithmetic is the scalar code's, in the same order; only the
+// loads are 128-bit.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float4 ld4(const float* __restrict__ p, size_t e) {
+  return *reinterpret_cast<const float4*>(p + e);
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, size_t e, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p + e) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void unpack4(const float4 a, float (&v)[4]) {
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+}
+
+// dT_at for the quad at e0 (coordinates c of e0).
+template <int ND>
+__device__ __forceinline__ void dT_at4(const float* __restrict__ a, const float* __restrict__ b,
+                                       const int (&c)[ND], size_t e0, const Shape3& sh, size_t N,
+                                       float (&tot)[4]) {
+  auto f4 = [&](int comp, size_t idx, float (&v)[4]) {
+    unpack4(ld4(a + comp * N, idx), v);
+    if (b) {
+      float w[4];
+      unpack4(ld4(b + comp * N, idx), w);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = ct::fsub(v[j], w[j]);
+    }
+  };
+  auto f1 = [&](int comp, size_t idx) -> float {
+    const float av = a[comp * N + idx];
+    return b ? ct::fsub(av, b[comp * N + idx]) : av;
+  };
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    float fc[4], lo[4], hi[4];
+    f4(k, e0, fc);
+    if (k < ND - 1) {
+      const size_t st = axis_stride<ND>(sh, k);
+      if (c[k] >= 1) {
+        f4(k, e0 - st, lo);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) lo[j] = 0.0f;
+      }
+      const bool h = c[k] <= sh.n[k] - 2;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) hi[j] = h ? fc[j] : 0.0f;
+    } else {
+      const int cl = c[ND - 1], nl = sh.n[ND - 1];
+      lo[0] = cl >= 1 ? f1(k, e0 - 1) : 0.0f;
+      lo[1] = fc[0];
+      lo[2] = fc[1];
+      lo[3] = fc[2];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) hi[j] = cl + j <= nl - 2 ? fc[j] : 0.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float term = ct::fsub(lo[j], hi[j]);
+      tot[j] = k == 0 ? term : ct::fadd(tot[j], term);
+    }
+  }
+}
+
+// dtd_at for the quad at e0; qc = q at e0..e0+3.
+template <int ND>
+__device__ __forceinline__ void dtd_at4(const float* __restrict__ q, const float (&qc)[4], const int (&c)[ND],
+                                        size_t e0, const Shape3& sh, float (&tot)[4]) {
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    float lo[4], hi[4];
+    if (k < ND - 1) {
+      const size_t st = axis_stride<ND>(sh, k);
+      float ql[4], qh[4];
+      const bool hl = c[k] >= 1, hh = c[k] <= sh.n[k] - 2;
+      if (hl) unpack4(ld4(q, e0 - st), ql);
+      if (hh) unpack4(ld4(q, e0 + st), qh);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        lo[j] = hl ? ct::fsub(qc[j], ql[j]) : 0.0f;
+        hi[j] = hh ? ct::fsub(qh[j], qc[j]) : 0.0f;
+      }
+    } else {
+      const int cl = c[ND - 1], nl = sh.n[ND - 1];
+      const float qm = cl >= 1 ? q[e0 - 1] : 0.0f;
+      const float qp = cl + 3 <= nl - 2 ? q[e0 + 4] : 0.0f;
+      const float prev[4] = {qm, qc[0], qc[1], qc[2]};
+      const float next[4] = {qc[1], qc[2], qc[3], qp};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        lo[j] = cl + j >= 1 ? ct::fsub(qc[j], prev[j]) : 0.0f;
+        hi[j] = cl + j <= nl - 2 ? ct::fsub(next[j], qc[j]) : 0.0f;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float term = ct::fsub(lo[j], hi[j]);
+      tot[j] = k == 0 ? term : ct::fadd(tot[j], term);
+    }
+  }
+}
+
+// d_at for the quad at e0; xc = x at e0..e0+3.
+template <int ND>
+__device__ __forceinline__ void d_at4(const float* __restrict__ x, const float (&xc)[4], const int (&c)[ND],
+                                      size_t e0, const Shape3& sh, float (&d)[ND][4]) {
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    float nx[4];
+    if (k < ND - 1) {
+      const size_t st = axis_stride<ND>(sh, k);
+      if (c[k] <= sh.n[k] - 2) {
+        unpack4(ld4(x, e0 + st), nx);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) nx[j] = xc[j];
+      }
+    } else {
+      const int cl = c[ND - 1], nl = sh.n[ND - 1];
+      nx[0] = xc[1];
+      nx[1] = xc[2];
+      nx[2] = xc[3];
+      nx[3] = cl + 3 <= nl - 2 ? x[e0 + 4] : xc[3];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) d[k][j] = ct::fsub(nx[j], xc[j]);
+  }
+}
+
 template <int ND>
 __global__ void __launch_bounds__(NT) k_init_state(const float* __restrict__ x, float* __restrict__ z,
                                                    float* __restrict__ u, float* __restrict__ dz,
-                                                   Shape3 sh, size_t N, int ng) {
+                                                   Shape3 sh, size_t N, int ng, int vec) {
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e0, sh, c);
+      float xc[4], d[ND][4];
+      unpack4(ld4(x, e0), xc);
+      d_at4<ND>(x, xc, c, e0, sh, d);
+      const float zero[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int t = 0; t < ng; ++t) {
+        const size_t o = (size_t)t * ND * N;
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+          st4(z + o + k * N, e0, d[k]);
+          st4(u + o + k * N, e0, zero);
+          st4(dz + o + k * N, e0, zero);
+        }
+      }
+    }
+    return;
+  }
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     int c[ND];
     coords<ND>(e, sh, c);
@@ -174,7 +329,19 @@ __global__ void __launch_bounds__(NT) k_init_state(const float* __restrict__ x, 
 
 // out = c * (sum of the adjoint split partials), plain (used once for A^T y).
 __global__ void __launch_bounds__(NT) k_scale_splits(const float* __restrict__ src, float* __restrict__ out,
-                                                     size_t n, int nsplit, float c) {
+                                                     size_t n, int nsplit, float c, int vec) {
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < n; e0 += 4 * (size_t)gridDim.x * NT) {
+      float4 a = ld4(src, e0);
+      for (int k = 1; k < nsplit; ++k) {
+        const float4 w = ld4(src + (size_t)k * n, e0);
+        a = make_float4(ct::fadd(a.x, w.x), ct::fadd(a.y, w.y), ct::fadd(a.z, w.z), ct::fadd(a.w, w.w));
+      }
+      *reinterpret_cast<float4*>(out + e0) =
+          make_float4(ct::fmul(c, a.x), ct::fmul(c, a.y), ct::fmul(c, a.z), ct::fmul(c, a.w));
+    }
+    return;
+  }
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
     float s = src[e];
     for (int k = 1; k < nsplit; ++k) s = ct::fadd(s, src[(size_t)k * n + e]);
@@ -186,8 +353,32 @@ template <int ND>
 __global__ void __launch_bounds__(NT)
     k_rhs(const float* __restrict__ atyc, const float* __restrict__ z, const float* __restrict__ u,
           const float* __restrict__ dz, float* __restrict__ rhs, Shape3 sh, size_t N, TermParams tp,
-          double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+          double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
+          int vec) {
   double acc[1] = {0.0};
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e0, sh, c);
+      float val[4], dv[4];
+      unpack4(ld4(atyc, e0), val);
+      for (int t = 0; t < tp.ng; ++t) {
+        const size_t o = (size_t)t * ND * N;
+        float g[4], h[4];
+        dT_at4<ND>(z + o, u + o, c, e0, sh, N, g);
+        dT_at4<ND>(dz + o, nullptr, c, e0, sh, N, h);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          val[j] = ct::fadd(val[j], ct::fmul(tp.rho, g[j]));
+          const float w = ct::fmul(tp.rho, h[j]);
+          dv[j] = (t == 0) ? w : ct::fadd(dv[j], w);
+        }
+      }
+      st4(rhs, e0, val);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[0] += (double)dv[j] * (double)dv[j];
+    }
+  } else {
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     int c[ND];
     coords<ND>(e, sh, c);
@@ -202,18 +393,47 @@ __global__ void __launch_bounds__(NT)
     rhs[e] = val;
     acc[0] += (double)dv * (double)dv;
   }
+  }
   double tot[1];
   if (ct::grid_sumk_last<NT, 1>(acc, partials, ticket, tot)) slots[S_DUAL2] = tot[0];
 }
 
 __global__ void __launch_bounds__(NT)
     k_resid2(const float* __restrict__ sino, const float* __restrict__ y, size_t n,
-             double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+             double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
+             int vec) {
   if (slots[S_XCLEAN] != 0.0) return;  // x unchanged: S_RESID2 is current
   double acc[1] = {0.0};
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-    const float d = ct::fsub(y[e], sino[e]);
-    acc[0] += (double)d * (double)d;
+  if (vec) {
+    // two quads per step for more loads in flight
+    const size_t stride = 4 * (size_t)gridDim.x * NT;
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < n; e0 += 2 * stride) {
+      const bool two = e0 + stride < n;
+      float a[4], b[4], a2[4], b2[4];
+      unpack4(ld4(y, e0), a);
+      unpack4(ld4(sino, e0), b);
+      if (two) {
+        unpack4(ld4(y, e0 + stride), a2);
+        unpack4(ld4(sino, e0 + stride), b2);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float d = ct::fsub(a[j], b[j]);
+        acc[0] += (double)d * (double)d;
+      }
+      if (two) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float d = ct::fsub(a2[j], b2[j]);
+          acc[0] += (double)d * (double)d;
+        }
+      }
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+      const float d = ct::fsub(y[e], sino[e]);
+      acc[0] += (double)d * (double)d;
+    }
   }
   double tot[1];
   if (ct::grid_sumk_last<NT, 1>(acc, partials, ticket, tot)) slots[S_RESID2] = tot[0];
@@ -254,10 +474,55 @@ __global__ void __launch_bounds__(NT)
                  float* __restrict__ p, float* __restrict__ lhsx, double* __restrict__ slots,
                  double* __restrict__ cg, double tol, double atol, int maxiter,
                  double* __restrict__ partials, unsigned int* __restrict__ ticket,
-                 cudaGraphConditionalHandle cond, int use_cond) {
+                 cudaGraphConditionalHandle cond, int use_cond, int vec) {
   if (!INIT && cg[CT_CG_DONE] != 0.0) return;
   const bool cached = INIT && slots[S_XCLEAN] != 0.0;
   double acc[2] = {0.0, 0.0};
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      float v[4], qc[4];
+      if (!INIT || !cached) unpack4(ld4(q, e0), qc);
+      if (cached) {
+        unpack4(ld4(lhsx, e0), v);
+      } else {
+        float4 a4 = ld4(adj, e0);
+        for (int k = 1; k < nsplit; ++k) {
+          const float4 w = ld4(adj + (size_t)k * N, e0);
+          a4 = make_float4(ct::fadd(a4.x, w.x), ct::fadd(a4.y, w.y), ct::fadd(a4.z, w.z), ct::fadd(a4.w, w.w));
+        }
+        float a[4];
+        unpack4(a4, a);
+        int c[ND];
+        coords<ND>(e0, sh, c);
+        float g[4];
+        dtd_at4<ND>(q, qc, c, e0, sh, g);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float vj = ct::fmul(tp.rho, g[j]);
+          for (int t = 1; t < tp.ng; ++t) vj = ct::fadd(vj, ct::fmul(tp.rho, g[j]));
+          v[j] = ct::fadd(vj, ct::fmul(tp.c, a[j]));
+        }
+        if (INIT) st4(lhsx, e0, v);
+      }
+      if (INIT) {
+        float b[4], re[4];
+        unpack4(ld4(rhs, e0), b);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) re[j] = ct::fsub(b[j], v[j]);
+        st4(out, e0, re);  // r
+        st4(p, e0, re);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          acc[0] += (double)re[j] * (double)re[j];
+          acc[1] += (double)b[j] * (double)b[j];
+        }
+      } else {
+        st4(out, e0, v);  // Ap
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[0] += (double)qc[j] * (double)v[j];
+      }
+    }
+  } else {
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     float v;
     if (cached) {
@@ -284,6 +549,7 @@ __global__ void __launch_bounds__(NT)
       out[e] = v;  // Ap
       acc[0] += (double)q[e] * (double)v;
     }
+  }
   }
   double tot[2];
   if (ct::grid_sumk_last<NT, 2>(acc, partials, ticket, tot)) {
@@ -334,38 +600,84 @@ __device__ __forceinline__ void prox_nd(int kind, float thr, const float (&v)[ND
   }
 }
 
+// z/u update of one element from its differences d (k_zu's body).
 template <int ND>
-__global__ void __launch_bounds__(NT)
-    k_zu(const float* __restrict__ x, float* __restrict__ z, float* __restrict__ u, float* __restrict__ dz,
-         Shape3 sh, size_t N, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
-         unsigned int* __restrict__ ticket) {
-  double acc[3] = {0.0, 0.0, 0.0};  // primal, g21, g1
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-    int c[ND];
-    coords<ND>(e, sh, c);
-    float d[ND];
-    d_at<ND>(x, c, e, sh, d);
-    for (int t = 0; t < tp.ng; ++t) {
-      const size_t o = (size_t)t * ND * N;
-      float zo[ND], v[ND], zn[ND];
+__device__ __forceinline__ void zu_el(const float (&d)[ND], float* __restrict__ z, float* __restrict__ u,
+                                      float* __restrict__ dz, size_t e, size_t N, const TermParams& tp,
+                                      double (&acc)[3]) {
+  for (int t = 0; t < tp.ng; ++t) {
+    const size_t o = (size_t)t * ND * N;
+    float zo[ND], v[ND], zn[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      zo[k] = z[o + k * N + e];
+      float ck = d[k];
+      if (tp.alpha != 1.0f) {
+        const float om = ct::fsub(1.0f, tp.alpha);
+        ck = ct::fadd(ct::fmul(tp.alpha, d[k]), ct::fmul(om, zo[k]));
+      }
+      v[k] = ct::fadd(ck, u[o + k * N + e]);
+    }
+    prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
+    double pr = 0.0;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      z[o + k * N + e] = zn[k];
+      u[o + k * N + e] = ct::fsub(v[k], zn[k]);
+      dz[o + k * N + e] = ct::fsub(zn[k], zo[k]);
+      const double pk = (double)d[k] - (double)zn[k];
+      pr = k == 0 ? pk * pk : pr + pk * pk;
+    }
+    acc[0] += (double)tp.rho * pr;
+    if (tp.kind[t] == 0) {
+      float s2 = ct::fmul(zn[0], zn[0]);
+#pragma unroll
+      for (int k = 1; k < ND; ++k) s2 = ct::fadd(s2, ct::fmul(zn[k], zn[k]));
+      acc[1] += (double)__fsqrt_rn(s2);
+    } else {
+      double a1 = fabs((double)zn[0]);
+#pragma unroll
+      for (int k = 1; k < ND; ++k) a1 += fabs((double)zn[k]);
+      acc[2] += a1;
+    }
+  }
+}
+
+// z/u update of the quad at e0: the state arrays move in 128-bit loads and
+// stores, the arithmetic is zu_el's per element, elements in order.
+template <int ND>
+__device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* __restrict__ z, float* __restrict__ u,
+                                        float* __restrict__ dz, size_t e0, size_t N, const TermParams& tp,
+                                        double (&acc)[3]) {
+  for (int t = 0; t < tp.ng; ++t) {
+    const size_t o = (size_t)t * ND * N;
+    float zo[ND][4], uo[ND][4];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      unpack4(ld4(z + o + k * N, e0), zo[k]);
+      unpack4(ld4(u + o + k * N, e0), uo[k]);
+    }
+    float zn4[ND][4], un4[ND][4], dz4[ND][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float v[ND], zn[ND];
 #pragma unroll
       for (int k = 0; k < ND; ++k) {
-        zo[k] = z[o + k * N + e];
-        float ck = d[k];
+        float ck = d[k][j];
         if (tp.alpha != 1.0f) {
           const float om = ct::fsub(1.0f, tp.alpha);
-          ck = ct::fadd(ct::fmul(tp.alpha, d[k]), ct::fmul(om, zo[k]));
+          ck = ct::fadd(ct::fmul(tp.alpha, d[k][j]), ct::fmul(om, zo[k][j]));
         }
-        v[k] = ct::fadd(ck, u[o + k * N + e]);
+        v[k] = ct::fadd(ck, uo[k][j]);
       }
       prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
       double pr = 0.0;
 #pragma unroll
       for (int k = 0; k < ND; ++k) {
-        z[o + k * N + e] = zn[k];
-        u[o + k * N + e] = ct::fsub(v[k], zn[k]);
-        dz[o + k * N + e] = ct::fsub(zn[k], zo[k]);
-        const double pk = (double)d[k] - (double)zn[k];
+        zn4[k][j] = zn[k];
+        un4[k][j] = ct::fsub(v[k], zn[k]);
+        dz4[k][j] = ct::fsub(zn[k], zo[k][j]);
+        const double pk = (double)d[k][j] - (double)zn[k];
         pr = k == 0 ? pk * pk : pr + pk * pk;
       }
       acc[0] += (double)tp.rho * pr;
@@ -380,6 +692,38 @@ __global__ void __launch_bounds__(NT)
         for (int k = 1; k < ND; ++k) a1 += fabs((double)zn[k]);
         acc[2] += a1;
       }
+    }
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      st4(z + o + k * N, e0, zn4[k]);
+      st4(u + o + k * N, e0, un4[k]);
+      st4(dz + o + k * N, e0, dz4[k]);
+    }
+  }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(NT)
+    k_zu(const float* __restrict__ x, float* __restrict__ z, float* __restrict__ u, float* __restrict__ dz,
+         Shape3 sh, size_t N, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
+         unsigned int* __restrict__ ticket, int vec) {
+  double acc[3] = {0.0, 0.0, 0.0};  // primal, g21, g1
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e0, sh, c);
+      float xc[4], d[ND][4];
+      unpack4(ld4(x, e0), xc);
+      d_at4<ND>(x, xc, c, e0, sh, d);
+      zu_quad<ND>(d, z, u, dz, e0, N, tp, acc);
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e, sh, c);
+      float d[ND];
+      d_at<ND>(x, c, e, sh, d);
+      zu_el<ND>(d, z, u, dz, e, N, tp, acc);
     }
   }
   double tot[3];
@@ -546,6 +890,8 @@ struct Ctx {
   float* x;
   double* itstat;
   TermParams tp;
+  int vi;  // image-sized kernels take the quad path (last axis % 4 == 0, x 16-B aligned)
+  int vs;  // sinogram-sized kernels take the quad path (size % 4 == 0, y 16-B aligned)
   template <class T>
   T* at(size_t off) const { return reinterpret_cast<T*>(ws + off); }
   double* slots() const { return at<double>(L.off_slots); }
@@ -594,10 +940,10 @@ ct_status enqueue_pre(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle c
   const double* clean = c.slots() + S_XCLEAN;
   CT_LAUNCH_ND(nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
                c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), rhs, c.P.sh, N, c.tp, c.slots(),
-               c.partials(), c.ticket());
+               c.partials(), c.ticket(), c.vi);
   CT_TRY(ct::launch_check("k_rhs"));
   CT_TRY(project(c, c.x, sinox, s, clean));
-  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket());
+  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket(), c.vs);
   CT_TRY(ct::launch_check("k_resid2"));
   k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21,
                             c.P.prm.lam_l1, 0);
@@ -609,12 +955,12 @@ ct_status enqueue_pre(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle c
     k_lhs_finish<2, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
                                             c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
                                             c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
-                                            cond, use_cond);
+                                            cond, use_cond, c.vi);
   else
     k_lhs_finish<3, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
                                             c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
                                             c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
-                                            cond, use_cond);
+                                            cond, use_cond, c.vi);
   return ct::launch_check("k_lhs_finish<init>");
 }
 
@@ -632,11 +978,11 @@ ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHand
   if (c.P.nd == 2)
     k_lhs_finish<2, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
                                              nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
-                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0);
+                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi);
   else
     k_lhs_finish<3, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
                                              nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
-                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0);
+                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi);
   CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
   CT_TRY(ct::cg_update_launch(c.x, r, p, ap, N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond));
   return ct::cg_direction_launch(p, r, N, c.cg(), c.ws + c.L.off_red, s);
@@ -644,7 +990,7 @@ ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHand
 
 ct_status enqueue_post(const Ctx& c, cudaStream_t s) {
   CT_LAUNCH_ND(c.P.nd, k_zu, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-               c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp, c.slots(), c.partials(), c.ticket());
+               c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp, c.slots(), c.partials(), c.ticket(), c.vi);
   return ct::launch_check("k_zu");
 }
 
@@ -661,10 +1007,10 @@ ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
   float* sinox = c.at<float>(c.L.off_sinox);
   CT_LAUNCH_ND(c.P.nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
                c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N,
-               c.tp, c.slots(), c.partials(), c.ticket());
+               c.tp, c.slots(), c.partials(), c.ticket(), c.vi);
   CT_TRY(ct::launch_check("k_rhs"));
   CT_TRY(project(c, c.x, sinox, s, c.slots() + S_XCLEAN));
-  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket());
+  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket(), c.vs);
   CT_TRY(ct::launch_check("k_resid2"));
   k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21,
                             c.P.prm.lam_l1, 1);
@@ -845,6 +1191,8 @@ ct_status make_ctx(const D* d, const char* who, const float* y, float* x, double
   tp.rho = (float)prm.rho;
   tp.alpha = (float)prm.alpha;
   tp.c = (float)(2.0 * prm.loss_scale);
+  c.vi = (c.P.sh.n[c.P.nd - 1] % 4 == 0 && ct::aligned(c.x, 16)) ? 1 : 0;
+  c.vs = (c.P.S % 4 == 0 && ct::aligned(c.y, 16)) ? 1 : 0;
   return c.P.proj.prepare();
 }
 
@@ -857,10 +1205,10 @@ ct_status run_solve(const Ctx& c, int32_t iter0, cudaStream_t s) {
     CT_TRY(c.P.proj.adj(c.y, c.at<float>(c.L.off_adj), c.at<float>(c.L.off_adjpart), s, nullptr));
     const int ns = c.P.proj.nsplit();
     const float* src = ns > 1 ? c.at<float>(c.L.off_adjpart) : c.at<float>(c.L.off_adj);
-    k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.P.N, ns, c.tp.c);
+    k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.P.N, ns, c.tp.c, c.vi);
     CT_TRY(ct::launch_check("k_scale_splits"));
     CT_LAUNCH_ND(c.P.nd, k_init_state, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-                 c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp.ng);
+                 c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp.ng, c.vi);
     CT_TRY(ct::launch_check("k_init_state"));
   }
   k_reset_call<<<1, 1, 0, s>>>(c.slots());

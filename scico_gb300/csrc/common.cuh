@@ -26,6 +26,13 @@ __host__ __device__ inline bool aligned(const void* p, size_t a) {
 
 inline size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// 1 when n elements split into float4 quads and every array is 16-B
+// aligned: the elementwise kernels then move 128 bits per access.
+template <class... P>
+inline int quad_ok(size_t n, const P*... ptrs) {
+  return (n % 4 == 0 && (aligned(ptrs, 16) && ...)) ? 1 : 0;
+}
+
 // ---------------------------------------------------------------------------
 // Exact float32 arithmetic.  The projector weights must be computed with the
 // same IEEE operations, in the same order, as the reference's float32

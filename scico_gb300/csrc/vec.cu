@@ -35,12 +35,46 @@ __device__ __forceinline__ bool grid_sum2_last(double a, double b, double* parti
 
 constexpr int NT = ct::kReduceThreads;
 
+// Quad path: with n % 4 == 0 and every array 16-B aligned a thread moves
+// four consecutive elements per 128-bit access, two quads per loop step so
+// that more loads are in flight; per element the arithmetic is the scalar
+// code's.
+__device__ __forceinline__ float4 ld4(const float* __restrict__ p, size_t e) {
+  return *reinterpret_cast<const float4*>(p + e);
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, size_t e, float4 v) {
+  *reinterpret_cast<float4*>(p + e) = v;
+}
+__device__ __forceinline__ float at4(const float4& v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
 __global__ void __launch_bounds__(NT)
     k_dot(const float* __restrict__ a, const float* __restrict__ b, size_t n,
-          double* __restrict__ out, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+          double* __restrict__ out, double* __restrict__ partials, unsigned int* __restrict__ ticket,
+          int vec) {
   double acc = 0.0;
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
-    acc += (double)a[e] * (double)b[e];
+  if (vec) {
+    const size_t stride = 4 * (size_t)gridDim.x * NT;
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < n; e0 += 2 * stride) {
+      const bool two = e0 + stride < n;
+      const float4 a0 = ld4(a, e0), b0 = ld4(b, e0);
+      float4 a1 = a0, b1 = b0;
+      if (two) {
+        a1 = ld4(a, e0 + stride);
+        b1 = ld4(b, e0 + stride);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc += (double)at4(a0, j) * (double)at4(b0, j);
+      if (two) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc += (double)at4(a1, j) * (double)at4(b1, j);
+      }
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT)
+      acc += (double)a[e] * (double)b[e];
+  }
   double t0, t1;
   if (grid_sum2_last<NT>(acc, 0.0, partials, ticket, t0, t1)) *out = t0;
 }
@@ -48,15 +82,33 @@ __global__ void __launch_bounds__(NT)
 __global__ void __launch_bounds__(NT)
     k_cg_init(const float* __restrict__ b, const float* __restrict__ Ax, float* __restrict__ r,
               float* __restrict__ p, size_t n, double tol, double atol, int maxiter,
-              double* __restrict__ s, double* __restrict__ partials, unsigned int* __restrict__ ticket) {
+              double* __restrict__ s, double* __restrict__ partials, unsigned int* __restrict__ ticket,
+              int vec) {
   double rr = 0.0, bb = 0.0;
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-    const float be = b[e];
-    const float re = ct::fsub(be, Ax[e]);
-    r[e] = re;
-    p[e] = re;
-    rr += (double)re * (double)re;
-    bb += (double)be * (double)be;
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < n; e0 += 4 * (size_t)gridDim.x * NT) {
+      const float4 b4 = ld4(b, e0), a4 = ld4(Ax, e0);
+      float re[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float be = at4(b4, j);
+        re[j] = ct::fsub(be, at4(a4, j));
+        rr += (double)re[j] * (double)re[j];
+        bb += (double)be * (double)be;
+      }
+      const float4 r4 = make_float4(re[0], re[1], re[2], re[3]);
+      st4(r, e0, r4);
+      st4(p, e0, r4);
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+      const float be = b[e];
+      const float re = ct::fsub(be, Ax[e]);
+      r[e] = re;
+      p[e] = re;
+      rr += (double)re * (double)re;
+      bb += (double)be * (double)be;
+    }
   }
   double trr, tbb;
   if (grid_sum2_last<NT>(rr, bb, partials, ticket, trr, tbb)) {
@@ -82,7 +134,7 @@ __global__ void __launch_bounds__(NT)
     k_cg_update(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
                 const float* __restrict__ Ap, size_t n, double* __restrict__ s,
                 double* __restrict__ partials, unsigned int* __restrict__ ticket,
-                cudaGraphConditionalHandle cond, int use_cond) {
+                cudaGraphConditionalHandle cond, int use_cond, int vec) {
   if (s[CT_CG_DONE] != 0.0) {  // uniform over the grid
     if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
     return;
@@ -90,12 +142,40 @@ __global__ void __launch_bounds__(NT)
   const double alpha = s[CT_CG_NUM] / s[CT_CG_PAP];
   const float af = (float)alpha;
   double rr = 0.0;
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-    const float pe = p[e];
-    x[e] = ct::fadd(x[e], ct::fmul(af, pe));
-    const float re = ct::fsub(r[e], ct::fmul(af, Ap[e]));
-    r[e] = re;
-    rr += (double)re * (double)re;
+  if (vec) {
+    const size_t stride = 4 * (size_t)gridDim.x * NT;
+    auto quad = [&](size_t e0, float4 x4, float4 r4, float4 p4, float4 a4) {
+      float xv[4], rv[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        xv[j] = ct::fadd(at4(x4, j), ct::fmul(af, at4(p4, j)));
+        rv[j] = ct::fsub(at4(r4, j), ct::fmul(af, at4(a4, j)));
+        rr += (double)rv[j] * (double)rv[j];
+      }
+      st4(x, e0, make_float4(xv[0], xv[1], xv[2], xv[3]));
+      st4(r, e0, make_float4(rv[0], rv[1], rv[2], rv[3]));
+    };
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < n; e0 += 2 * stride) {
+      const bool two = e0 + stride < n;
+      const float4 x0 = ld4(x, e0), r0 = ld4(r, e0), p0 = ld4(p, e0), a0 = ld4(Ap, e0);
+      float4 x1 = x0, r1 = r0, p1 = p0, a1 = a0;
+      if (two) {
+        x1 = ld4(x, e0 + stride);
+        r1 = ld4(r, e0 + stride);
+        p1 = ld4(p, e0 + stride);
+        a1 = ld4(Ap, e0 + stride);
+      }
+      quad(e0, x0, r0, p0, a0);
+      if (two) quad(e0 + stride, x1, r1, p1, a1);
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
+      const float pe = p[e];
+      x[e] = ct::fadd(x[e], ct::fmul(af, pe));
+      const float re = ct::fsub(r[e], ct::fmul(af, Ap[e]));
+      r[e] = re;
+      rr += (double)re * (double)re;
+    }
   }
   double trr, t1;
   if (grid_sum2_last<NT>(rr, 0.0, partials, ticket, trr, t1)) {
@@ -118,12 +198,31 @@ __global__ void __launch_bounds__(NT)
 // the marker when it starts; the last block to finish (ticket in the second
 // word of the reduction workspace) clears it, after all blocks have read it.
 __global__ void k_cg_direction(float* __restrict__ p, const float* __restrict__ r, size_t n,
-                               double* __restrict__ s, unsigned int* __restrict__ ticket) {
+                               double* __restrict__ s, unsigned int* __restrict__ ticket, int vec) {
   if (s[CT_CG_RAN] == 0.0) return;  // uniform over the grid
   const float bf = (float)s[CT_CG_BETA];
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x)
-    p[e] = ct::fadd(r[e], ct::fmul(bf, p[e]));
+  if (vec) {
+    const size_t stride = 4 * (size_t)gridDim.x * blockDim.x;
+    auto quad = [&](size_t e0, float4 r4, float4 p4) {
+      st4(p, e0, make_float4(ct::fadd(r4.x, ct::fmul(bf, p4.x)), ct::fadd(r4.y, ct::fmul(bf, p4.y)),
+                             ct::fadd(r4.z, ct::fmul(bf, p4.z)), ct::fadd(r4.w, ct::fmul(bf, p4.w))));
+    };
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x); e0 < n; e0 += 2 * stride) {
+      const bool two = e0 + stride < n;
+      const float4 r0 = ld4(r, e0), p0 = ld4(p, e0);
+      float4 r1 = r0, p1 = p0;
+      if (two) {
+        r1 = ld4(r, e0 + stride);
+        p1 = ld4(p, e0 + stride);
+      }
+      quad(e0, r0, p0);
+      if (two) quad(e0 + stride, r1, p1);
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (size_t)gridDim.x * blockDim.x)
+      p[e] = ct::fadd(r[e], ct::fmul(bf, p[e]));
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -145,8 +244,9 @@ ct_status ct_dot(const float* a, const float* b, int64_t n, double* out_dev, voi
   RedWs w;
   ct_status st = red_ws(workspace, workspace_bytes, "ct_dot", w);
   if (st != CT_OK) return st;
+  const int vec = ct::quad_ok((size_t)n, a, b);
   k_dot<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(a, b, (size_t)n, out_dev, w.partials,
-                                                            w.ticket);
+                                                            w.ticket, vec);
   return ct::launch_check("k_dot");
 }
 
@@ -159,8 +259,9 @@ ct_status ct_cg_init(const float* b, const float* Ax, float* r, float* p, int64_
   RedWs w;
   ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_init", w);
   if (st != CT_OK) return st;
+  const int vec = ct::quad_ok((size_t)n, b, Ax, r, p);
   k_cg_init<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(
-      b, Ax, r, p, (size_t)n, tol, atol, maxiter, scalars, w.partials, w.ticket);
+      b, Ax, r, p, (size_t)n, tol, atol, maxiter, scalars, w.partials, w.ticket, vec);
   return ct::launch_check("k_cg_init");
 }
 
@@ -172,8 +273,9 @@ ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap, int6
   RedWs w;
   ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_update", w);
   if (st != CT_OK) return st;
+  const int vec = ct::quad_ok((size_t)n, x, r, p, Ap);
   k_cg_update<<<ct::kReduceBlocks, NT, 0, ct::as_stream(stream)>>>(x, r, p, Ap, (size_t)n, scalars,
-                                                                  w.partials, w.ticket, 0, 0);
+                                                                  w.partials, w.ticket, 0, 0, vec);
   return ct::launch_check("k_cg_update");
 }
 
@@ -196,14 +298,15 @@ ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, 
                            int use_cond) {
   unsigned int* ticket = static_cast<unsigned int*>(red_ws);
   double* partials = reinterpret_cast<double*>(static_cast<char*>(red_ws) + 256);
-  k_cg_update<<<kReduceBlocks, NT, 0, s>>>(x, r, p, Ap, n, scalars, partials, ticket, cond, use_cond);
+  k_cg_update<<<kReduceBlocks, NT, 0, s>>>(x, r, p, Ap, n, scalars, partials, ticket, cond, use_cond,
+                                           quad_ok(n, x, r, p, Ap));
   return launch_check("k_cg_update");
 }
 
 ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, void* red_ws,
                               cudaStream_t s) {
   unsigned int* ticket2 = static_cast<unsigned int*>(red_ws) + 1;
-  k_cg_direction<<<kReduceBlocks, NT, 0, s>>>(p, r, n, scalars, ticket2);
+  k_cg_direction<<<kReduceBlocks, NT, 0, s>>>(p, r, n, scalars, ticket2, quad_ok(n, p, r));
   return launch_check("k_cg_direction");
 }
 
