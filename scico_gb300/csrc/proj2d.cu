@@ -85,19 +85,6 @@ __device__ __forceinline__ void weight_floor(float px, float width, float inv_wi
   w = ct::fmul(fminf(dist, width), inv_width);
 }
 
-// Fast path for |px| < 2^22: t = kMagic + floor(px) exactly (one round-down
-// add), dist = (floor(px) + 1) - px and w = sat(dist * inv_width), which is
-// min(1 - (px - floor(px)), width) / width up to one rounding of the product
-// (dist is the reference's 1 - (px - floor(px)) exactly for px >= 0; below
-// the detector's first bin it may differ by one rounding).
-__device__ __forceinline__ void weight_fast(float px, float inv_width, int& tbits, float& w) {
-  const float t = __fadd_rd(px, kMagic);
-  tbits = __float_as_int(t);
-  const float fl1 = ct::fsub(t, kMagic - 1.0f);
-  const float dist = ct::fsub(fl1, px);
-  w = __saturatef(ct::fmul(dist, inv_width));
-}
-
 __device__ __forceinline__ void st_shared(uint32_t addr, float v) {
   asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
 }
@@ -144,6 +131,12 @@ __device__ __forceinline__ unsigned long long fsub2(unsigned long long a, unsign
 // Walk one tile row for one view.  REV walks j downwards (Pdx1 < 0) so that
 // the bin key never decreases.  Bin b receives, in walk order, the (1-w) x of
 // the pixels with key b-1 followed by the w x of the pixels with key b.
+//
+// Fast floor for |px| < 2^22: t = magic + floor(px) exactly (one round-down
+// add), dist = (floor(px) + 1) - px and w = sat(dist * inv_width), which is
+// min(1 - (px - floor(px)), width) / width up to one rounding of the product
+// (dist is the reference's 1 - (px - floor(px)) exactly for px >= 0; below
+// the detector's first bin it may differ by one rounding).
 //
 // walk_row_fast: |Pdx1| < 0.999 and |Px| < 2^21, so consecutive keys differ
 // by 0 or 1.  The Px, floor, distance and 1 - w steps of two consecutive
@@ -246,10 +239,55 @@ __device__ __forceinline__ void strip_bins(const ViewParams& p, int i0, int c0, 
 // Shared memory of k_proj2d_fwd_strips: a 16-B header (the copy barrier),
 // then one region used twice: first the 32 x kRS strip, then, once every lane
 // holds its tile row in registers, the partial rows [kFW][32][LS] and two
-// slot buffers [2][kFW][cspan] (one per view parity).
+// slot buffers [2][kFW][cspan] (one per view parity); then the per-view
+// parameters of the CTA's run of views (FwdViewSmem).
 __host__ __device__ constexpr size_t fwd_region_floats(int LS, int cspan) {
   return (size_t)kT * kRS > (size_t)kFW * kT * LS + 2u * kFW * cspan ? (size_t)kT * kRS
                                                                      : (size_t)kFW * kT * LS + 2u * kFW * cspan;
+}
+constexpr int kMaxVpc = 16;  // views per forward CTA (upper bound of the plan's vpc)
+struct FwdViewSmem {
+  float4 pv[kMaxVpc];          // pxmin, Pdx0, Pdx1, 1/width
+  float width[kMaxVpc];
+  int2 strip[kMaxVpc];         // strip base bin, strip span
+  int4 tile[kMaxVpc][kFW];     // per tile: base bin, span (0 = nothing to do), strip offset, fast floor
+};
+
+// Per-view parameters of a forward CTA's run of views, one lane per (view,
+// tile): the view's table entry, the strip's bins and each tile's base bin,
+// span, offset in the strip and floor path (every lane of a warp would
+// otherwise compute the same values for its tile).  A span that does not fit
+// the partial rows or the slots (impossible for a table from
+// ct_proj2d_views) sets bit 0 of the error word and skips the tile.
+__device__ __forceinline__ void fwd_view_params(const FwdArgs& a, FwdViewSmem* vs, int i0, int c0, int ch) {
+  const int vbeg = blockIdx.y * a.vpc;
+  const int nvw = min(a.nv, vbeg + a.vpc) - vbeg;
+  const int t = threadIdx.x;
+  if (t >= nvw * kFW) return;
+  const int vi = t / kFW, w = t - vi * kFW;
+  const ViewParams p = load_view(a.views, vbeg + vi);
+  int cb, ssp;
+  strip_bins(p, i0, c0, cb, ssp);
+  int base = 0, span = 0, off = 0, fast = 0;
+  const int j0 = (ch * (kCW / kT) + w) * kT;
+  if (j0 < a.cols && i0 < a.rows) {
+    float lo, hi;
+    rect_px(p, i0, i0 + kT - 1, j0, j0 + kT - 1, lo, hi);
+    base = (int)floorf(lo);
+    span = (int)floorf(hi) - base + 2;
+    off = base - cb;
+    fast = (fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit && fabsf(p.pd1) < 0.999f) ? 1 : 0;
+    if (span > a.L || off < 0 || off + span > a.cspan) {
+      atomicOr(a.errflag, 1);
+      span = 0;
+    }
+  }
+  vs->tile[vi][w] = make_int4(base, span, off, fast);
+  if (w == 0) {
+    vs->pv[vi] = make_float4(p.pxmin, p.pd0, p.pd1, p.inv_width);
+    vs->width[vi] = p.width;
+    vs->strip[vi] = make_int2(cb, ssp);
+  }
 }
 
 // grid = (n_strips, view groups, batch), block = 256.  LSC: the partial-row
@@ -264,6 +302,7 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   float* strip = reinterpret_cast<float*>(smem_raw + 16);            // [32][kRS]
   float* part = strip;                                               // [kFW][32][LS]
   float* slots = part + kFW * kT * LS;                             // [2][kFW][cspan]
+  FwdViewSmem* vs = reinterpret_cast<FwdViewSmem*>(strip + fwd_region_floats(LS, a.cspan));
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int s = blockIdx.x;
@@ -292,6 +331,7 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
     for (int r = warp; r < kT; r += kFW)
       for (int c = lane; c < kRS; c += 32)
         if (r >= vrows || c >= vcols) strip[r * kRS + c] = 0.0f;
+    fwd_view_params(a, vs, i0, c0, ch);
     if (!ct::mbar_wait_bounded(bar, 0, kMaxPolls)) {
       if (tid == 0) atomicOr(a.errflag, 2);
       ct::mbar_wait_bounded(bar, 0, kMaxPolls);
@@ -300,12 +340,12 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
     for (int r = warp; r < kT; r += kFW)
       for (int c = lane; c < kRS; c += 32)
         strip[r * kRS + c] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
+    fwd_view_params(a, vs, i0, c0, ch);
   }
   __syncthreads();
 
   const int tj = ch * (kCW / kT) + warp;  // this warp's tile column
   const int j0 = tj * kT;
-  const bool tile_live = (j0 < a.cols) && (i0 < a.rows);
   const float fi = (float)(i0 + lane);
   const float fj0 = (float)j0;
   const int vbeg = blockIdx.y * a.vpc;
@@ -339,36 +379,28 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   // (after the barrier that ends the combine reading it).
   int zoff0 = 0, zspan0 = 0, zoff1 = 0, zspan1 = 0;
   for (int v = vbeg; v < vend; ++v) {
-    const int par = (v - vbeg) & 1;
-    const ViewParams p = load_view(a.views, v);
-    int cb, ssp;
-    strip_bins(p, i0, c0, cb, ssp);
+    const int vi = v - vbeg, par = vi & 1;
+    const float4 pv = vs->pv[vi];
+    const int4 tp = vs->tile[vi][warp];
     float* slot = slots + (par * kFW + warp) * a.cspan;
     {
       const int zo = par ? zoff1 : zoff0, zs = par ? zspan1 : zspan0;
       for (int k = lane; k < zs; k += 32) slot[zo + k] = 0.0f;
     }
     // ---- this warp's tile --------------------------------------------------
-    int off = 0, span = 0;
-    if (tile_live) {
-      float lo, hi;
-      rect_px(p, i0, i0 + kT - 1, j0, j0 + kT - 1, lo, hi);
-      const int base = (int)floorf(lo);
-      span = (int)floorf(hi) - base + 2;
-      off = base - cb;
-      const bool fast = fmaxf(fabsf(lo), fabsf(hi)) < kFastLimit && fabsf(p.pd1) < 0.999f;
-      if (span > a.L || off < 0 || off + span > a.cspan) {  // cannot happen for a table from ct_proj2d_views
-        if (lane == 0) atomicOr(a.errflag, 1);
-        span = 0;
-      } else {
-        const float R = ct::fadd(p.pxmin, ct::fmul(p.pd0, fi));
-        if (fast) {
+    const int off = tp.z, span = tp.y;
+    if (span > 0) {
+      {
+        const int base = tp.x;
+        const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
+        if (tp.w) {
           const uint32_t row_addr = ct::smem_u32(wpart) - 4u * (uint32_t)(kMagicBits + base);
-          if (p.pd1 >= 0.0f)
-            walk_row_fast<false>(xr, row_addr, magic, p.pd1, fj0, R, p.inv_width);
+          if (pv.z >= 0.0f)
+            walk_row_fast<false>(xr, row_addr, magic, pv.z, fj0, R, pv.w);
           else
-            walk_row_fast<true>(xr, row_addr, magic, p.pd1, fj0, R, p.inv_width);
+            walk_row_fast<true>(xr, row_addr, magic, pv.z, fj0, R, pv.w);
         } else {
+          const ViewParams p{pv.x, pv.y, pv.z, vs->width[vi], pv.w};
           if (p.pd1 >= 0.0f)
             walk_row_gen<false>(xr, mp, p, R, fj0, base);
           else
@@ -427,7 +459,7 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
     // ---- combine the 8 tiles in tile order into the strip's bins ----------
     const float* s0 = slots + par * kFW * a.cspan;
     float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + v) * a.cspan;
-    const int n = min(ssp, a.cspan);
+    const int n = min(vs->strip[vi].y, a.cspan);
     for (int k = tid; k < n; k += kFW * 32) {
       float acc = s0[k];
 #pragma unroll
@@ -653,7 +685,9 @@ int* errflag_ptr() {
   return cached[dev];
 }
 
-size_t fwd_smem_bytes(int LS, int cspan) { return 16 + sizeof(float) * fwd_region_floats(LS, cspan); }
+size_t fwd_smem_bytes(int LS, int cspan) {
+  return 16 + sizeof(float) * fwd_region_floats(LS, cspan) + sizeof(FwdViewSmem);
+}
 
 size_t adj_smem_bytes(int W) {
   return sizeof(float2) * (size_t)kAVC * W + sizeof(float4) * kAVC + sizeof(float) * kAVC +
@@ -700,7 +734,7 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   while ((p.LS & 31) != 15 && (p.LS & 31) != 17) ++p.LS;
   p.cspan = (int)floorf((float)(kCW - 1) * mw + 1.01f) + 3;
   const long work = (long)p.n_strips * g->n_views * batch;
-  p.vpc = (int)std::min<long>(16, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
+  p.vpc = (int)std::min<long>(kMaxVpc, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
   p.fwd_groups = (g->n_views + p.vpc - 1) / p.vpc;
   p.fwd_bytes = round_up((size_t)batch * p.n_strips * g->n_views * p.cspan * sizeof(float), 256);
   p.fwd_smem = fwd_smem_bytes(p.LS, p.cspan);
