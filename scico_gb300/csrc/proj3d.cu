@@ -132,6 +132,66 @@ __device__ __forceinline__ void tile_bins(float m11, float m12, float m13, int j
   hi = (int)floorf(pmax - 0.25f) + 3;
 }
 
+// Tile order of the forward: Z-order (Morton) over the tile grid's
+// power-of-two bounding box, axis-2 tile bit lowest, the longer side's
+// surplus bits on top.  A tile group takes a run of consecutive tiles in this
+// order, a compact patch of the image, so that for every view the tiles it
+// visits one after another touch overlapping detector columns and the
+// accumulator's read-modify-write stays in L2.
+__device__ __forceinline__ int bit_len(int n) {  // bits of n - 1 (0 for n <= 1)
+  return n <= 1 ? 0 : 32 - __clz(n - 1);
+}
+__device__ __forceinline__ void zorder_decode(int code, int bj, int bk, int& tj, int& tk) {
+  const int m = min(bj, bk);
+  tj = 0;
+  tk = 0;
+  for (int b = 0; b < m; ++b) {
+    tk |= ((code >> (2 * b)) & 1) << b;
+    tj |= ((code >> (2 * b + 1)) & 1) << b;
+  }
+  const int rest = code >> (2 * m);
+  if (bj > m) tj |= rest << m;
+  else tk |= rest << m;
+}
+// Tiles of the grid [0, nj) x [0, nk) inside the box [j, j + sj) x [k, k + sk).
+__device__ __forceinline__ int tiles_in(int j, int sj, int k, int sk, int nj, int nk) {
+  return max(0, min(nj, j + sj) - j) * max(0, min(nk, k + sk) - k);
+}
+// Code of the r-th tile of the grid in Z-order (r < nj * nk): descend the
+// surplus blocks, then the quadrants, counting the grid tiles each holds.
+__device__ int zorder_select(int r, int nj, int nk) {
+  const int bj = bit_len(nj), bk = bit_len(nk), m = min(bj, bk);
+  const int sq = 1 << m;
+  int code = 0, j = 0, k = 0;
+  const int nblk = 1 << (max(bj, bk) - m);
+  for (int blk = 0; blk < nblk; ++blk) {
+    const int jb = bj > m ? blk * sq : 0, kb = bj > m ? 0 : blk * sq;
+    const int c = tiles_in(jb, sq, kb, sq, nj, nk);
+    if (r < c) {
+      code = blk << (2 * m);
+      j = jb;
+      k = kb;
+      break;
+    }
+    r -= c;
+  }
+  for (int l = m - 1; l >= 0; --l) {
+    const int s = 1 << l;
+    for (int q = 0; q < 4; ++q) {
+      const int dj = q >> 1, dk = q & 1;
+      const int c = tiles_in(j + dj * s, s, k + dk * s, s, nj, nk);
+      if (r < c || q == 3) {
+        code |= q << (2 * l);
+        j += dj * s;
+        k += dk * s;
+        break;
+      }
+      r -= c;
+    }
+  }
+  return code;
+}
+
 __global__ void __launch_bounds__(256, 2) k_p3_ax0_fwd(const Ax0FwdArgs a) {
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) float smem[];
@@ -163,8 +223,23 @@ __global__ void __launch_bounds__(256, 2) k_p3_ax0_fwd(const Ax0FwdArgs a) {
   }
   __syncthreads();
 
-  for (int t = g; t < a.n_tiles; t += a.G) {
-    const int j0 = (t / a.tiles_k) * kTileJ, k0 = (t % a.tiles_k) * kTileK;
+  // this group's run of tiles in Z-order, ranks [g per, (g + 1) per): each
+  // thread looks up one rank, 256 tiles at a time
+  __shared__ int2 tlist[256];  // tile origins (j0, k0)
+  const int nrun = min((a.n_tiles + a.G - 1) / a.G, a.n_tiles - g * ((a.n_tiles + a.G - 1) / a.G));
+  for (int q = 0; q < nrun; ++q) {
+    if ((q & 255) == 0) {
+      if (q + tid < nrun) {
+        const int tiles_j = a.n_tiles / a.tiles_k, per = (a.n_tiles + a.G - 1) / a.G;
+        int tj, tk;
+        zorder_decode(zorder_select(g * per + q + tid, tiles_j, a.tiles_k), bit_len(tiles_j),
+                      bit_len(a.tiles_k), tj, tk);
+        tlist[tid] = make_int2(tj * kTileJ, tk * kTileK);
+      }
+      __syncthreads();
+    }
+    const int2 t0 = tlist[q & 255];
+    const int j0 = t0.x, k0 = t0.y;
     // stage vol[i0+s][j0+j][k0+k] as sv[(j*16+k)*66 + s] with register-free
     // 4-byte async copies, all in flight at once.  A warp copies two
     // 16-float rows, slices s and s+1 of one j (lanes = k, then the second
