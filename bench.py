@@ -31,6 +31,7 @@ on the data path; value = all ranks' iterations / max time.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import math
 import os
@@ -93,27 +94,35 @@ def _hbm_peak():
 
 
 class ClockSampler:
-    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region.
 
-    FIELDS = ["clocks.sm", "clocks.max.sm", "clocks_event_reasons.hw_slowdown",
+    nvidia-smi starts half a second before the region and samples every
+    25 ms; only samples whose own timestamps fall inside the region count
+    (all samples of the run are used, and said so, if none does)."""
+
+    FIELDS = ["timestamp", "clocks.sm", "clocks.max.sm", "clocks_event_reasons.hw_slowdown",
               "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
               "clocks_event_reasons.sw_power_cap"]
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.t0 = self.t1 = 0.0
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={','.join(self.FIELDS)}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)
         except Exception:
             self.proc = None
+        self.t0 = time.time()
         return self
 
     def __exit__(self, *exc):
+        self.t1 = time.time()
         self.result = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         if self.proc is None:
             return False
@@ -123,23 +132,30 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
             out = ""
-        sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in out.strip().splitlines():
             parts = [p.strip() for p in line.split(",")]
             if len(parts) != len(self.FIELDS):
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx.append(float(parts[1]))
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(parts[1]), float(parts[2]), parts[3:]))
             except ValueError:
                 continue
-            for name, val in zip(names, parts[2:]):
-                if val.lower().startswith("active"):
-                    reasons.add(name)
-        if sm:
-            self.result = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                           "samples": len(sm)}
+        inside = [r for r in rows if self.t0 <= r[0] <= self.t1]
+        window = "timed region"
+        if not inside:
+            inside, window = rows, "whole run (no sample inside the timed region)"
+        if inside:
+            reasons = set()
+            for r in inside:
+                for name, val in zip(names, r[3]):
+                    if val.lower().startswith("active"):
+                        reasons.add(name)
+            self.result = {"sm_mhz": statistics.median(r[1] for r in inside),
+                           "sm_max_mhz": max(r[2] for r in inside), "reasons": sorted(reasons),
+                           "samples": len(inside), "window": window}
         return False
 
 
