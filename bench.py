@@ -61,6 +61,8 @@ def _args():
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"],
                     help="c1/c2: 2D ADMM-TV (default c2); c5: 3D ADMM-TV, 256^3 x 360 views")
     ap.add_argument("--cpu-iters", type=int, default=1, help="ADMM iterations per CPU-baseline sample")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the planner's default projector schedule instead of measuring one first")
     return ap.parse_args()
 
 
@@ -287,6 +289,9 @@ def run_gpu(args):
 
     # ---- workload (device) -------------------------------------------------
     A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+    # projector launch schedules measured for this geometry and recorded
+    # (ct_proj2d_autotune), once, before anything is timed
+    schedule = A.autotune() if not args.no_autotune else A.schedule()
     x_gt = torch.from_numpy(c.phantom()).to(dev)
     y_clean = A(x_gt).cpu().numpy()
     y_host_np = workloads.noisy(y_clean, c.noise, c.noise_seed)
@@ -434,7 +439,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded 20-ellipse phantom, 0.5% Gaussian noise)",
-            "config": _config_json(c, args.config),
+            "config": dict(_config_json(c, args.config), projector_schedule=schedule),
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(c.n_views * c.det_count * 4),
                     "d2h_bytes_per_step": int(c.n * c.n * 4),

@@ -128,6 +128,46 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
                         ct_stream_t stream);
 
 /*
+ * Launch schedule of the 2D projector for one geometry and batch: views per
+ * CTA of the forward and view splits of the adjoint.  No counterpart in the
+ * reference (XLA picks its own launch shapes); the batched-scan workload asks
+ * for schedules chosen by measurement.
+ */
+typedef struct ct_proj2d_schedule {
+  int32_t views_per_cta; /* forward: views per CTA */
+  int32_t adj_splits;    /* adjoint: view splits (partial images summed in order) */
+  float fwd_us;          /* measured device time per forward call (0 if not measured) */
+  float adj_us;          /* measured device time per adjoint call (0 if not measured) */
+  int32_t tuned;         /* 1: recorded by ct_proj2d_autotune; 0: the planner's default */
+} ct_proj2d_schedule;
+
+/*
+ * Autotuner: times the forward for each candidate views-per-CTA and the
+ * adjoint (with its split sum) for each candidate split count on `stream`
+ * with CUDA events (one untimed call, then `reps` timed calls each), and
+ * records the fastest of each in a process-wide table (guarded by a mutex)
+ * keyed by the geometry's sizes and batch.  Every later call on that
+ * geometry (ct_proj2d_fwd/adj, the fused solvers) uses the recorded
+ * schedule; results change only in the adjoint's split summation order.
+ * img and sino are scratch (overwritten); the workspace needs
+ * max(fwd_bytes, adj_bytes) of ct_proj2d_workspace, whose adj_bytes already
+ * covers every split count a schedule may pick, so workspaces sized before
+ * tuning stay valid.  Blocks the host until the stream drains; not allowed
+ * inside a stream capture (CT_ERR_INVALID_ARG).
+ */
+ct_status ct_proj2d_autotune(const ct_geom2d* g, int32_t batch, float* img,
+                             float* sino, void* workspace, size_t workspace_bytes,
+                             int32_t reps, ct_stream_t stream,
+                             ct_proj2d_schedule* chosen);
+
+/* The schedule ct_proj2d_fwd/adj use for this geometry and batch now. */
+ct_status ct_proj2d_schedule_get(const ct_geom2d* g, int32_t batch,
+                                 ct_proj2d_schedule* out);
+
+/* Forget every recorded schedule (later calls use the planner's defaults). */
+void ct_proj2d_schedule_clear(void);
+
+/*
  * Ramp filter of XRayTransform2D.fbp (_xray2d.py:158-221): every row of
  * `sino` (n_rows rows of det_count samples, e.g. batch x n_views) convolved
  * with the Kak & Slaney eq. (61) ramp filter at tau = 1 and cropped to the

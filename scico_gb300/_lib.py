@@ -70,6 +70,16 @@ class CtError(RuntimeError):
         super().__init__(f"{func}: {message}")
 
 
+class Proj2dSchedule(ctypes.Structure):
+    _fields_ = [
+        ("views_per_cta", c_int32),
+        ("adj_splits", c_int32),
+        ("fwd_us", ctypes.c_float),
+        ("adj_us", ctypes.c_float),
+        ("tuned", c_int32),
+    ]
+
+
 class Geom2D(ctypes.Structure):
     _fields_ = [
         ("rows", c_int32),
@@ -147,6 +157,9 @@ _SIGNATURES = {
     "ct_proj2d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_proj2d_fwd_noalloc": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_proj2d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_proj2d_autotune": (ctypes.c_int, [P, c_int32, P, P, P, c_size_t, c_int32, P, P]),
+    "ct_proj2d_schedule_get": (ctypes.c_int, [P, c_int32, P]),
+    "ct_proj2d_schedule_clear": (None, []),
     "ct_fbp_filter": (ctypes.c_int, [P, P, c_int32, c_int32, P]),
     "ct_proj3d_views": (ctypes.c_int, [P, c_int32, P, P, P, P, P, P]),
     "ct_proj3d_workspace": (ctypes.c_int, [P, c_int32, P, P]),

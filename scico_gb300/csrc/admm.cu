@@ -767,6 +767,8 @@ struct Projector {
   ct::Proj3dPlan p3{};
   size_t fwd_bytes() const { return nd == 2 ? p2.fwd_bytes : p3.fwd_bytes; }
   size_t adj_bytes() const { return nd == 2 ? p2.adj_bytes : p3.adj_bytes; }
+  // split area to reserve: the largest any recorded 2D schedule may use
+  size_t adj_ws_bytes() const { return nd == 2 ? p2.adj_ws_bytes : p3.adj_bytes; }
   int nsplit() const { return nd == 2 ? p2.nsplit : p3.nsplit; }
   ct_status prepare() const { return nd == 2 ? ct::proj2d_prepare(p2) : ct::proj3d_prepare(g3, p3); }
   ct_status fwd(const float* img, float* sino, void* ws, cudaStream_t s, const double* skip) const {
@@ -852,7 +854,7 @@ Layout layout(const Problem& P) {
   L.off_u = take(zbytes);
   L.off_dz = take(zbytes);
   L.off_fwd = take(P.proj.fwd_bytes() > 0 ? P.proj.fwd_bytes() : 256);
-  L.off_adjpart = take(P.proj.adj_bytes() > 0 ? P.proj.adj_bytes() : 256);
+  L.off_adjpart = take(P.proj.adj_ws_bytes() > 0 ? P.proj.adj_ws_bytes() : 256);
   L.off_lhsx = take(P.N * 4);
   L.off_sinox = take(P.S * 4);
   L.total = o;
@@ -1046,6 +1048,10 @@ size_t make_key(const Ctx& c, unsigned char* key) {
   };
   put(&c.P.nd, sizeof(c.P.nd));
   put(c.P.desc, c.P.desc_size);
+  if (c.P.nd == 2) {  // the projector's schedule (the autotuner may record a new one)
+    put(&c.P.proj.p2.vpc, sizeof(int));
+    put(&c.P.proj.p2.nsplit, sizeof(int));
+  }
   put(&c.ws, sizeof(c.ws));
   put(&c.y, sizeof(c.y));
   put(&c.x, sizeof(c.x));

@@ -12,12 +12,22 @@ struct Proj2dPlan {
   size_t fwd_bytes, fwd_smem;
   // adjoint: 16x64 tiles, view splits, staged window length
   int adj_gx, adj_gy, nsplit, per_split, W;
-  size_t adj_bytes;  // split partial images (0 when nsplit == 1)
+  size_t adj_bytes;     // split partial images of this plan (0 when nsplit == 1)
+  size_t adj_ws_bytes;  // the same for the largest split count a schedule may pick
   size_t adj_smem;
 };
 
+// Launch schedule of the 2D projector: forward views per CTA and adjoint view
+// splits (0 = the planner's default).  ct_proj2d_autotune measures candidates
+// and records the fastest per geometry; proj2d_plan uses the recorded one.
+struct Sched2d {
+  int vpc = 0;
+  int ns = 0;
+};
+
 ct_status proj2d_check(const ct_geom2d* g, const char* who);
-Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch);
+Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch);  // recorded schedule, else default
+Proj2dPlan proj2d_plan_sched(const ct_geom2d* g, int batch, Sched2d s);
 // One-time per-process function attributes (large dynamic shared memory);
 // must run before any stream capture.
 ct_status proj2d_prepare(const Proj2dPlan& p);

@@ -28,6 +28,9 @@
 // |Px| < 2^22, checked per tile and view, with a floorf path otherwise):
 // full-rate FP32 operations instead of conversion instructions.
 #include <algorithm>
+#include <cstring>
+#include <map>
+#include <tuple>
 #include <mutex>
 
 #include "common.cuh"
@@ -365,8 +368,9 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   }
   __syncthreads();  // the strip is dead from here: its bytes become rows and slots
   {
-    const int nz = kFW * kT * LS + 2 * kFW * a.cspan;
-    for (int e = tid; e < nz; e += kFW * 32) part[e] = 0.0f;
+    const int nz4 = (kFW * kT * LS + 2 * kFW * a.cspan) / 4;  // rows and slots are whole float4s
+    float4* z4 = reinterpret_cast<float4*>(part);
+    for (int e = tid; e < nz4; e += kFW * 32) z4[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   __syncthreads();
 
@@ -716,7 +720,14 @@ ct_status proj2d_check(const ct_geom2d* g, const char* who) {
   return CT_OK;
 }
 
-Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
+// Largest adjoint split count a schedule may use: up to twice the splits
+// that fill the GPU, at least 16 views per split.
+int max_splits(const ct_geom2d* g, long ctas) {
+  int ns = ctas < 2L * kAdjTargetCtas ? (int)((2L * kAdjTargetCtas + ctas - 1) / ctas) : 1;
+  return std::max(1, std::min(ns, std::max(1, g->n_views / kAdjMinViewsPerSplit)));
+}
+
+Proj2dPlan proj2d_plan_sched(const ct_geom2d* g, int batch, Sched2d sc) {
   Proj2dPlan p;
   const float mw = g->max_width * 1.0001f;
   // Keys inside an a x b pixel rectangle differ by at most
@@ -734,7 +745,8 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   while ((p.LS & 31) != 15 && (p.LS & 31) != 17) ++p.LS;
   p.cspan = (int)floorf((float)(kCW - 1) * mw + 1.01f) + 3;
   const long work = (long)p.n_strips * g->n_views * batch;
-  p.vpc = (int)std::min<long>(kMaxVpc, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
+  p.vpc = sc.vpc > 0 ? std::min(sc.vpc, kMaxVpc)
+                     : (int)std::min<long>(kMaxVpc, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
   p.fwd_groups = (g->n_views + p.vpc - 1) / p.vpc;
   p.fwd_bytes = round_up((size_t)batch * p.n_strips * g->n_views * p.cspan * sizeof(float), 256);
   p.fwd_smem = fwd_smem_bytes(p.LS, p.cspan);
@@ -743,14 +755,56 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   p.adj_gx = (g->cols + kAJ - 1) / kAJ;
   p.adj_gy = (g->rows + kAI - 1) / kAI;
   const long ctas = (long)p.adj_gx * p.adj_gy * batch;
+  const int ns_max = max_splits(g, ctas);
   int ns = 1;
-  if (ctas < kAdjTargetCtas) ns = (int)((kAdjTargetCtas + ctas - 1) / ctas);
-  ns = std::min(ns, std::max(1, g->n_views / kAdjMinViewsPerSplit));
+  if (sc.ns > 0) {
+    ns = std::min(sc.ns, ns_max);
+  } else {
+    if (ctas < kAdjTargetCtas) ns = (int)((kAdjTargetCtas + ctas - 1) / ctas);
+    ns = std::min(ns, std::max(1, g->n_views / kAdjMinViewsPerSplit));
+  }
   p.per_split = (g->n_views + ns - 1) / ns;
   p.nsplit = (g->n_views + p.per_split - 1) / p.per_split;
-  p.adj_bytes =
-      p.nsplit > 1 ? round_up((size_t)p.nsplit * batch * g->rows * g->cols * sizeof(float), 256) : 0;
+  const size_t img = (size_t)batch * g->rows * g->cols * sizeof(float);
+  p.adj_bytes = p.nsplit > 1 ? round_up((size_t)p.nsplit * img, 256) : 0;
+  const int ws_splits = std::max(p.nsplit, ns_max);
+  p.adj_ws_bytes = ws_splits > 1 ? round_up((size_t)ws_splits * img, 256) : 0;
   return p;
+}
+
+// ---- recorded schedules ------------------------------------------------------
+struct SchedKey {
+  int rows, cols, nv, det, batch;
+  uint32_t width_bits;
+  bool operator<(const SchedKey& o) const {
+    return std::tie(rows, cols, nv, det, batch, width_bits) <
+           std::tie(o.rows, o.cols, o.nv, o.det, o.batch, o.width_bits);
+  }
+};
+struct SchedVal {
+  Sched2d s;
+  float fwd_us, adj_us;
+};
+std::mutex g_sched_mu;
+std::map<SchedKey, SchedVal> g_sched;
+
+SchedKey sched_key(const ct_geom2d* g, int batch) {
+  uint32_t wb;
+  memcpy(&wb, &g->max_width, sizeof(wb));
+  return SchedKey{g->rows, g->cols, g->n_views, g->det_count, batch, wb};
+}
+
+bool sched_lookup(const ct_geom2d* g, int batch, SchedVal& out) {
+  std::lock_guard<std::mutex> lk(g_sched_mu);
+  const auto it = g_sched.find(sched_key(g, batch));
+  if (it == g_sched.end()) return false;
+  out = it->second;
+  return true;
+}
+
+Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
+  SchedVal v;
+  return proj2d_plan_sched(g, batch, sched_lookup(g, batch, v) ? v.s : Sched2d{});
 }
 
 ct_status proj2d_prepare(const Proj2dPlan& p) {
@@ -833,7 +887,7 @@ ct_status ct_proj2d_workspace(const ct_geom2d* g, int32_t batch, size_t* fwd_byt
   if (batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_proj2d_workspace: batch=%d", batch);
   const ct::Proj2dPlan p = ct::proj2d_plan(g, batch);
   if (fwd_bytes) *fwd_bytes = p.fwd_bytes;
-  if (adj_bytes) *adj_bytes = p.adj_bytes;
+  if (adj_bytes) *adj_bytes = p.adj_ws_bytes;  // fits any schedule the autotuner may record
   return CT_OK;
 }
 
@@ -875,6 +929,132 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img, int32
   const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
   k_sum_splits<<<blocks, 256, 0, s>>>(part, img, n, p.nsplit, n);
   return ct::launch_check("k_sum_splits");
+}
+
+}  // extern "C"
+
+// ---- autotuning ------------------------------------------------------------------
+namespace {
+
+// Device time of `reps` calls of fn (after one untimed call), per call, in µs.
+template <class F>
+ct_status time_calls(F&& fn, int reps, cudaStream_t s, float& us) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ct_status st = ct::cuda_check(cudaEventCreate(&e0), "autotune event");
+  if (st == CT_OK) st = ct::cuda_check(cudaEventCreate(&e1), "autotune event");
+  if (st == CT_OK) st = fn();
+  if (st == CT_OK) st = ct::cuda_check(cudaEventRecord(e0, s), "autotune event record");
+  for (int r = 0; r < reps && st == CT_OK; ++r) st = fn();
+  if (st == CT_OK) st = ct::cuda_check(cudaEventRecord(e1, s), "autotune event record");
+  if (st == CT_OK) st = ct::cuda_check(cudaEventSynchronize(e1), "autotune event sync");
+  float ms = 0.0f;
+  if (st == CT_OK) st = ct::cuda_check(cudaEventElapsedTime(&ms, e0, e1), "autotune elapsed time");
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  us = 1000.0f * ms / (float)reps;
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+ct_status ct_proj2d_autotune(const ct_geom2d* g, int32_t batch, float* img, float* sino, void* workspace,
+                             size_t workspace_bytes, int32_t reps, ct_stream_t stream,
+                             ct_proj2d_schedule* chosen) {
+  const char* who = "ct_proj2d_autotune";
+  ct_status st = ct::proj2d_check(g, who);
+  if (st != CT_OK) return st;
+  if (!img || !sino) return ct::fail(CT_ERR_INVALID_ARG, "%s: null array", who);
+  if (batch <= 0 || reps <= 0) return ct::fail(CT_ERR_INVALID_ARG, "%s: batch=%d reps=%d", who, batch, reps);
+  cudaStream_t s = ct::as_stream(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  st = ct::cuda_check(cudaStreamIsCapturing(s, &cap), "stream capture query");
+  if (st != CT_OK) return st;
+  if (cap != cudaStreamCaptureStatusNone)
+    return ct::fail(CT_ERR_INVALID_ARG, "%s: cannot measure inside a stream capture", who);
+  const ct::Proj2dPlan p0 = ct::proj2d_plan_sched(g, batch, ct::Sched2d{});
+  const size_t need = std::max(p0.fwd_bytes, p0.adj_ws_bytes);
+  if (!workspace || workspace_bytes < need || !ct::aligned(workspace, 256))
+    return ct::fail(CT_ERR_WORKSPACE, "%s: need %zu bytes (256-B aligned), got %zu", who, need, workspace_bytes);
+  st = ct::proj2d_prepare(p0);
+  if (st != CT_OK) return st;
+  float* ws = static_cast<float*>(workspace);
+
+  // forward: views per CTA
+  static const int kVpcCand[] = {2, 3, 4, 5, 6, 7, 8, 10, 12, 16};
+  ct::Sched2d best;
+  float best_f = 0.0f;
+  for (int vpc : kVpcCand) {
+    if (vpc > kMaxVpc) continue;
+    const ct::Proj2dPlan p = ct::proj2d_plan_sched(g, batch, ct::Sched2d{vpc, 0});
+    float us = 0.0f;
+    st = time_calls([&] { return ct::proj2d_fwd_launch(g, p, img, sino, batch, ws, s, nullptr); }, reps, s, us);
+    if (st != CT_OK) return st;
+    if (best.vpc == 0 || us < best_f) {
+      best.vpc = p.vpc;
+      best_f = us;
+    }
+  }
+  // adjoint: view splits (the split sum included, as ct_proj2d_adj runs it)
+  const long ctas = (long)p0.adj_gx * p0.adj_gy * batch;
+  const int ns_max = ct::max_splits(g, ctas);
+  const size_t n = (size_t)batch * g->rows * g->cols;
+  float best_a = 0.0f;
+  int last = 0;
+  for (int ns = 1; ns <= ns_max; ++ns) {
+    const ct::Proj2dPlan p = ct::proj2d_plan_sched(g, batch, ct::Sched2d{0, ns});
+    if (p.nsplit == last) continue;  // same split count as the previous candidate
+    last = p.nsplit;
+    float us = 0.0f;
+    st = time_calls(
+        [&] {
+          ct_status r = ct::proj2d_adj_launch(g, p, sino, img, ws, batch, s, nullptr);
+          if (r != CT_OK || p.nsplit == 1) return r;
+          const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+          k_sum_splits<<<blocks, 256, 0, s>>>(ws, img, n, p.nsplit, n);
+          return ct::launch_check("k_sum_splits");
+        },
+        reps, s, us);
+    if (st != CT_OK) return st;
+    if (best.ns == 0 || us < best_a) {
+      best.ns = p.nsplit;
+      best_a = us;
+    }
+  }
+  {
+    std::lock_guard<std::mutex> lk(ct::g_sched_mu);
+    ct::g_sched[ct::sched_key(g, batch)] = ct::SchedVal{best, best_f, best_a};
+  }
+  if (chosen) {
+    chosen->views_per_cta = best.vpc;
+    chosen->adj_splits = best.ns;
+    chosen->fwd_us = best_f;
+    chosen->adj_us = best_a;
+    chosen->tuned = 1;
+  }
+  return CT_OK;
+}
+
+ct_status ct_proj2d_schedule_get(const ct_geom2d* g, int32_t batch, ct_proj2d_schedule* out) {
+  ct_status st = ct::proj2d_check(g, "ct_proj2d_schedule_get");
+  if (st != CT_OK) return st;
+  if (!out || batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_proj2d_schedule_get: out=%p batch=%d",
+                                          (void*)out, batch);
+  ct::SchedVal v{};
+  const bool tuned = ct::sched_lookup(g, batch, v);
+  const ct::Proj2dPlan p = ct::proj2d_plan(g, batch);
+  out->views_per_cta = p.vpc;
+  out->adj_splits = p.nsplit;
+  out->fwd_us = tuned ? v.fwd_us : 0.0f;
+  out->adj_us = tuned ? v.adj_us : 0.0f;
+  out->tuned = tuned ? 1 : 0;
+  return CT_OK;
+}
+
+void ct_proj2d_schedule_clear(void) {
+  std::lock_guard<std::mutex> lk(ct::g_sched_mu);
+  ct::g_sched.clear();
 }
 
 }  // extern "C"

@@ -427,6 +427,37 @@ class XRayTransform2D(LinearOperator):
                   _lib.ctypes.addressof(fwd), _lib.ctypes.addressof(adj))
         return int(fwd.value), int(adj.value)
 
+    def autotune(self, batch: int = 1, reps: int = 10) -> dict:
+        """Measure the projector's launch schedules for this geometry and
+        ``batch`` (forward views per CTA, adjoint view splits) and record the
+        fastest, which every later projection and fused solve on the same
+        geometry uses (``ct_proj2d_autotune``).  Runs on the current stream
+        and waits for it; not inside a stream capture.  No counterpart in the
+        reference.  Returns the chosen schedule and its measured times."""
+        g = self.geometry()
+        fwd_bytes, adj_bytes = self.workspace_bytes(batch)
+        ws = _device.workspace(max(fwd_bytes, adj_bytes, 256))
+        img = _device.empty((batch,) + self.input_shape)
+        sino = _device.empty((batch,) + self.output_shape)
+        img.zero_()
+        out = _lib.Proj2dSchedule()
+        _lib.call("ct_proj2d_autotune", _lib.ctypes.addressof(g), batch, img.data_ptr(), sino.data_ptr(),
+                  ws.data_ptr(), ws.numel(), reps, _device.stream(), _lib.ctypes.addressof(out))
+        return self._schedule_dict(out)
+
+    def schedule(self, batch: int = 1) -> dict:
+        """The launch schedule projections of this geometry use now (recorded
+        by :meth:`autotune`, else the planner's default)."""
+        g = self.geometry()
+        out = _lib.Proj2dSchedule()
+        _lib.call("ct_proj2d_schedule_get", _lib.ctypes.addressof(g), batch, _lib.ctypes.addressof(out))
+        return self._schedule_dict(out)
+
+    @staticmethod
+    def _schedule_dict(s) -> dict:
+        return {"views_per_cta": int(s.views_per_cta), "adj_splits": int(s.adj_splits),
+                "fwd_us": float(s.fwd_us), "adj_us": float(s.adj_us), "tuned": bool(s.tuned)}
+
     # -- operator -----------------------------------------------------------
     def _batched(self, x, core_shape, name):
         t = _device.to_device(x, name=name)

@@ -36,6 +36,8 @@ def main(argv=None):
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
     ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
     ap.add_argument("--streams", type=int, default=0, help="c3: internal streams of the batch solve (0 = auto)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="c3: measure and record projector schedules for every scan geometry before timing")
     ap.add_argument("--plain", action="store_true",
                     help="c3: also time the per-scan loops without graphs (fused solver with plain launches, "
                          "and scico_gb300.optimize.ADMM on the drop-in operators)")
@@ -231,6 +233,17 @@ def _c3(a, dev):
     both from device-resident data, CUDA events."""
     cfgs = workloads.batched_configs()
     n = len(cfgs)
+    tune_s = 0.0
+    if a.autotune:
+        import time
+
+        t0 = time.perf_counter()
+        seen = set()
+        for c in cfgs:
+            if (c.n, c.n_views) not in seen:
+                seen.add((c.n, c.n_views))
+                linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count).autotune(reps=5)
+        tune_s = time.perf_counter() - t0
     ys, xs, wss, descs, its, keep = [], [], [], [], [], []
     for c in cfgs:
         A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
@@ -280,7 +293,7 @@ def _c3(a, dev):
     pairs = sum(float(cg[k].sum() + a.iters) * cfgs[k].n ** 2 * cfgs[k].n_views for k in range(n))
     out = {"op": "c3", "scans": n, "iters": a.iters, "streams": a.streams, "batched_s": tb,
            "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb, "interactions_per_application": inter,
-           "mean_cg_iters": float(cg.mean()),
+           "mean_cg_iters": float(cg.mean()), "autotune_s": tune_s,
            "projection_pair_interactions": pairs}
     if a.plain:
         # the fused per-scan solver with every launch issued from the host
