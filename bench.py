@@ -428,11 +428,12 @@ def run_gpu(args):
     # call reset (4); per iteration the pre phase (rhs, forward strips and
     # gather, residual, itstat, adjoint, CG start = 7), the CG loop body (the
     # graph's WHILE node runs it exactly CG_It times: forward strips and
-    # gather, adjoint, lhs, CG update, direction = 6) and the z/u update (1);
+    # gather, adjoint, lhs, CG update, direction = 6), the z/u update and the
+    # ADMM loop step (2);
     # the itstat epilogue (rhs, forward strips and gather, residual, itstat =
     # 5).  CG_It comes from the solve's own itstat records.
     cg_its = [int(v) for v in itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()]
-    launches_per_step = 4 + sum(7 + 6 * k + 1 for k in cg_its) + 5
+    launches_per_step = 4 + sum(7 + 6 * k + 2 for k in cg_its) + 5
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -590,7 +591,7 @@ def run_gpu_3d(args):
                              f"to {k:.1f} + 2 pairs per ADMM iteration ({per_iter:.1f} s per iteration)"}
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
-    launches_per_step = 4 + sum(7 + 6 * k + 1 for k in cg_its) + 5  # as the 2D solver; projector = 2 kernels
+    launches_per_step = 4 + sum(7 + 6 * k + 2 for k in cg_its) + 5  # as the 2D solver; projector = 2 kernels
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

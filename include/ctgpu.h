@@ -378,7 +378,7 @@ typedef struct ct_admm_tv_desc {
   double rho;           /* ADMM penalty, same for every g_i              */
   double loss_scale;    /* SquaredL2Loss scale (0.5)                     */
   double alpha;         /* ADMM relaxation (1.0 = none)                  */
-  int32_t use_graph;    /* 1 = replay the iteration as a CUDA graph      */
+  int32_t use_graph;    /* 1 = the whole solve is one CUDA graph launch  */
 } ct_admm_tv_desc;
 
 /* Fields of one itstat record (double each). */
@@ -415,10 +415,15 @@ ct_status ct_admm_tv_solve(const ct_admm_tv_desc* d, const float* y, float* x,
  * (itstat_dev itself may be NULL) and its own workspace workspace[k] of
  * workspace_bytes[k] bytes (ct_admm_tv_workspace of descs[k]).  For many
  * scans of different sizes (no counterpart in the reference, whose scripts
- * solve one scan after another): each scan replays its own iteration graph
- * on one of n_streams internal streams (0 = min(n, 16), at most 32), scans
- * assigned longest-estimated-first to the least-loaded stream.  All work
- * starts after prior work on `stream`, and `stream` waits for all of it.
+ * solve one scan after another).  When every descs[k].use_graph is 1 the
+ * whole batch is one CUDA graph launch on `stream`: n independent branches,
+ * each a whole solve with its ADMM loop and CG loops as device-side
+ * conditional nodes (the graph is built on first use and cached for the same
+ * set of problems); n_streams is then unused.  Otherwise each scan runs with
+ * plain launches on one of n_streams internal streams (0 = min(n, 16), at
+ * most 32), scans assigned longest-estimated-first to the least-loaded
+ * stream.  All work starts after prior work on `stream`, and `stream` waits
+ * for all of it.
  */
 ct_status ct_admm_tv_solve_batch(const ct_admm_tv_desc* descs, int32_t n,
                                  const float* const* y, float* const* x,

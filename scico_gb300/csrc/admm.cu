@@ -9,8 +9,11 @@
 // and rho.  The elementwise kernels are templated on ND; A is whichever
 // projector the descriptor names.
 //
-// Per outer iteration (each kernel below is one launch; the whole iteration
-// is captured once into a CUDA graph and replayed):
+// Per outer iteration (each kernel below is one launch; with graphs the
+// whole solve is captured once into a CUDA graph -- set-up, the iterations
+// as a conditional WHILE node that k_admm_next keeps running for maxiter
+// iterations, the statistics epilogue -- and launched once per call; a batch
+// of scans is one graph with one such branch per scan):
 //   k_rhs         rhs = c A^T y + sum_i rho D^T(z_i - u_i); also the dual
 //                 residual ||sum_i rho D^T(z_i - z_i_old)|| of the previous
 //                 iteration
@@ -59,6 +62,7 @@ enum Slot {
   S_HAVE_PREV = 5,
   S_REC = 6,      // records written in this call
   S_XCLEAN = 7,   // 1 while lhs(x) and A x in the workspace belong to the current x
+  S_ITER = 8,     // ADMM iterations run in this call (the graph's device-side loop)
   S_CG = 16,      // CT_CG_NSCALARS doubles
   S_COUNT = 32
 };
@@ -740,6 +744,16 @@ __global__ void k_reset_call(double* __restrict__ slots) {
   slots[S_REC] = 0.0;
   slots[S_HAVE_PREV] = 0.0;
   slots[S_XCLEAN] = 0.0;  // the caller may have changed x between calls
+  slots[S_ITER] = 0.0;
+}
+
+// End of one ADMM iteration in the solve graph: count it and keep the
+// graph's iteration loop (a conditional WHILE node) running while fewer than
+// maxiter iterations have run.
+__global__ void k_admm_next(double* __restrict__ slots, int maxiter, cudaGraphConditionalHandle h) {
+  const double it = slots[S_ITER] + 1.0;
+  slots[S_ITER] = it;
+  cudaGraphSetConditional(h, it < (double)maxiter ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------------------
@@ -766,7 +780,6 @@ struct Projector {
   ct::Proj2dPlan p2{};
   ct::Proj3dPlan p3{};
   size_t fwd_bytes() const { return nd == 2 ? p2.fwd_bytes : p3.fwd_bytes; }
-  size_t adj_bytes() const { return nd == 2 ? p2.adj_bytes : p3.adj_bytes; }
   // split area to reserve: the largest any recorded 2D schedule may use
   size_t adj_ws_bytes() const { return nd == 2 ? p2.adj_ws_bytes : p3.adj_bytes; }
   int nsplit() const { return nd == 2 ? p2.nsplit : p3.nsplit; }
@@ -1025,8 +1038,7 @@ ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
 constexpr int kMaxGraphs = 256;
 
 struct GraphEntry {
-  unsigned char key[512];
-  size_t key_len = 0;
+  std::vector<unsigned char> key;
   int device = -1;
   cudaGraphExec_t exec = nullptr;
   unsigned long long last_use = 0;
@@ -1040,13 +1052,14 @@ struct GraphCache {
 };
 GraphCache g_cache;
 
-size_t make_key(const Ctx& c, unsigned char* key) {
-  size_t n = 0;
+void make_key(const Ctx& c, int32_t iter0, std::vector<unsigned char>& key) {
   auto put = [&](const void* p, size_t b) {
-    memcpy(key + n, p, b);
-    n += b;
+    const unsigned char* q = static_cast<const unsigned char*>(p);
+    key.insert(key.end(), q, q + b);
   };
+  const int fresh = iter0 == 0 ? 1 : 0;  // the solve starts from x (state initialised in the graph)
   put(&c.P.nd, sizeof(c.P.nd));
+  put(&fresh, sizeof(fresh));
   put(c.P.desc, c.P.desc_size);
   if (c.P.nd == 2) {  // the projector's schedule (the autotuner may record a new one)
     put(&c.P.proj.p2.vpc, sizeof(int));
@@ -1056,76 +1069,114 @@ size_t make_key(const Ctx& c, unsigned char* key) {
   put(&c.y, sizeof(c.y));
   put(&c.x, sizeof(c.x));
   put(&c.itstat, sizeof(c.itstat));
-  return n;
 }
 
-// The iteration graph: pre-phase kernels, then a conditional WHILE node
-// whose body is one CG step (the CG start and every CG update set the
-// condition on the device: run while CG has not converged), then the z/u
-// update.  Each phase is stream-captured into its place in the graph.
-ct_status build_iteration_graph(const Ctx& c, cudaStream_t cs, cudaGraph_t& graph) {
-  CT_TRY(ct::cuda_check(cudaGraphCreate(&graph, 0), "graph create"));
-  cudaGraphConditionalHandle cond = 0;
-  CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&cond, graph, 0, cudaGraphCondAssignDefault),
-                        "conditional handle"));
-  // pre phase
-  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, graph, nullptr, nullptr, 0,
-                                                      cudaStreamCaptureModeThreadLocal),
-                        "capture pre"));
-  ct_status st = enqueue_pre(c, cs, cond, 1);
+// Capture fn(stream) into `graph` after `deps`; the capture's last nodes
+// (at most 8) are returned in `tail`.
+template <class F>
+ct_status capture_into(cudaStream_t cs, cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
+                       std::vector<cudaGraphNode_t>& tail, F&& fn) {
+  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, graph, deps.empty() ? nullptr : deps.data(), nullptr,
+                                                      deps.size(), cudaStreamCaptureModeThreadLocal),
+                        "begin capture"));
+  ct_status st = fn(cs);
   cudaStreamCaptureStatus cst;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t ndeps = 0;
-  cudaError_t ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &deps, nullptr, &ndeps);
-  cudaGraphNode_t pre_tail[8];
-  const size_t npre = ndeps < 8 ? ndeps : 8;
-  for (size_t k = 0; ce == cudaSuccess && k < npre; ++k) pre_tail[k] = deps[k];
+  const cudaGraphNode_t* fr = nullptr;
+  size_t nfr = 0;
+  cudaError_t ce = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &fr, nullptr, &nfr);
+  tail.clear();
+  for (size_t k = 0; ce == cudaSuccess && k < nfr && k < 8; ++k) tail.push_back(fr[k]);
   cudaGraph_t out = nullptr;
   cudaError_t ce2 = cudaStreamEndCapture(cs, &out);
   CT_TRY(st);
   CT_TRY(ct::cuda_check(ce, "capture info"));
-  CT_TRY(ct::cuda_check(ce2, "end capture pre"));
-  if (ndeps > 8) return ct::fail(CT_ERR_CUDA, "unexpected capture frontier of %zu nodes", ndeps);
-  // conditional WHILE node for the CG loop
-  cudaGraphNodeParams cp = {};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = cond;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t cnode = nullptr;
-  CT_TRY(ct::cuda_check(cudaGraphAddNode(&cnode, graph, pre_tail, nullptr, npre, &cp), "conditional node"));
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
-  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
-                                                      cudaStreamCaptureModeThreadLocal),
-                        "capture body"));
-  st = enqueue_cg_step(c, cs, cond, 1);
-  ce2 = cudaStreamEndCapture(cs, &out);
-  CT_TRY(st);
-  CT_TRY(ct::cuda_check(ce2, "end capture body"));
-  // post phase after the loop
-  CT_TRY(ct::cuda_check(cudaStreamBeginCaptureToGraph(cs, graph, &cnode, nullptr, 1,
-                                                      cudaStreamCaptureModeThreadLocal),
-                        "capture post"));
-  st = enqueue_post(c, cs);
-  ce2 = cudaStreamEndCapture(cs, &out);
-  CT_TRY(st);
-  return ct::cuda_check(ce2, "end capture post");
+  CT_TRY(ct::cuda_check(ce2, "end capture"));
+  if (nfr > 8) return ct::fail(CT_ERR_CUDA, "unexpected capture frontier of %zu nodes", nfr);
+  return CT_OK;
 }
 
-// The executable iteration graph of a problem (built on first use).
-// Caller holds g_cache.m.
-ct_status graph_for(const Ctx& c, cudaGraphExec_t& exec) {
+// Append one whole solve to `graph`, independent of every other node:
+// the state set-up (iter0 == 0) and k_reset_call, then the ADMM loop as a
+// conditional WHILE node whose body is one iteration -- the pre-phase
+// kernels, the CG loop as a nested WHILE node (its start and every CG
+// update set its condition on the device: run while CG has not converged),
+// the z/u update and k_admm_next -- then the statistics epilogue.
+ct_status append_solve(const Ctx& c, int32_t iter0, cudaStream_t cs, cudaGraph_t graph) {
+  const Params& prm = c.P.prm;
+  std::vector<cudaGraphNode_t> tail;
+  CT_TRY(capture_into(cs, graph, {}, tail, [&](cudaStream_t s) -> ct_status {
+    if (iter0 == 0) {
+      CT_TRY(ct::cuda_check(cudaMemsetAsync(c.ws, 0, c.L.off_atyc, s), "memset state"));
+      // A^T y, scaled by 2*scale (hoisted out of the loop: y is constant).
+      CT_TRY(c.P.proj.adj(c.y, c.at<float>(c.L.off_adj), c.at<float>(c.L.off_adjpart), s, nullptr));
+      const int ns = c.P.proj.nsplit();
+      const float* src = ns > 1 ? c.at<float>(c.L.off_adjpart) : c.at<float>(c.L.off_adj);
+      k_scale_splits<<<NB, NT, 0, s>>>(src, c.at<float>(c.L.off_atyc), c.P.N, ns, c.tp.c, c.vi);
+      CT_TRY(ct::launch_check("k_scale_splits"));
+      CT_LAUNCH_ND(c.P.nd, k_init_state, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
+                   c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp.ng, c.vi);
+      CT_TRY(ct::launch_check("k_init_state"));
+    }
+    k_reset_call<<<1, 1, 0, s>>>(c.slots());
+    return ct::launch_check("k_reset_call");
+  }));
+  if (prm.maxiter > 0) {
+    cudaGraphConditionalHandle loop = 0;
+    CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&loop, graph, 1, cudaGraphCondAssignDefault),
+                          "loop handle"));
+    cudaGraphNodeParams lp = {};
+    lp.type = cudaGraphNodeTypeConditional;
+    lp.conditional.handle = loop;
+    lp.conditional.type = cudaGraphCondTypeWhile;
+    lp.conditional.size = 1;
+    cudaGraphNode_t lnode = nullptr;
+    CT_TRY(ct::cuda_check(cudaGraphAddNode(&lnode, graph, tail.data(), nullptr, tail.size(), &lp), "loop node"));
+    cudaGraph_t body = lp.conditional.phGraph_out[0];
+    cudaGraphConditionalHandle cg = 0;
+    CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&cg, body, 0, cudaGraphCondAssignDefault),
+                          "CG handle"));
+    std::vector<cudaGraphNode_t> pre;
+    CT_TRY(capture_into(cs, body, {}, pre, [&](cudaStream_t s) { return enqueue_pre(c, s, cg, 1); }));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cg;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode = nullptr;
+    CT_TRY(ct::cuda_check(cudaGraphAddNode(&cnode, body, pre.data(), nullptr, pre.size(), &cp), "CG node"));
+    std::vector<cudaGraphNode_t> unused;
+    CT_TRY(capture_into(cs, cp.conditional.phGraph_out[0], {}, unused,
+                        [&](cudaStream_t s) { return enqueue_cg_step(c, s, cg, 1); }));
+    CT_TRY(capture_into(cs, body, {cnode}, unused, [&](cudaStream_t s) -> ct_status {
+      CT_TRY(enqueue_post(c, s));
+      k_admm_next<<<1, 1, 0, s>>>(c.slots(), prm.maxiter, loop);
+      return ct::launch_check("k_admm_next");
+    }));
+    tail.assign(1, lnode);
+  } else {
+    return CT_OK;  // no iteration: no statistics either
+  }
+  std::vector<cudaGraphNode_t> end;
+  return capture_into(cs, graph, tail, end, [&](cudaStream_t s) { return enqueue_epilogue(c, s); });
+}
+
+// The executable graph of one solve, or of a batch of solves (independent
+// branches of one graph), built on first use and cached by the problems'
+// keys.  Caller holds g_cache.m.
+ct_status graph_for(const Ctx* cs, int n, int32_t iter0, cudaGraphExec_t& exec) {
   int dev = 0;
   CT_TRY(ct::cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
   if (dev < 0 || dev >= 64) return ct::fail(CT_ERR_UNSUPPORTED, "device %d", dev);
   if (!g_cache.capture[dev])
     CT_TRY(ct::cuda_check(cudaStreamCreateWithFlags(&g_cache.capture[dev], cudaStreamNonBlocking),
                           "capture stream"));
-  unsigned char key[512];
-  const size_t kl = make_key(c, key);
+  std::vector<unsigned char> key;
+  key.insert(key.end(), reinterpret_cast<const unsigned char*>(&n),
+             reinterpret_cast<const unsigned char*>(&n) + sizeof(n));
+  for (int k = 0; k < n; ++k) make_key(cs[k], iter0, key);
   GraphEntry* slot = nullptr;
   for (GraphEntry& e : g_cache.e) {
-    if (e.exec && e.device == dev && e.key_len == kl && memcmp(e.key, key, kl) == 0) {
+    if (e.exec && e.device == dev && e.key == key) {
       e.last_use = ++g_cache.clock;
       exec = e.exec;
       return CT_OK;
@@ -1137,32 +1188,32 @@ ct_status graph_for(const Ctx& c, cudaGraphExec_t& exec) {
     slot->exec = nullptr;
   }
   cudaGraph_t graph = nullptr;
-  ct_status st = build_iteration_graph(c, g_cache.capture[dev], graph);
+  CT_TRY(ct::cuda_check(cudaGraphCreate(&graph, 0), "graph create"));
+  ct_status st = CT_OK;
+  for (int k = 0; k < n && st == CT_OK; ++k) st = append_solve(cs[k], iter0, g_cache.capture[dev], graph);
   if (st != CT_OK) {
-    if (graph) cudaGraphDestroy(graph);
+    cudaGraphDestroy(graph);
     return st;
   }
   cudaError_t ce = cudaGraphInstantiate(&slot->exec, graph, 0);
   cudaGraphDestroy(graph);
   if (ce != cudaSuccess) slot->exec = nullptr;
   CT_TRY(ct::cuda_check(ce, "graph instantiate"));
-  memcpy(slot->key, key, kl);
-  slot->key_len = kl;
+  slot->key = std::move(key);
   slot->device = dev;
   slot->last_use = ++g_cache.clock;
   exec = slot->exec;
   return CT_OK;
 }
 
-ct_status run_graph(const Ctx& c, cudaStream_t s) {
+// One launch of the cached graph of n solves on stream s.
+ct_status run_graph(const Ctx* cs, int n, int32_t iter0, cudaStream_t s) {
   cudaGraphExec_t exec = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_cache.m);
-    CT_TRY(graph_for(c, exec));
+    CT_TRY(graph_for(cs, n, iter0, exec));
   }
-  for (int k = 0; k < c.P.prm.maxiter; ++k)
-    CT_TRY(ct::cuda_check(cudaGraphLaunch(exec, s), "graph launch"));
-  return CT_OK;
+  return ct::cuda_check(cudaGraphLaunch(exec, s), "graph launch");
 }
 
 // Validate one problem and fill its solver context.
@@ -1205,6 +1256,7 @@ ct_status make_ctx(const D* d, const char* who, const float* y, float* x, double
 // Enqueue one solve on stream s.
 ct_status run_solve(const Ctx& c, int32_t iter0, cudaStream_t s) {
   const Params& prm = c.P.prm;
+  if (prm.use_graph) return run_graph(&c, 1, iter0, s);  // the whole solve: one graph launch
   if (iter0 == 0) {
     CT_TRY(ct::cuda_check(cudaMemsetAsync(c.ws, 0, c.L.off_atyc, s), "memset state"));
     // A^T y, scaled by 2*scale (hoisted out of the loop: y is constant).
@@ -1220,11 +1272,7 @@ ct_status run_solve(const Ctx& c, int32_t iter0, cudaStream_t s) {
   k_reset_call<<<1, 1, 0, s>>>(c.slots());
   CT_TRY(ct::launch_check("k_reset_call"));
   if (prm.maxiter == 0) return CT_OK;
-  if (prm.use_graph) {
-    CT_TRY(run_graph(c, s));
-  } else {
-    for (int k = 0; k < prm.maxiter; ++k) CT_TRY(enqueue_iteration(c, s));
-  }
+  for (int k = 0; k < prm.maxiter; ++k) CT_TRY(enqueue_iteration(c, s));
   return enqueue_epilogue(c, s);
 }
 
@@ -1305,9 +1353,16 @@ ct_status ct_admm_tv_solve_batch(const ct_admm_tv_desc* descs, int32_t n, const 
   if (n_streams < 0 || n_streams > kMaxBatchStreams)
     return ct::fail(CT_ERR_INVALID_ARG, "%s: n_streams=%d (0..%d)", who, n_streams, kMaxBatchStreams);
   std::vector<Ctx> cs((size_t)n);
-  for (int k = 0; k < n; ++k)
+  bool all_graph = true;
+  for (int k = 0; k < n; ++k) {
     CT_TRY(make_ctx(&descs[k], who, y[k], x[k], itstat_dev ? itstat_dev[k] : nullptr, workspace[k],
                     workspace_bytes[k], cs[k]));
+    all_graph = all_graph && cs[k].P.prm.use_graph;
+  }
+  // All scans in one launch: a graph whose n independent branches are the
+  // whole solves (built once per set of problems and cached).
+  if (all_graph) return run_graph(cs.data(), n, iter0, ct::as_stream(stream));
+  // Plain launches: the scans on a pool of streams.
   const int ns = n_streams > 0 ? std::min(n_streams, n) : std::min(n, 16);
   // longest-processing-time-first assignment to the least-loaded stream
   std::vector<int> order((size_t)n);

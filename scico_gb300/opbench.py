@@ -37,7 +37,7 @@ def main(argv=None):
     ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
     ap.add_argument("--streams", type=int, default=0, help="c3: internal streams of the batch solve (0 = auto)")
     ap.add_argument("--autotune", action="store_true",
-                    help="c3: measure and record projector schedules for every scan geometry before timing")
+                    help="c3, modl: measure and record projector schedules (ct_proj2d_autotune) before timing")
     ap.add_argument("--plain", action="store_true",
                     help="c3: also time the per-scan loops without graphs (fused solver with plain launches, "
                          "and scico_gb300.optimize.ADMM on the drop-in operators)")
@@ -198,6 +198,7 @@ def _modl(a, dev):
     torch.backends.cuda.matmul.allow_tf32 = False
     c = workloads.C4
     H = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+    schedule = H.autotune(batch=c.batch, reps=5) if a.autotune else H.schedule(batch=c.batch)
     x_gt = torch.from_numpy(c.phantoms()).to(dev)
     y = H.project(x_gt)
     y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.phantom_seed)).to(dev)
@@ -223,7 +224,8 @@ def _modl(a, dev):
     print(json.dumps({"op": "modl", "config": "c4", "batch": c.batch, "recompute": a.recompute,
                       "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
                       "images_per_s_train": c.batch / (tf + tb), "projector_applications_forward": n_proj,
-                      "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach())}))
+                      "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach()),
+                      "projector_schedule": schedule}))
 
 
 def _c3(a, dev):
