@@ -263,6 +263,28 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# Multi-rank timing (one process per GPU, independent replicas)
+# ---------------------------------------------------------------------------
+
+
+def max_over_ranks(dist, t_local: float, device) -> float:
+    """The largest of every rank's time (the job ends with its slowest rank);
+    the rank's own time when not distributed."""
+    if dist is None:
+        return t_local
+    import torch
+
+    tt = torch.tensor([t_local], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, t_max: float) -> float:
+    """Units all ranks processed per second of the slowest rank."""
+    return units_per_rank * world / t_max
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 
@@ -334,14 +356,8 @@ def run_gpu(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
     barrier()
-    t_local = sum(times)
-    t_max = t_local
-    if dist is not None:
-        tt = torch.tensor([t_local], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    iters_total = c.maxiter * args.steps * world
-    value = iters_total / t_max
+    t_max = max_over_ranks(dist, sum(times), dev)
+    value = whole_job_rate(c.maxiter * args.steps, world, t_max)
     objective = float(itstat[c.maxiter - 1, _lib.CT_ITSTAT_OBJECTIVE])
     x_dev = x.clone()
 
@@ -367,12 +383,8 @@ def run_gpu(args):
         xr = e2e_step()
         e2e_times.append(time.perf_counter() - t0)
     barrier()
-    e2e_t = sum(e2e_times)
-    if dist is not None:
-        tt = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
-    e2e_value = c.maxiter * args.steps * world / e2e_t
+    e2e_t = max_over_ranks(dist, sum(e2e_times), dev)
+    e2e_value = whole_job_rate(c.maxiter * args.steps, world, e2e_t)
     e2e_dev_diff = float((xr.to(dev) - x_dev).norm() / x_dev.norm())
 
     # ---- roofline: the forward projector, live CUDA events ---------------------
@@ -525,12 +537,8 @@ def run_gpu_3d(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
     barrier()
-    t_max = sum(times)
-    if dist is not None:
-        tt = torch.tensor([t_max], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = c.maxiter * args.steps * world / t_max
+    t_max = max_over_ranks(dist, sum(times), dev)
+    value = whole_job_rate(c.maxiter * args.steps, world, t_max)
     cg_its = [int(v) for v in itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()]
     x_dev = x.clone()
 
@@ -554,7 +562,8 @@ def run_gpu_3d(args):
         xr = e2e_step()
         e2e_t += time.perf_counter() - t0
     barrier()
-    e2e_value = c.maxiter * args.steps * world / e2e_t
+    e2e_t = max_over_ranks(dist, e2e_t, dev)
+    e2e_value = whole_job_rate(c.maxiter * args.steps, world, e2e_t)
     e2e_diff = float((xr.to(dev) - x_dev).norm() / x_dev.norm())
 
     # roofline: the 3D forward projector, live CUDA events

@@ -53,3 +53,64 @@ def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
     with bench.ClockSampler(0) as clk:
         pass
     assert clk.result["samples"] == 0 and clk.result["sm_mhz"] is None
+
+
+def _rank_worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(REPO))
+    import torch.distributed as dist
+
+    import bench
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        t_max = bench.max_over_ranks(dist, 1.0 + 0.5 * rank, "cpu")
+        out.put((rank, t_max, bench.whole_job_rate(100, world, t_max)))
+    finally:
+        dist.destroy_process_group()
+
+
+def _free_port():
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_max_over_ranks_gloo_world2():
+    """Two replicas on gloo: every rank gets the slowest rank's time, and the
+    whole-job rate counts both ranks' units."""
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    assert [g[1] for g in got] == [1.5, 1.5]
+    assert all(abs(g[2] - 200 / 1.5) < 1e-9 for g in got)
+
+
+def test_single_process_rate():
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    assert bench.max_over_ranks(None, 2.0, "cpu") == 2.0
+    assert bench.whole_job_rate(100, 1, 2.0) == 50.0
+
+
+def test_reference_arm_nonzero_rank_exits_quietly():
+    """Under torchrun only rank 0 runs the reference arm; the others exit 0
+    without output."""
+    import subprocess
+
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip() == ""
