@@ -190,3 +190,18 @@ def test_c1_admm_quality(cuda):
     assert ex <= 3 * fx + 1e-4, (ex, fx)
     assert eo <= 3 * fo + 1e-4, (eo, fo)
     assert es <= 3 * fs + 0.02, (es, fs)
+
+def test_fused_rectangular_odd_columns(cuda):
+    """A 30 x 45 image: the last axis is not a multiple of 4, so the fused
+    kernels take their scalar path; converged regime against the float64
+    oracle as for square images."""
+    x_gt = workloads.random_ellipses(48, 4, 21)[:30, :45].copy()
+    ang = np.linspace(0, np.pi, 40, endpoint=False)
+    g = ctref.xray2d_defaults(x_gt.shape, ang)
+    y = workloads.noisy(ctref.xray2d_project(x_gt, g, np.float64).astype(np.float32), 0.01, 22)
+    s = _solver(cuda, ang, y, x_gt.shape, lam21=0.02, lam1=0.01, fused=True)
+    x = s.solve().cpu().numpy()
+    x64, hist, _, _ = _oracle(y, x_gt.shape, g, lam_l21=0.02, lam_l1=0.01, rho=50.0, maxiter=5, cg_maxiter=30,
+                              cg_tol=1e-5)
+    assert ctref.rel_l2(x, x64) <= 1e-4
+    np.testing.assert_allclose(s.history(transpose=True).Objective, [r["Objective"] for r in hist], rtol=1e-4)
