@@ -144,3 +144,67 @@ def test_workspace_errors(cuda):
     st = lib.ct_proj2d_fwd(ctypes.addressof(g), x.data_ptr(), y.data_ptr(), 1, None, 0,
                            _device.stream())
     assert st == _lib.CT_ERR_WORKSPACE
+
+
+def _edge_op(shape, nv, **kw):
+    ang = np.linspace(0, np.pi, nv, endpoint=False)
+    import warnings
+
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        H = linop.XRayTransform2D(shape, ang, **kw)
+    return H, ctref.xray2d_defaults(shape, ang, **kw)
+
+
+@pytest.mark.parametrize("case", [
+    dict(shape=(1, 1), nv=1, det_count=3),                 # one pixel, one view
+    dict(shape=(8, 600), nv=7),                            # three strip chunks, a partial tile row
+    dict(shape=(20, 20), nv=9, dx=2.0, det_count=60),      # pixels 2.8 bins wide: long spans, general walk
+], ids=["1x1", "8x600", "dx2"])
+def test_edge_geometries_vs_oracle(cuda, case):
+    """Against the oracle with the reference's float32 arithmetic to 1e-5.
+    Against float64 only where the weight model is continuous (projected
+    pixels at most one bin wide: wider ones jump from weight 0 to 1/width as
+    Px crosses an integer, so float32 and float64 Px disagree by whole
+    pixels), to 1e-4: float32 Px is rounded to ~|Px| 6e-8 bins."""
+    case = dict(case)
+    shape, nv = case.pop("shape"), case.pop("nv")
+    H, g = _edge_op(shape, nv, **case)
+    rng = np.random.default_rng(5)
+    x = rng.random(shape).astype(np.float32)
+    y = rng.random(H.output_shape).astype(np.float32)
+    ax = H.project(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    aty = H.back_project(torch.from_numpy(y).to(cuda)).cpu().numpy()
+    assert ctref.rel_l2(ax, ctref.xray2d_project(x, g, np.float32)) <= 1e-5
+    assert ctref.rel_l2(aty, ctref.xray2d_back_project(y, g, np.float32)) <= 1e-5
+    if H.max_width <= 1.0 + 1e-6:
+        assert ctref.rel_l2(ax, ctref.xray2d_project(x, g, np.float64)) <= 1e-4
+        assert ctref.rel_l2(aty, ctref.xray2d_back_project(y, g, np.float64)) <= 1e-4
+    lhs, rhs = float((ax.astype(np.float64) * y).sum()), float((x.astype(np.float64) * aty).sum())
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+
+
+def test_far_detector_offset_general_floor(cuda):
+    """|Px| near 3e6 (beyond the fast floor's 2^21): every tile takes the
+    general floor path.  Float32 Px resolves only 1/4 bin there, so the check
+    is against the oracle with the reference's float32 weights."""
+    H, g = _edge_op((24, 24), 3, y0=-3_000_000.0, det_count=3_000_040)
+    rng = np.random.default_rng(6)
+    x = rng.random((24, 24)).astype(np.float32)
+    ax = H.project(torch.from_numpy(x).to(cuda)).cpu().numpy()
+    ref = ctref.xray2d_project(x, g, np.float32)
+    assert np.abs(ref).sum() > 0  # the image lands on the detector
+    assert ctref.rel_l2(ax, ref) <= 1e-5
+    ys = np.zeros(H.output_shape, np.float32)
+    ys[:, 2_999_950:3_000_040] = rng.random((3, 90)).astype(np.float32)
+    aty = H.back_project(torch.from_numpy(ys).to(cuda)).cpu().numpy()
+    assert ctref.rel_l2(aty, ctref.xray2d_back_project(ys, g, np.float32)) <= 1e-5
+
+
+def test_too_wide_pixels_rejected(cuda):
+    """Projected pixels wider than the forward's partial rows hold (about 4
+    bins: dx = 4 gives 5.7) are refused with CT_ERR_UNSUPPORTED, not
+    computed wrongly."""
+    H, _ = _edge_op((16, 16), 4, dx=4.0, det_count=100)
+    with pytest.raises(_lib.CtError, match="too large"):
+        H.project(torch.zeros((16, 16), device=cuda))
