@@ -144,17 +144,19 @@ __device__ __forceinline__ unsigned long long fsub2(unsigned long long a, unsign
 // walk_row_fast: |Pdx1| < 0.999 and |Px| < 2^21, so consecutive keys differ
 // by 0 or 1.  The Px, floor, distance and 1 - w steps of two consecutive
 // pixels run as paired instructions (each element rounded as the scalar
-// step: Px's products stay scalar), then the two pixels enter the carry in
+// step), then the two pixels enter the carry in
 // walk order: when the key advances, the current bin's sum is complete and
 // the next bin's (1-w) x sum becomes the current one.  The floor uses the
 // lane's own magic number kMagic + lane LS (an integer below 2^24, so
 // t = magic + floor(px) is still exact), which makes the float bits of t the
 // lane's partial-row index plus a constant: the store address is
 // row_addr + 4 bits(t) with row_addr = warp_rows_addr - 4 (kMagicBits + base),
-// the same for every lane of the warp.
+// the same for every lane of the warp.  pj[j] = Pdx1 * (j0 + j), the
+// rounded column products of the warp's tile (a per-warp shared table, read
+// by broadcast 16-byte loads).
 template <bool REV>
-__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, float magic, float pd1,
-                                              float fj0, float R, float inv_width) {
+__device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t row_addr, float magic,
+                                              const float* __restrict__ pj, float R, float inv_width) {
   const unsigned long long R2 = pk2(R, R);
   const unsigned long long M2 = pk2(magic, magic), M12 = pk2(magic - 1.0f, magic - 1.0f);
   const unsigned long long one2 = pk2(1.0f, 1.0f);
@@ -162,31 +164,44 @@ __device__ __forceinline__ void walk_row_fast(const float (&xr)[kT], uint32_t ro
   int tbp = 0;
   auto step = [&](int tb, float w, float omw, float x, bool first) {
     if (first) tbp = tb;
-    const bool next = tb != tbp;  // the key advanced by one bin
+    const bool next = tb != tbp;  // the key advanced by one bin: bin tbp is complete
+    if (next) st_shared(row_addr + 4u * (uint32_t)tbp, A);
     const float a0 = next ? B : A;
     const float b0 = next ? 0.0f : B;
     A = fmaf(w, x, a0);
     B = fmaf(omw, x, b0);
     tbp = tb;
-    st_shared(row_addr + 4u * (uint32_t)tb, A);
   };
+  // Columns (2h, 2h+1) are evaluated as one pair (lower column in the low
+  // half); REV steps the pair's upper column first.
 #pragma unroll
-  for (int t = 0; t < kT; t += 2) {
-    const int ja = REV ? kT - 1 - t : t;
-    const int jb = REV ? kT - 2 - t : t + 1;
-    const unsigned long long px2 =
-        fadd2(R2, pk2(ct::fmul(pd1, fj0 + (float)ja), ct::fmul(pd1, fj0 + (float)jb)));
-    const unsigned long long t2 = fadd2_rd(px2, M2);
-    const unsigned long long d2 = fsub2(fsub2(t2, M12), px2);
-    float ta, tb, da, db;
-    upk2(t2, ta, tb);
-    upk2(d2, da, db);
-    const float wa = __saturatef(ct::fmul(da, inv_width)), wb = __saturatef(ct::fmul(db, inv_width));
-    float oa, ob;
-    upk2(fsub2(one2, pk2(wa, wb)), oa, ob);
-    step(__float_as_int(ta), wa, oa, xr[ja], t == 0);
-    step(__float_as_int(tb), wb, ob, xr[jb], false);
+  for (int q = 0; q < kT / 4; ++q) {
+    const int qq = REV ? kT / 4 - 1 - q : q;
+    const float4 p4 = *reinterpret_cast<const float4*>(pj + 4 * qq);
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int h = REV ? 1 - hh : hh;
+      const int jl = 4 * qq + 2 * h;
+      const unsigned long long px2 = fadd2(R2, h ? pk2(p4.z, p4.w) : pk2(p4.x, p4.y));
+      const unsigned long long t2 = fadd2_rd(px2, M2);
+      const unsigned long long d2 = fsub2(fsub2(t2, M12), px2);
+      float tl, th, dl, dh;
+      upk2(t2, tl, th);
+      upk2(d2, dl, dh);
+      const float wl = __saturatef(ct::fmul(dl, inv_width)), wh = __saturatef(ct::fmul(dh, inv_width));
+      float ol, oh;
+      upk2(fsub2(one2, pk2(wl, wh)), ol, oh);
+      const bool first = q == 0 && hh == 0;
+      if (!REV) {
+        step(__float_as_int(tl), wl, ol, xr[jl], first);
+        step(__float_as_int(th), wh, oh, xr[jl + 1], false);
+      } else {
+        step(__float_as_int(th), wh, oh, xr[jl + 1], first);
+        step(__float_as_int(tl), wl, ol, xr[jl], false);
+      }
+    }
   }
+  st_shared(row_addr + 4u * (uint32_t)tbp, A);
   st_shared(row_addr + 4u * (uint32_t)tbp + 4u, B);
 }
 
@@ -254,6 +269,7 @@ struct FwdViewSmem {
   float width[kMaxVpc];
   int2 strip[kMaxVpc];         // strip base bin, strip span
   int4 tile[kMaxVpc][kFW];     // per tile: base bin, span (0 = nothing to do), strip offset, fast floor
+  float pj[kFW][kT];           // per warp: Pdx1 * j over its tile's columns for the current view
 };
 
 // Per-view parameters of a forward CTA's run of views, one lane per (view,
@@ -399,10 +415,15 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
         const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
         if (tp.w) {
           const uint32_t row_addr = ct::smem_u32(wpart) - 4u * (uint32_t)(kMagicBits + base);
+          // the tile's column products, one lane per column (the previous
+          // view's reads ended before the CTA barrier)
+          float* pj = vs->pj[warp];
+          pj[lane] = ct::fmul(pv.z, fj0 + (float)lane);
+          __syncwarp();
           if (pv.z >= 0.0f)
-            walk_row_fast<false>(xr, row_addr, magic, pv.z, fj0, R, pv.w);
+            walk_row_fast<false>(xr, row_addr, magic, pj, R, pv.w);
           else
-            walk_row_fast<true>(xr, row_addr, magic, pv.z, fj0, R, pv.w);
+            walk_row_fast<true>(xr, row_addr, magic, pj, R, pv.w);
         } else {
           const ViewParams p{pv.x, pv.y, pv.z, vs->width[vi], pv.w};
           if (p.pd1 >= 0.0f)
