@@ -13,7 +13,9 @@
 //     direction in which k never decreases, carrying the running sums of the
 //     current bin and the next in registers and storing finished bins in its
 //     shared-memory partial row.  The 32 partial rows are summed in row
-//     order, the 8 tiles in tile order, giving the strip's bins for the view.
+//     order into the tile's bins; the warps need no barrier until every view
+//     of the run is done, then the 8 tiles are summed in tile order into the
+//     strip's bins of each view.
 //   k_proj2d_fwd_gather  sums, per detector bin, the strips that cover it in
 //     strip order.
 //   No atomics: the result is bit-reproducible.
@@ -256,14 +258,14 @@ __device__ __forceinline__ void strip_bins(const ViewParams& p, int i0, int c0, 
 
 // Shared memory of k_proj2d_fwd_strips: a 16-B header (the copy barrier),
 // then one region used twice: first the 32 x kRS strip, then, once every lane
-// holds its tile row in registers, the partial rows [kFW][32][LS] and two
-// slot buffers [2][kFW][cspan] (one per view parity); then the per-view
-// parameters of the CTA's run of views (FwdViewSmem).
-__host__ __device__ constexpr size_t fwd_region_floats(int LS, int cspan) {
-  return (size_t)kT * kRS > (size_t)kFW * kT * LS + 2u * kFW * cspan ? (size_t)kT * kRS
-                                                                     : (size_t)kFW * kT * LS + 2u * kFW * cspan;
+// holds its tile row in registers, the partial rows [kFW][32][LS]; then the
+// tiles' bins of every view of the CTA's run [kMaxVpc][kFW][L]; then the
+// per-view parameters of the run (FwdViewSmem).
+__host__ __device__ constexpr size_t fwd_region_floats(int LS) {
+  return (size_t)kT * kRS > (size_t)kFW * kT * LS ? (size_t)kT * kRS : (size_t)kFW * kT * LS;
 }
 constexpr int kMaxVpc = 16;  // views per forward CTA (upper bound of the plan's vpc)
+__host__ __device__ constexpr size_t fwd_tbins_floats(int L) { return (size_t)kMaxVpc * kFW * L; }
 struct FwdViewSmem {
   float4 pv[kMaxVpc];          // pxmin, Pdx0, Pdx1, 1/width
   float width[kMaxVpc];
@@ -276,7 +278,7 @@ struct FwdViewSmem {
 // tile): the view's table entry, the strip's bins and each tile's base bin,
 // span, offset in the strip and floor path (every lane of a warp would
 // otherwise compute the same values for its tile).  A span that does not fit
-// the partial rows or the slots (impossible for a table from
+// the partial rows or the strip's bins (impossible for a table from
 // ct_proj2d_views) sets bit 0 of the error word and skips the tile.
 __device__ __forceinline__ void fwd_view_params(const FwdArgs& a, FwdViewSmem* vs, int i0, int c0, int ch) {
   const int vbeg = blockIdx.y * a.vpc;
@@ -320,8 +322,8 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* strip = reinterpret_cast<float*>(smem_raw + 16);            // [32][kRS]
   float* part = strip;                                               // [kFW][32][LS]
-  float* slots = part + kFW * kT * LS;                             // [2][kFW][cspan]
-  FwdViewSmem* vs = reinterpret_cast<FwdViewSmem*>(strip + fwd_region_floats(LS, a.cspan));
+  float* tbins = strip + fwd_region_floats(LS);                      // [kMaxVpc][kFW][L]
+  FwdViewSmem* vs = reinterpret_cast<FwdViewSmem*>(tbins + fwd_tbins_floats(a.L));
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int s = blockIdx.x;
@@ -382,113 +384,109 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       xr[4 * q + 3] = f.w;
     }
   }
-  __syncthreads();  // the strip is dead from here: its bytes become rows and slots
-  {
-    const int nz4 = (kFW * kT * LS + 2 * kFW * a.cspan) / 4;  // rows and slots are whole float4s
-    float4* z4 = reinterpret_cast<float4*>(part);
-    for (int e = tid; e < nz4; e += kFW * 32) z4[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  }
-  __syncthreads();
-
+  __syncthreads();  // the strip is dead from here: its bytes become partial rows
+  // From here to the combine every warp works alone on its tile: its partial
+  // rows, its column products and its rows of the tile bins.
   float* wpart = part + warp * kT * LS;
+  {
+    float4* z4 = reinterpret_cast<float4*>(wpart);  // kT * LS floats per warp: whole float4s (kT = 32)
+    for (int e = lane; e < kT * LS / 4; e += 32) z4[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  __syncwarp();
+
   float* mp = wpart + lane * LS;
   const float magic = kMagic + (float)(lane * LS);  // exact: an integer below 2^24
-  // Slot rows hold each tile's bins at strip-relative offsets and zeros
-  // elsewhere, so the tile combine needs no range checks.  A warp clears what
-  // it wrote into a slot buffer when it reuses that buffer two views later
-  // (after the barrier that ends the combine reading it).
-  int zoff0 = 0, zspan0 = 0, zoff1 = 0, zspan1 = 0;
   for (int v = vbeg; v < vend; ++v) {
-    const int vi = v - vbeg, par = vi & 1;
-    const float4 pv = vs->pv[vi];
+    const int vi = v - vbeg;
     const int4 tp = vs->tile[vi][warp];
-    float* slot = slots + (par * kFW + warp) * a.cspan;
-    {
-      const int zo = par ? zoff1 : zoff0, zs = par ? zspan1 : zspan0;
-      for (int k = lane; k < zs; k += 32) slot[zo + k] = 0.0f;
+    const int span = tp.y;
+    if (span == 0) continue;  // warp-uniform
+    const float4 pv = vs->pv[vi];
+    const int base = tp.x;
+    const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
+    if (tp.w) {
+      const uint32_t row_addr = ct::smem_u32(wpart) - 4u * (uint32_t)(kMagicBits + base);
+      // the tile's column products, one lane per column (the previous
+      // view's reads ended before the warp barrier that closed it)
+      float* pj = vs->pj[warp];
+      pj[lane] = ct::fmul(pv.z, fj0 + (float)lane);
+      __syncwarp();
+      if (pv.z >= 0.0f)
+        walk_row_fast<false>(xr, row_addr, magic, pj, R, pv.w);
+      else
+        walk_row_fast<true>(xr, row_addr, magic, pj, R, pv.w);
+    } else {
+      const ViewParams p{pv.x, pv.y, pv.z, vs->width[vi], pv.w};
+      if (p.pd1 >= 0.0f)
+        walk_row_gen<false>(xr, mp, p, R, fj0, base);
+      else
+        walk_row_gen<true>(xr, mp, p, R, fj0, base);
     }
-    // ---- this warp's tile --------------------------------------------------
-    const int off = tp.z, span = tp.y;
-    if (span > 0) {
-      {
-        const int base = tp.x;
-        const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
-        if (tp.w) {
-          const uint32_t row_addr = ct::smem_u32(wpart) - 4u * (uint32_t)(kMagicBits + base);
-          // the tile's column products, one lane per column (the previous
-          // view's reads ended before the CTA barrier)
-          float* pj = vs->pj[warp];
-          pj[lane] = ct::fmul(pv.z, fj0 + (float)lane);
-          __syncwarp();
-          if (pv.z >= 0.0f)
-            walk_row_fast<false>(xr, row_addr, magic, pj, R, pv.w);
-          else
-            walk_row_fast<true>(xr, row_addr, magic, pj, R, pv.w);
-        } else {
-          const ViewParams p{pv.x, pv.y, pv.z, vs->width[vi], pv.w};
-          if (p.pd1 >= 0.0f)
-            walk_row_gen<false>(xr, mp, p, R, fj0, base);
-          else
-            walk_row_gen<true>(xr, mp, p, R, fj0, base);
-        }
-        __syncwarp();
-        // Bins 0..31 of the tile: lane = bin, rows summed in row order; the
-        // read entries are zeroed again.
-        if (lane < span) {
-          float acc = 0.0f;
-          float* q = wpart + lane;
+    __syncwarp();
+    // The tile's bins for this view: lane = bin, rows summed in row order
+    // (the read entries are zeroed again).
+    float* tb = tbins + ((size_t)vi * kFW + warp) * a.L;
+    if (lane < span) {
+      float acc = 0.0f;
+      float* q = wpart + lane;
 #pragma unroll
+      for (int r = 0; r < kT; ++r) {
+        acc += q[r * LS];
+        q[r * LS] = 0.0f;
+      }
+      tb[lane] = acc;
+    }
+    if (span > 32) {
+      if (span <= 35) {
+        // at most 3 more bins: lane = row, then a fixed butterfly over rows
+        float* q = mp + 32;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          if (32 + e < span) {  // warp-uniform
+            float t = q[e];
+            q[e] = 0.0f;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
+            if (lane == 0) tb[32 + e] = t;
+          }
+        }
+      } else {
+        for (int k = 32 + lane; k < span; k += 32) {
+          float acc = 0.0f;
+          float* q = wpart + k;
+#pragma unroll 8
           for (int r = 0; r < kT; ++r) {
             acc += q[r * LS];
             q[r * LS] = 0.0f;
           }
-          slot[off + lane] = acc;
-        }
-        if (span > 32) {
-          if (span <= 35) {
-            // at most 3 more bins: lane = row, then a fixed butterfly over rows
-            float* q = mp + 32;
-#pragma unroll
-            for (int e = 0; e < 3; ++e) {
-              if (32 + e < span) {  // warp-uniform
-                float t = q[e];
-                q[e] = 0.0f;
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
-                if (lane == 0) slot[off + 32 + e] = t;
-              }
-            }
-          } else {
-            for (int k = 32 + lane; k < span; k += 32) {
-              float acc = 0.0f;
-              float* q = wpart + k;
-#pragma unroll 8
-              for (int r = 0; r < kT; ++r) {
-                acc += q[r * LS];
-                q[r * LS] = 0.0f;
-              }
-              slot[off + k] = acc;
-            }
-          }
+          tb[k] = acc;
         }
       }
     }
-    if (par) {
-      zoff1 = off;
-      zspan1 = span;
-    } else {
-      zoff0 = off;
-      zspan0 = span;
-    }
-    __syncthreads();
-    // ---- combine the 8 tiles in tile order into the strip's bins ----------
-    const float* s0 = slots + par * kFW * a.cspan;
-    float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + v) * a.cspan;
-    const int n = min(vs->strip[vi].y, a.cspan);
-    for (int k = tid; k < n; k += kFW * 32) {
-      float acc = s0[k];
+    __syncwarp();  // rows zeroed (lane = bin) before the next walk writes them (lane = row)
+  }
+  __syncthreads();
+  // ---- combine the 8 tiles in tile order into the strip's bins, every view
+  // of the run: warp w takes views w, w + 8; bin k of the strip gets the
+  // tiles whose span covers it ------------------------------------------------
+  for (int vi = warp; vi < vend - vbeg; vi += kFW) {
+    int toff[kFW], tspan[kFW];
 #pragma unroll
-      for (int w = 1; w < kFW; ++w) acc += s0[w * a.cspan + k];
+    for (int w = 0; w < kFW; ++w) {
+      const int4 tp = vs->tile[vi][w];
+      toff[w] = tp.z;
+      tspan[w] = tp.y;
+    }
+    const float* tb = tbins + (size_t)vi * kFW * a.L;
+    float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + vbeg + vi) * a.cspan;
+    const int n = min(vs->strip[vi].y, a.cspan);
+    for (int k = lane; k < n; k += 32) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int w = 0; w < kFW; ++w) {
+        const int o = k - toff[w];
+        if ((unsigned)o < (unsigned)tspan[w]) acc += tb[w * a.L + o];
+      }
       po[k] = acc;
     }
   }
@@ -710,8 +708,8 @@ int* errflag_ptr() {
   return cached[dev];
 }
 
-size_t fwd_smem_bytes(int LS, int cspan) {
-  return 16 + sizeof(float) * fwd_region_floats(LS, cspan) + sizeof(FwdViewSmem);
+size_t fwd_smem_bytes(int LS, int L) {
+  return 16 + sizeof(float) * (fwd_region_floats(LS) + fwd_tbins_floats(L)) + sizeof(FwdViewSmem);
 }
 
 size_t adj_smem_bytes(int W) {
@@ -770,7 +768,7 @@ Proj2dPlan proj2d_plan_sched(const ct_geom2d* g, int batch, Sched2d sc) {
                      : (int)std::min<long>(kMaxVpc, std::max<long>(2, (work + kFwdTargetCtas - 1) / kFwdTargetCtas));
   p.fwd_groups = (g->n_views + p.vpc - 1) / p.vpc;
   p.fwd_bytes = round_up((size_t)batch * p.n_strips * g->n_views * p.cspan * sizeof(float), 256);
-  p.fwd_smem = fwd_smem_bytes(p.LS, p.cspan);
+  p.fwd_smem = fwd_smem_bytes(p.LS, p.L);
   p.W = (int)floorf((float)(kAJ - 1) * mw + 1.01f) + 3;
   p.adj_smem = adj_smem_bytes(p.W);
   p.adj_gx = (g->cols + kAJ - 1) / kAJ;
