@@ -46,7 +46,7 @@ constexpr int kFW = 8;          // warps of a forward CTA (one tile each)
 constexpr int kRS = kCW + 4;    // strip row stride in floats: 16-B rows, conflict-free LDS.128
 constexpr int kFwdTargetCtas = 1824;
 constexpr int kLSDefault = 47;  // partial-row stride when projected pixels are at most one bin wide
-constexpr int kGL = 8;          // strips read per round by a forward gather warp
+constexpr int kGL = 16;         // strips read per round by a forward gather warp
 constexpr int kAI = 16;         // adjoint tile rows
 constexpr int kAJ = 64;         // adjoint tile columns
 constexpr int kAPX = 4;         // pixels per adjoint thread
@@ -92,6 +92,13 @@ __device__ __forceinline__ void weight_floor(float px, float width, float inv_wi
 
 __device__ __forceinline__ void st_shared(uint32_t addr, float v) {
   asm volatile("st.shared.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
+// Reads a shared float and leaves 0 in its place (one instruction).
+__device__ __forceinline__ float xchg_zero_shared(uint32_t addr) {
+  uint32_t r;
+  asm volatile("atom.shared.exch.b32 %0, [%1], 0;" : "=r"(r) : "r"(addr) : "memory");
+  return __uint_as_float(r);
 }
 
 __device__ __forceinline__ float2 ld_shared2(uint32_t addr) {
@@ -423,28 +430,24 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
         walk_row_gen<true>(xr, mp, p, R, fj0, base);
     }
     __syncwarp();
-    // The tile's bins for this view: lane = bin, rows summed in row order
-    // (the read entries are zeroed again).
+    // The tile's bins for this view: lane = bin, rows summed in row order;
+    // each entry is read and zeroed by one shared exchange.
     float* tb = tbins + ((size_t)vi * kFW + warp) * a.L;
     if (lane < span) {
       float acc = 0.0f;
-      float* q = wpart + lane;
+      const uint32_t q = ct::smem_u32(wpart + lane);
 #pragma unroll
-      for (int r = 0; r < kT; ++r) {
-        acc += q[r * LS];
-        q[r * LS] = 0.0f;
-      }
+      for (int r = 0; r < kT; ++r) acc += xchg_zero_shared(q + 4u * (uint32_t)(r * LS));
       tb[lane] = acc;
     }
     if (span > 32) {
       if (span <= 35) {
         // at most 3 more bins: lane = row, then a fixed butterfly over rows
-        float* q = mp + 32;
+        const uint32_t q = ct::smem_u32(mp + 32);
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
           if (32 + e < span) {  // warp-uniform
-            float t = q[e];
-            q[e] = 0.0f;
+            float t = xchg_zero_shared(q + 4u * (uint32_t)e);
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) t += __shfl_xor_sync(0xffffffffu, t, d);
             if (lane == 0) tb[32 + e] = t;
@@ -453,12 +456,9 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       } else {
         for (int k = 32 + lane; k < span; k += 32) {
           float acc = 0.0f;
-          float* q = wpart + k;
+          const uint32_t q = ct::smem_u32(wpart + k);
 #pragma unroll 8
-          for (int r = 0; r < kT; ++r) {
-            acc += q[r * LS];
-            q[r * LS] = 0.0f;
-          }
+          for (int r = 0; r < kT; ++r) acc += xchg_zero_shared(q + 4u * (uint32_t)(r * LS));
           tb[k] = acc;
         }
       }
