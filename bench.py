@@ -388,8 +388,8 @@ def run_gpu(args):
     e2e_dev_diff = float((xr.to(dev) - x_dev).norm() / x_dev.norm())
 
     # ---- roofline: the forward projector, live CUDA events ---------------------
-    fwd_bytes, _ = A.workspace_bytes(1)
-    pws = _device.workspace(fwd_bytes)
+    fwd_bytes, adj_bytes = A.workspace_bytes(1)
+    pws = _device.workspace(max(fwd_bytes, adj_bytes))
     sino = torch.empty((c.n_views, c.det_count), device=dev)
     img = x_dev.clone()
     bp = torch.empty_like(img)

@@ -20,11 +20,11 @@
 //     strip order.
 //   No atomics: the result is bit-reproducible.
 // Adjoint (A^T), k_proj2d_adj: pixel-driven gather with the same weights.  A
-//   CTA owns a 16x64 pixel tile; per run of 32 views it stages the tile's
+//   CTA owns a 32x64 pixel tile; per run of 32 views it stages the tile's
 //   detector windows in shared memory as (y[k], y[k+1]) pairs (zero outside
-//   the detector), then each thread accumulates its 4 pixels over the views
-//   in view order.  Small images split the views into a fixed number of
-//   runs whose partial images are summed in run order.
+//   the detector), then each thread accumulates its 2 x 4 pixels over the
+//   views in view order.  Small images split the views into a fixed number
+//   of runs whose partial images are summed in run order.
 //
 // floor(Px) is taken with one round-down float add of 1.5*2^23 (exact for
 // |Px| < 2^22, checked per tile and view, with a floorf path otherwise):
@@ -47,9 +47,11 @@ constexpr int kRS = kCW + 4;    // strip row stride in floats: 16-B rows, confli
 constexpr int kFwdTargetCtas = 1824;
 constexpr int kLSDefault = 47;  // partial-row stride when projected pixels are at most one bin wide
 constexpr int kGL = 16;         // strips read per round by a forward gather warp
-constexpr int kAI = 16;         // adjoint tile rows
+constexpr int kAI = 32;         // adjoint tile rows
 constexpr int kAJ = 64;         // adjoint tile columns
-constexpr int kAPX = 4;         // pixels per adjoint thread
+constexpr int kAPX = 4;         // columns per adjoint thread
+constexpr int kAR = 2;          // rows per adjoint thread
+constexpr int kAdjThreads = 256;  // adjoint CTA: 32 x 64 pixels = kAdjThreads x kAR x kAPX
 constexpr int kAVC = 32;        // views staged per adjoint run
 constexpr int kAdjTargetCtas = 1216;  // 152 SMs x 8: view splits until the CTAs balance over the SMs
 constexpr int kAdjMinViewsPerSplit = 16;
@@ -562,49 +564,63 @@ struct AdjArgs {
 // pair of key k lives at shared address off + 8 (kMagicBits + k) for the
 // float bits kMagicBits + k of kMagic + k.
 
-// adj_view_fast with the Px, floor and distance steps of two pixels per
-// paired instruction (bit-identical to the scalar form).
-__device__ __forceinline__ void adj_view_fast2(const float4 pv, uint32_t off, float fi, const float (&fj)[kAPX],
-                                               float (&acc)[kAPX]) {
-  const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
-  const unsigned long long R2 = pk2(R, R);
+// adj_view_fast with the Px, floor, distance and 1 - w steps of two pixels
+// per paired instruction (bit-identical to the scalar form); the column
+// products Pdx1 * j are shared by the thread's rows.
+__device__ __forceinline__ void adj_view_fast2(const float4 pv, uint32_t off, const float (&fi)[kAR],
+                                               const float (&fj)[kAPX], float (&acc)[kAR][kAPX]) {
   const unsigned long long M2 = pk2(kMagic, kMagic), M12 = pk2(kMagic - 1.0f, kMagic - 1.0f);
+  const unsigned long long one2 = pk2(1.0f, 1.0f);
+  float pj[kAPX];
 #pragma unroll
-  for (int h = 0; h < kAPX / 2; ++h) {
-    const unsigned long long px2 =
-        fadd2(R2, pk2(ct::fmul(pv.z, fj[2 * h]), ct::fmul(pv.z, fj[2 * h + 1])));
-    const unsigned long long t2 = fadd2_rd(px2, M2);
-    const unsigned long long d2 = fsub2(fsub2(t2, M12), px2);
-    float t0, t1, d0, d1;
-    upk2(t2, t0, t1);
-    upk2(d2, d0, d1);
-    const float w0 = __saturatef(ct::fmul(d0, pv.w)), w1 = __saturatef(ct::fmul(d1, pv.w));
-    const float2 y0 = ld_shared2(off + 8u * (uint32_t)__float_as_int(t0));
-    const float2 y1 = ld_shared2(off + 8u * (uint32_t)__float_as_int(t1));
-    acc[2 * h] = fmaf(y0.x, w0, acc[2 * h]);
-    acc[2 * h] = fmaf(y0.y, ct::fsub(1.0f, w0), acc[2 * h]);
-    acc[2 * h + 1] = fmaf(y1.x, w1, acc[2 * h + 1]);
-    acc[2 * h + 1] = fmaf(y1.y, ct::fsub(1.0f, w1), acc[2 * h + 1]);
+  for (int q = 0; q < kAPX; ++q) pj[q] = ct::fmul(pv.z, fj[q]);
+#pragma unroll
+  for (int r = 0; r < kAR; ++r) {
+    const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi[r]));
+    const unsigned long long R2 = pk2(R, R);
+#pragma unroll
+    for (int h = 0; h < kAPX / 2; ++h) {
+      const unsigned long long px2 = fadd2(R2, pk2(pj[2 * h], pj[2 * h + 1]));
+      const unsigned long long t2 = fadd2_rd(px2, M2);
+      const unsigned long long d2 = fsub2(fsub2(t2, M12), px2);
+      float t0, t1, d0, d1;
+      upk2(t2, t0, t1);
+      upk2(d2, d0, d1);
+      const float w0 = __saturatef(ct::fmul(d0, pv.w)), w1 = __saturatef(ct::fmul(d1, pv.w));
+      float o0, o1;
+      upk2(fsub2(one2, pk2(w0, w1)), o0, o1);
+      const float2 y0 = ld_shared2(off + 8u * (uint32_t)__float_as_int(t0));
+      const float2 y1 = ld_shared2(off + 8u * (uint32_t)__float_as_int(t1));
+      acc[r][2 * h] = fmaf(y0.x, w0, acc[r][2 * h]);
+      acc[r][2 * h] = fmaf(y0.y, o0, acc[r][2 * h]);
+      acc[r][2 * h + 1] = fmaf(y1.x, w1, acc[r][2 * h + 1]);
+      acc[r][2 * h + 1] = fmaf(y1.y, o1, acc[r][2 * h + 1]);
+    }
   }
 }
 
 __device__ __forceinline__ void adj_view_gen(const float4 pv, float width, int base, const float2* __restrict__ wy,
-                                             float fi, const float (&fj)[kAPX], float (&acc)[kAPX]) {
-  const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi));
+                                             const float (&fi)[kAR], const float (&fj)[kAPX],
+                                             float (&acc)[kAR][kAPX]) {
 #pragma unroll
-  for (int q = 0; q < kAPX; ++q) {
-    const float px = ct::fadd(R, ct::fmul(pv.z, fj[q]));
-    int key;
-    float w;
-    weight_floor(px, width, pv.w, base, key, w);
-    const float2 y = wy[key];
-    acc[q] = fmaf(y.x, w, acc[q]);
-    acc[q] = fmaf(y.y, ct::fsub(1.0f, w), acc[q]);
+  for (int r = 0; r < kAR; ++r) {
+    const float R = ct::fadd(pv.x, ct::fmul(pv.y, fi[r]));
+#pragma unroll
+    for (int q = 0; q < kAPX; ++q) {
+      const float px = ct::fadd(R, ct::fmul(pv.z, fj[q]));
+      int key;
+      float w;
+      weight_floor(px, width, pv.w, base, key, w);
+      const float2 y = wy[key];
+      acc[r][q] = fmaf(y.x, w, acc[r][q]);
+      acc[r][q] = fmaf(y.y, ct::fsub(1.0f, w), acc[r][q]);
+    }
   }
 }
 
-// grid = (ceil(cols/64), ceil(rows/16), batch*nsplit), block = 256.
-__global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
+// grid = (ceil(cols/64), ceil(rows/32), batch*nsplit), block = 256: thread
+// (ty, tx) owns rows ty and ty + 16 at columns tx + 16 q of the 32 x 64 tile.
+__global__ void __launch_bounds__(kAdjThreads) k_proj2d_adj(const AdjArgs a) {
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sy = reinterpret_cast<float2*>(smem_raw);          // [kAVC][W]
@@ -614,20 +630,24 @@ __global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
   int* sf = sb + kAVC;                                       // [kAVC] 1 = fast floor, -1 = skip
   uint32_t* so = reinterpret_cast<uint32_t*>(sf + kAVC);     // [kAVC] fast-path address offset
 
+  constexpr int kWarps = kAdjThreads / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int z = blockIdx.z;
   const int b = z / a.nsplit, sidx = z - b * a.nsplit;
   const int vbeg = sidx * a.per_split, vend = min(a.nv, vbeg + a.per_split);
   const int i0 = blockIdx.y * kAI, j0 = blockIdx.x * kAJ;
   const int ty = tid >> 4, tx = tid & 15;
-  const int i = i0 + ty;
-  const float fi = (float)i;
+  float fi[kAR];
+#pragma unroll
+  for (int r = 0; r < kAR; ++r) fi[r] = (float)(i0 + ty + (kAI / kAR) * r);
   float fj[kAPX];
 #pragma unroll
   for (int q = 0; q < kAPX; ++q) fj[q] = (float)(j0 + tx + 16 * q);
-  float acc[kAPX];
+  float acc[kAR][kAPX];
 #pragma unroll
-  for (int q = 0; q < kAPX; ++q) acc[q] = 0.0f;
+  for (int r = 0; r < kAR; ++r)
+#pragma unroll
+    for (int q = 0; q < kAPX; ++q) acc[r][q] = 0.0f;
   const float* yb = a.sino + (size_t)b * a.nv * a.det;
 
   for (int a0 = vbeg; a0 < vend; a0 += kAVC) {
@@ -651,7 +671,7 @@ __global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
       so[tid] = ct::smem_u32(sy + tid * a.W) - 8u * (uint32_t)(kMagicBits + base);
     }
     __syncthreads();
-    for (int v = warp; v < n; v += 8) {
+    for (int v = warp; v < n; v += kWarps) {
       const float* yr = yb + (size_t)(a0 + v) * a.det;
       const int base = sb[v];
       float2* wy = sy + v * a.W;
@@ -671,12 +691,16 @@ __global__ void __launch_bounds__(256) k_proj2d_adj(const AdjArgs a) {
         adj_view_gen(sp[v], sw[v], sb[v], sy + v * a.W, fi, fj, acc);
     }
   }
-  if (i < a.rows) {
-    float* o = a.out + (size_t)sidx * a.split_stride + (size_t)b * a.rows * a.cols + (size_t)i * a.cols;
 #pragma unroll
-    for (int q = 0; q < kAPX; ++q) {
-      const int j = j0 + tx + 16 * q;
-      if (j < a.cols) o[j] = acc[q];
+  for (int r = 0; r < kAR; ++r) {
+    const int i = i0 + ty + (kAI / kAR) * r;
+    if (i < a.rows) {
+      float* o = a.out + (size_t)sidx * a.split_stride + (size_t)b * a.rows * a.cols + (size_t)i * a.cols;
+#pragma unroll
+      for (int q = 0; q < kAPX; ++q) {
+        const int j = j0 + tx + 16 * q;
+        if (j < a.cols) o[j] = acc[r][q];
+      }
     }
   }
 }
@@ -891,7 +915,7 @@ ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   a.skip = skip;
   if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
   dim3 grid(p.adj_gx, p.adj_gy, batch * p.nsplit);
-  k_proj2d_adj<<<grid, 256, p.adj_smem, s>>>(a);
+  k_proj2d_adj<<<grid, kAdjThreads, p.adj_smem, s>>>(a);
   return launch_check("k_proj2d_adj");
 }
 
