@@ -20,9 +20,9 @@
 //     strip order.
 //   No atomics: the result is bit-reproducible.
 // Adjoint (A^T), k_proj2d_adj: pixel-driven gather with the same weights.  A
-//   CTA owns a 32x64 pixel tile; per run of 32 views it stages the tile's
+//   CTA owns a 64x64 pixel tile; per run of 32 views it stages the tile's
 //   detector windows in shared memory as (y[k], y[k+1]) pairs (zero outside
-//   the detector), then each thread accumulates its 2 x 4 pixels over the
+//   the detector), then each thread accumulates its 4 x 4 pixels over the
 //   views in view order.  Small images split the views into a fixed number
 //   of runs whose partial images are summed in run order.
 //
@@ -47,11 +47,11 @@ constexpr int kRS = kCW + 4;    // strip row stride in floats: 16-B rows, confli
 constexpr int kFwdTargetCtas = 1824;
 constexpr int kLSDefault = 47;  // partial-row stride when projected pixels are at most one bin wide
 constexpr int kGL = 16;         // strips read per round by a forward gather warp
-constexpr int kAI = 32;         // adjoint tile rows
+constexpr int kAI = 64;         // adjoint tile rows
 constexpr int kAJ = 64;         // adjoint tile columns
 constexpr int kAPX = 4;         // columns per adjoint thread
-constexpr int kAR = 2;          // rows per adjoint thread
-constexpr int kAdjThreads = 256;  // adjoint CTA: 32 x 64 pixels = kAdjThreads x kAR x kAPX
+constexpr int kAR = 4;          // rows per adjoint thread
+constexpr int kAdjThreads = 256;  // adjoint CTA: 64 x 64 pixels = kAdjThreads x kAR x kAPX
 constexpr int kAVC = 32;        // views staged per adjoint run
 constexpr int kAdjTargetCtas = 1216;  // 152 SMs x 8: view splits until the CTAs balance over the SMs
 constexpr int kAdjMinViewsPerSplit = 16;
@@ -618,8 +618,9 @@ __device__ __forceinline__ void adj_view_gen(const float4 pv, float width, int b
   }
 }
 
-// grid = (ceil(cols/64), ceil(rows/32), batch*nsplit), block = 256: thread
-// (ty, tx) owns rows ty and ty + 16 at columns tx + 16 q of the 32 x 64 tile.
+// grid = (ceil(cols/64), ceil(rows/64), batch*nsplit), block = 256: thread
+// (ty, tx) owns rows ty + 16 r (r < kAR) at columns tx + 16 q (q < kAPX) of
+// the 64 x 64 tile.
 __global__ void __launch_bounds__(kAdjThreads) k_proj2d_adj(const AdjArgs a) {
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -793,7 +794,7 @@ Proj2dPlan proj2d_plan_sched(const ct_geom2d* g, int batch, Sched2d sc) {
   p.fwd_groups = (g->n_views + p.vpc - 1) / p.vpc;
   p.fwd_bytes = round_up((size_t)batch * p.n_strips * g->n_views * p.cspan * sizeof(float), 256);
   p.fwd_smem = fwd_smem_bytes(p.LS, p.L);
-  p.W = (int)floorf((float)(kAJ - 1) * mw + 1.01f) + 3;
+  p.W = (int)floorf((float)(std::max(kAI, kAJ) - 1) * mw + 1.01f) + 3;
   p.adj_smem = adj_smem_bytes(p.W);
   p.adj_gx = (g->cols + kAJ - 1) / kAJ;
   p.adj_gy = (g->rows + kAI - 1) / kAI;
