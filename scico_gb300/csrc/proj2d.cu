@@ -33,6 +33,7 @@
 #include <cstring>
 #include <map>
 #include <tuple>
+#include <vector>
 #include <mutex>
 
 #include "common.cuh"
@@ -1044,9 +1045,15 @@ ct_status ct_proj2d_autotune(const ct_geom2d* g, int32_t batch, float* img, floa
   const long ctas = (long)p0.adj_gx * p0.adj_gy * batch;
   const int ns_max = ct::max_splits(g, ctas);
   const size_t n = (size_t)batch * g->rows * g->cols;
-  float best_a = 0.0f;
+  // Split counts 1, 2, 4, 8, ...: neighbours far enough apart in time that
+  // the choice does not flip between runs on noise (the split count sets the
+  // adjoint's summation order, and with it the rounding a caller sees).
+  // Timings within kTie of the fastest count as ties and go to the fewest
+  // splits (less split memory).
+  constexpr float kTie = 1.03f;
+  std::vector<std::pair<int, float>> cand;
   int last = 0;
-  for (int ns = 1; ns <= ns_max; ++ns) {
+  for (int ns = 1; ns <= ns_max; ns *= 2) {
     const ct::Proj2dPlan p = ct::proj2d_plan_sched(g, batch, ct::Sched2d{0, ns});
     if (p.nsplit == last) continue;  // same split count as the previous candidate
     last = p.nsplit;
@@ -1061,9 +1068,16 @@ ct_status ct_proj2d_autotune(const ct_geom2d* g, int32_t batch, float* img, floa
         },
         reps, s, us);
     if (st != CT_OK) return st;
-    if (best.ns == 0 || us < best_a) {
-      best.ns = p.nsplit;
-      best_a = us;
+    cand.emplace_back(p.nsplit, us);
+  }
+  float fastest = cand.front().second;
+  for (const auto& c : cand) fastest = std::min(fastest, c.second);
+  float best_a = 0.0f;
+  for (const auto& c : cand) {
+    if (c.second <= kTie * fastest) {
+      best.ns = c.first;
+      best_a = c.second;
+      break;
     }
   }
   {
