@@ -496,25 +496,26 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
 }
 
 // sino[b, v, bin] = sum over strips (strip order) of the strip bins covering
-// bin.  A warp takes 32 consecutive bins of one view: its lanes compute the
-// strips' bin ranges (lane = strip), a ballot lists the strips that meet the
-// warp's bins, and the listed strips are read kGL at a time (loads first,
-// then the sums in strip order, zero where a strip misses the bin).
-// grid = (n_views, ceil(det / 256), batch), block = 256.
-__global__ void __launch_bounds__(256)
+// bin.  A warp takes 64 consecutive bins of one view (lane: bins k0 + lane
+// and k0 + 32 + lane): its lanes compute the strips' bin ranges (lane =
+// strip), a ballot lists the strips that meet the warp's bins, and the
+// listed strips are read kGL at a time (loads first, then the sums in strip
+// order, zero where a strip misses the bin).
+// grid = (n_views, ceil(det / 256), batch), block = 128.
+__global__ void __launch_bounds__(128)
     k_proj2d_fwd_gather(const float* __restrict__ part, float* __restrict__ sino,
                         const float* __restrict__ views, int nv, int det, int cspan, int n_chunks,
                         int n_strips, const double* __restrict__ skip) {
   if (skip && *skip != 0.0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int v = blockIdx.x, b = blockIdx.z;
-  const int k0 = blockIdx.y * 256 + warp * 32;
+  const int k0 = blockIdx.y * 256 + warp * 64;
   if (k0 >= det) return;  // whole warp
   const ViewParams p = load_view(views, v);
-  const int bin = k0 + lane;
+  const int bin0 = k0 + lane, bin1 = k0 + 32 + lane;
   const float* pb = part + ((size_t)b * n_strips * nv + v) * cspan;
   const size_t sstride = (size_t)nv * cspan;
-  float acc = 0.0f;
+  float acc0 = 0.0f, acc1 = 0.0f;
   for (int c = 0; c < n_strips; c += 32) {
     const int s = c + lane;
     int base = 0, span = 0;
@@ -523,26 +524,34 @@ __global__ void __launch_bounds__(256)
       strip_bins(p, ti * kT, ch * kCW, base, span);
       span = min(span, cspan);
     }
-    unsigned mask = __ballot_sync(0xffffffffu, s < n_strips && base < k0 + 32 && base + span > k0);
+    unsigned mask = __ballot_sync(0xffffffffu, s < n_strips && base < k0 + 64 && base + span > k0);
     while (mask) {
-      float val[kGL];
+      float v0[kGL], v1[kGL];
 #pragma unroll
       for (int u = 0; u < kGL; ++u) {
-        val[u] = 0.0f;
+        v0[u] = 0.0f;
+        v1[u] = 0.0f;
         if (mask) {
           const int sl = __ffs(mask) - 1;
           mask &= mask - 1u;
           const int bs = __shfl_sync(0xffffffffu, base, sl);
           const int sp = __shfl_sync(0xffffffffu, span, sl);
-          const int off = bin - bs;
-          if ((unsigned)off < (unsigned)sp) val[u] = __ldg(pb + (size_t)(c + sl) * sstride + off);
+          const float* q = pb + (size_t)(c + sl) * sstride;
+          const int o0 = bin0 - bs, o1 = bin1 - bs;
+          if ((unsigned)o0 < (unsigned)sp) v0[u] = __ldg(q + o0);
+          if ((unsigned)o1 < (unsigned)sp) v1[u] = __ldg(q + o1);
         }
       }
 #pragma unroll
-      for (int u = 0; u < kGL; ++u) acc += val[u];
+      for (int u = 0; u < kGL; ++u) {
+        acc0 += v0[u];
+        acc1 += v1[u];
+      }
     }
   }
-  if (bin < det) sino[((size_t)b * nv + v) * det + bin] = acc;
+  float* so = sino + ((size_t)b * nv + v) * det;
+  if (bin0 < det) so[bin0] = acc0;
+  if (bin1 < det) so[bin1] = acc1;
 }
 
 // ---------------------------------------------------------------------------
@@ -894,7 +903,7 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   ct_status st = launch_check("k_proj2d_fwd_strips");
   if (st != CT_OK) return st;
   dim3 g2(g->n_views, (g->det_count + 255) / 256, batch);
-  k_proj2d_fwd_gather<<<g2, 256, 0, s>>>(
+  k_proj2d_fwd_gather<<<g2, 128, 0, s>>>(
       part, sino, g->views, g->n_views, g->det_count, p.cspan, p.n_chunks, p.n_strips, skip);
   return launch_check("k_proj2d_fwd_gather");
 }
