@@ -143,10 +143,13 @@ typedef struct ct_proj2d_schedule {
 
 /*
  * Autotuner: times the forward for each candidate views-per-CTA and the
- * adjoint (with its split sum) for each candidate split count on `stream`
- * with CUDA events (one untimed call, then `reps` timed calls each), and
- * records the fastest of each in a process-wide table (guarded by a mutex)
- * keyed by the geometry's sizes and batch.  Every later call on that
+ * adjoint (with its split sum) for the split counts 1, 2, 4, 8, ... on
+ * `stream` with CUDA events (one untimed call, then `reps` timed calls
+ * each), and records the fastest forward and, among adjoint timings within
+ * 3 % of the fastest, the fewest splits (so the choice, which sets the
+ * adjoint's summation order, does not flip between runs on noise) in a
+ * process-wide table (guarded by a mutex) keyed by the geometry's sizes and
+ * batch.  Every later call on that
  * geometry (ct_proj2d_fwd/adj, the fused solvers) uses the recorded
  * schedule; results change only in the adjoint's split summation order.
  * img and sino are scratch (overwritten); the workspace needs
