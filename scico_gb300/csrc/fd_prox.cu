@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(ct::kReduceThreads)
 extern "C" {
 
 ct_status ct_fd_out_count(const ct_fd_desc* d, int64_t* count) {
-  FdParams p;
+  FdParams p{};
   ct_status st = make_fd(d, p, "ct_fd_out_count");
   if (st != CT_OK) return st;
   if (!count) return ct::fail(CT_ERR_INVALID_ARG, "ct_fd_out_count: null count");
@@ -235,7 +235,7 @@ ct_status ct_fd_out_count(const ct_fd_desc* d, int64_t* count) {
 
 ct_status ct_fd_fwd(const ct_fd_desc* d, const float* x, float* out, int32_t batch,
                     ct_stream_t stream) {
-  FdParams p;
+  FdParams p{};
   ct_status st = make_fd(d, p, "ct_fd_fwd");
   if (st != CT_OK) return st;
   if (!x || !out) return ct::fail(CT_ERR_INVALID_ARG, "ct_fd_fwd: null array");
@@ -248,7 +248,7 @@ ct_status ct_fd_fwd(const ct_fd_desc* d, const float* x, float* out, int32_t bat
 
 ct_status ct_fd_adj(const ct_fd_desc* d, const float* dx, float* x, int32_t batch,
                     ct_stream_t stream) {
-  FdParams p;
+  FdParams p{};
   ct_status st = make_fd(d, p, "ct_fd_adj");
   if (st != CT_OK) return st;
   if (!x || !dx) return ct::fail(CT_ERR_INVALID_ARG, "ct_fd_adj: null array");

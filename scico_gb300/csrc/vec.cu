@@ -241,7 +241,7 @@ ct_status ct_dot(const float* a, const float* b, int64_t n, double* out_dev, voi
                  size_t workspace_bytes, ct_stream_t stream) {
   if (!a || !b || !out_dev) return ct::fail(CT_ERR_INVALID_ARG, "ct_dot: null pointer");
   if (n < 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_dot: n=%lld", (long long)n);
-  RedWs w;
+  RedWs w{};
   ct_status st = red_ws(workspace, workspace_bytes, "ct_dot", w);
   if (st != CT_OK) return st;
   const int vec = ct::quad_ok((size_t)n, a, b);
@@ -256,7 +256,7 @@ ct_status ct_cg_init(const float* b, const float* Ax, float* r, float* p, int64_
   if (!b || !Ax || !r || !p || !scalars)
     return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_init: null pointer");
   if (n < 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_init: n=%lld", (long long)n);
-  RedWs w;
+  RedWs w{};
   ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_init", w);
   if (st != CT_OK) return st;
   const int vec = ct::quad_ok((size_t)n, b, Ax, r, p);
@@ -270,7 +270,7 @@ ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap, int6
                        ct_stream_t stream) {
   if (!x || !r || !p || !Ap || !scalars)
     return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_update: null pointer");
-  RedWs w;
+  RedWs w{};
   ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_update", w);
   if (st != CT_OK) return st;
   const int vec = ct::quad_ok((size_t)n, x, r, p, Ap);
@@ -282,7 +282,7 @@ ct_status ct_cg_update(float* x, float* r, const float* p, const float* Ap, int6
 ct_status ct_cg_direction(float* p, const float* r, int64_t n, double* scalars, void* workspace,
                           size_t workspace_bytes, ct_stream_t stream) {
   if (!p || !r || !scalars) return ct::fail(CT_ERR_INVALID_ARG, "ct_cg_direction: null pointer");
-  RedWs w;
+  RedWs w{};
   ct_status st = red_ws(workspace, workspace_bytes, "ct_cg_direction", w);
   if (st != CT_OK) return st;
   return ct::cg_direction_launch(p, r, (size_t)n, scalars, workspace, ct::as_stream(stream));
