@@ -16,14 +16,27 @@ synthetic sinogram (20-ellipse phantom, 0.5%-of-peak Gaussian noise).
   roofline  the forward projector (dominant kernel) timed live with CUDA
             events: algorithmic bytes = 4 B per pixel-view interaction +
             the sinogram write, against the measured HBM copy bandwidth.
-  cpu_baseline  the C/OpenMP restatement of scico's path (reference float32
-            policy) timed on the host cores on a bounded sample.
+            That figure measures interaction throughput: the image and
+            sinogram stay in L2, so the kernel is bound by instruction issue
+            and shared memory, not DRAM; the measured DRAM bytes per call
+            (ncu), their rate and the issue-slot figures are reported beside
+            it.
+  cpu_baseline  the C/OpenMP restatement of scico's path timed on all host
+            cores for the same whole 100-iteration solve from x0 = 0.
+  secondary the other workloads, each CUDA-event timed with its own clock
+            samples: the 3D solve (256^3, 360 views), the 64 uneven scans
+            solved in one batch call against per-scan loops, and the
+            unrolled-CG training step (forward and backward).
 
 ``--config c5`` runs the 3D workload instead (256^3 volume, 360 views about
 axis 0, L1 + L2,1 TV, 30 iterations, CG <= 8), with the same keys.
 
 ``--impl reference`` times that CPU restatement alone as the reference arm
-(scico itself runs on JAX, which is not installable on these machines).
+(scico itself runs on JAX, which is not installable on these machines): the
+same whole solve from x0 = 0, its iterations split over the --steps timed
+steps (state carried from one step to the next), with the GPU solver's
+precision policy (float64 CG dot products) so both arms run the same
+algorithm; both lines report the CG steps their solve ran.
 Multi-GPU (``--gpus N`` under torchrun): independent replicas, no collective
 on the data path; value = all ranks' iterations / max time.
 """
@@ -60,7 +73,11 @@ def _args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"],
                     help="c1/c2: 2D ADMM-TV (default c2); c5: 3D ADMM-TV, 256^3 x 360 views")
-    ap.add_argument("--cpu-iters", type=int, default=1, help="ADMM iterations per CPU-baseline sample")
+    ap.add_argument("--ref-precision", default="f64dots", choices=["f64dots", "f32"],
+                    help="CPU restatement's CG scalars: float64 dot products (the GPU solver's policy, default) "
+                         "or float32 (the reference's own)")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the secondary workloads (3D solve, batched scans, training step)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the planner's default projector schedule instead of measuring one first")
     return ap.parse_args()
@@ -166,19 +183,39 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 
-def cpu_sample(c, iters: int, threads: int):
-    """Time `iters` ADMM-TV iterations of workload `c` on the CPU restatement."""
+def cpu_full_solve(c, threads: int, segments: int = 1, warmup: int = 0, dot64: bool = True):
+    """The whole `c.maxiter`-iteration ADMM-TV solve of workload `c` from
+    x0 = 0 on the C/OpenMP restatement, its iterations split into `segments`
+    consecutive timed windows (the state carried from one to the next, so the
+    windows together are exactly one solve).  `warmup` untimed single
+    iterations of a throwaway solve come first.  Returns the per-window
+    times, the iterations of each window, the solve's CG step counts, its
+    final objective and the thread count used."""
     from oracle import ctref_c
     from scico_gb300 import workloads
 
     G = ctref_c.Geometry((c.n, c.n), c.angles, det_count=c.det_count)
     used = ctref_c.set_threads(threads)
-    x_gt = c.phantom()
-    y = workloads.noisy(G.project(x_gt), c.noise, c.noise_seed)
-    t0 = time.perf_counter()
-    G.admm_tv(y, c.lam, c.rho, iters, cg_maxiter=c.cg_maxiter, cg_tol=c.cg_tol)
-    dt = time.perf_counter() - t0
-    return iters / dt, used, dt
+    y = workloads.noisy(G.project(c.phantom()), c.noise, c.noise_seed)
+    kw = dict(cg_maxiter=c.cg_maxiter, cg_tol=c.cg_tol, dot64=dot64)
+    for _ in range(warmup):
+        G.admm_tv(y, c.lam, c.rho, 1, **kw)
+    bounds = np.linspace(0, c.maxiter, segments + 1).round().astype(int)
+    state, times, n_its, stats = None, [], [], []
+    for k in range(segments):
+        n = int(bounds[k + 1] - bounds[k])
+        n_its.append(n)
+        if n == 0:
+            times.append(0.0)
+            continue
+        t0 = time.perf_counter()
+        x, z, u, it = G.admm_tv(y, c.lam, c.rho, n, state=state, **kw)
+        times.append(time.perf_counter() - t0)
+        state = (x, z, u)
+        stats.append(it)
+    it = np.concatenate(stats)
+    return {"times": times, "iterations": n_its, "cg": [int(v) for v in it[:, 3]],
+            "objective": float(it[-1, 0]), "threads": used}
 
 
 def cpu_sample_3d(c, cg_steps: float, threads: int):
@@ -238,25 +275,28 @@ def run_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
         return 0
     c = _workload(args.config)
-    threads = ctref_c.default_threads()
-    for _ in range(args.warmup):
-        cpu_sample(c, args.cpu_iters, threads)
-    total_it, total_t, used = 0, 0.0, threads
-    for _ in range(args.steps):
-        _, used, dt = cpu_sample(c, args.cpu_iters, threads)
-        total_it += args.cpu_iters
-        total_t += dt
-    value = total_it / total_t
-    sample = (f"{args.cpu_iters} ADMM-TV iteration(s) per step of the {c.n}x{c.n}/{c.n_views}/{c.det_count} "
-              f"workload; C/OpenMP restatement of scico's float32 path (scico runs on JAX, not installable here)")
+    dot64 = args.ref_precision == "f64dots"
+    r = cpu_full_solve(c, ctref_c.default_threads(), segments=max(1, args.steps), warmup=args.warmup, dot64=dot64)
+    total_t = sum(r["times"])
+    value = c.maxiter / total_t
+    pol = "float64 CG dot products (the GPU solver's precision policy)" if dot64 else \
+        "float32 CG scalars (the reference's precision)"
+    sample = (f"the whole {c.maxiter}-iteration ADMM-TV solve from x0 = 0 of the {c.n}x{c.n}/{c.n_views}/"
+              f"{c.det_count} workload, split over the {args.steps} timed steps; C/OpenMP restatement of scico's "
+              f"path with {pol}, every iteration as scico evaluates it (A^T y, itstat operator applications); "
+              f"scico runs on JAX, not installable here")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(1, args.steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 20-ellipse phantom, 0.5% Gaussian noise)",
         "config": _config_json(c, args.config),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": r["threads"], "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "solve_s": total_t, "cg_steps_total": int(sum(r["cg"])),
+        "iterations_with_cg_steps": int(sum(1 for k in r["cg"] if k > 0)),
+        "projector_applications": int(4 * c.maxiter + 2 * sum(r["cg"])), "final_objective": r["objective"],
+        "ref_precision": args.ref_precision,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -416,12 +456,8 @@ def run_gpu(args):
     alg_adj = 4.0 * inter + 4.0 * c.n * c.n
     peak, peak_kind = _hbm_peak()
     achieved = alg_fwd / t_fwd / 1e9
-    traffic = None
-    prof = ROOT / "profiles" / f"proj2d_fwd_{args.config}.md"
-    if prof.exists():  # dram__bytes_read.sum + dram__bytes_write.sum of one call (ncu)
-        for line in prof.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_call:"):
-                traffic = int(line.split(":")[1])
+    prof = _ncu_figures(f"proj2d_fwd_{args.config}")
+    traffic = prof.get("dram_bytes_per_call")
 
     # ---- CPU baseline (rank 0, N = 1) -----------------------------------------
     cpu = None
@@ -429,10 +465,12 @@ def run_gpu(args):
         try:
             from oracle import ctref_c
 
-            v, used, dt = cpu_sample(c, args.cpu_iters, ctref_c.default_threads())
-            cpu = {"value": v, "unit": UNIT, "cores": used, "kind": "port",
-                   "sample": f"{args.cpu_iters} ADMM-TV iteration(s) (CG<=10, itstat on) of the same workload, "
-                             f"C/OpenMP restatement of scico's float32 path, {dt:.1f} s"}
+            r = cpu_full_solve(c, ctref_c.default_threads(), dot64=True)
+            dt = sum(r["times"])
+            cpu = {"value": c.maxiter / dt, "unit": UNIT, "cores": r["threads"], "kind": "port",
+                   "sample": f"the whole {c.maxiter}-iteration solve from x0 = 0 ({dt:.1f} s, {sum(r['cg'])} CG "
+                             "steps), C/OpenMP restatement of scico's path with float64 CG dot products",
+                   "cg_steps_total": int(sum(r["cg"]))}
         except Exception as exc:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
@@ -460,18 +498,82 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "kernel": "ct_proj2d_fwd", "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes": alg_fwd, "launch_s": t_fwd,
+                         "model": "4 B per pixel-view interaction + the sinogram write (a sweep that streams the "
+                                  "image once per view); a measure of interaction throughput",
                          "interactions_per_s": inter / t_fwd,
+                         "dram": None if traffic is None else {
+                             "bytes_per_call": traffic, "gbs": traffic / t_fwd / 1e9,
+                             "frac_of_hbm": traffic / t_fwd / 1e9 / peak},
+                         "limiter": prof.get("limiter"),
+                         "ncu": {k: v for k, v in prof.items() if k not in ("limiter", "dram_bytes_per_call")},
                          "adjoint": {"launch_s": t_adj, "achieved": alg_adj / t_adj / 1e9,
-                                     "frac": alg_adj / t_adj / 1e9 / peak}},
+                                     "frac": alg_adj / t_adj / 1e9 / peak, "interactions_per_s": inter / t_adj}},
             "cpu_baseline": cpu,
             "clocks": clk.result,
             "gpu_launches": launches_per_step * args.steps,
             "final_objective": objective,
+            "cg_steps_total": int(sum(cg_its)),
+            "iterations_with_cg_steps": int(sum(1 for k in cg_its if k > 0)),
         }
+        if not args.no_secondary and world == 1:
+            del ws, pws, flush
+            torch.cuda.empty_cache()
+            line["secondary"] = secondary(dev)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def _ncu_figures(name):
+    """Figures of the last ncu capture of a kernel (profiles/<name>.json:
+    DRAM bytes per call, issue activity, instructions per interaction, the
+    limiter), or {} when none is committed."""
+    f = ROOT / "profiles" / f"{name}.json"
+    try:
+        return json.loads(f.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def secondary(dev):
+    """The other benchmark workloads at N = 1, each timed with CUDA events
+    and its own clock samples: the 3D ADMM-TV solve (256^3, 360 views, 30
+    iterations, CG <= 8) and its forward projector; the 64 uneven scans (50
+    iterations each) in one batch call against the fused per-scan graph
+    loop, the per-scan loop with plain launches and the drop-in ADMM loop;
+    the unrolled-CG training step (16 x 256^2, 5 blocks x CG 10)."""
+    import torch
+
+    from scico_gb300 import opbench, workloads
+
+    out = {}
+    peak, _ = _hbm_peak()
+    with ClockSampler(dev.index) as clk:
+        a3 = opbench.admm3d(dev, iters=workloads.C5.maxiter, warmup=1, reps=2)
+    out["c5_admm_tv_3d"] = {"iters_per_s": a3["iters_per_s"], "s_per_solve": a3["median_s"],
+                            "iterations": a3["iters"], "cg_steps_total": int(sum(a3["cg_steps"])),
+                            "clocks": clk.result}
+    with ClockSampler(dev.index) as clk:
+        p3 = opbench.proj3d(dev, "fwd", warmup=2, reps=5)
+    out["c5_proj3d_fwd"] = {"launch_s": p3["median_s"], "achieved_gbs": p3["alg_gbs"],
+                            "frac": p3["alg_gbs"] / peak, "interactions_per_s": p3["interactions_per_s"],
+                            "clocks": clk.result}
+    torch.cuda.empty_cache()
+    with ClockSampler(dev.index) as clk:
+        b = opbench.c3(dev, iters=50, warmup=1, reps=2, autotune=True, plain=True)
+    out["c3_batched_scans"] = {k: b[k] for k in ("scans", "iters", "batched_s", "scans_per_s", "looped_s",
+                                                 "speedup", "looped_plain_launch_s", "speedup_vs_plain_launch",
+                                                 "looped_generic_s", "speedup_vs_generic", "mean_cg_iters")}
+    out["c3_batched_scans"]["clocks"] = clk.result
+    torch.cuda.empty_cache()
+    with ClockSampler(dev.index) as clk:
+        m = opbench.modl(dev, warmup=2, reps=3)
+    out["c4_unrolled_cg_training"] = {k: m[k] for k in ("batch", "forward_s", "backward_s",
+                                                         "backward_over_forward", "images_per_s_train",
+                                                         "peak_mem_gb")}
+    out["c4_unrolled_cg_training"]["clocks"] = clk.result
+    return out
 
 
 def run_gpu_3d(args):

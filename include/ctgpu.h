@@ -128,6 +128,31 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
                         ct_stream_t stream);
 
 /*
+ * Device-side checks.  The projector kernels never trap: a check that fails
+ * on the device sets a bit of a per-device error word and skips the work it
+ * guards (bit 0: a forward tile's bins exceed the plan; bit 1: a forward
+ * strip copy did not complete within the wait's poll limit, and the CTA
+ * wrote zeros for its bins; bit 2: an adjoint view window exceeds the plan).
+ * No reference counterpart (scico's projector is XLA code without waits).
+ *
+ * ct_proj2d_check synchronises `stream`, then reads and clears the word:
+ * CT_OK when it was 0, CT_ERR_TIMEOUT when bit 1 was set, else
+ * CT_ERR_UNSUPPORTED; ct_last_error() names the bits.  ct_proj2d_errflag
+ * and ct_proj3d_errflag return and clear the raw words (-1 if unreadable).
+ *
+ * ct_set_wait_poll_limit sets the number of mbarrier polls the forward's
+ * strip-copy wait makes before it gives up (default 2^24, process-wide,
+ * read when a call launches; a solver graph keeps the value current at
+ * its capture).  0 makes every wait give up at once: failure-detection
+ * tests use it to exercise the timeout path without a hung GPU.
+ */
+ct_status ct_proj2d_check(ct_stream_t stream);
+int ct_proj2d_errflag(void);
+int ct_proj3d_errflag(void);
+void ct_set_wait_poll_limit(uint32_t polls);
+uint32_t ct_wait_poll_limit(void);
+
+/*
  * Launch schedule of the 2D projector for one geometry and batch: views per
  * CTA of the forward and view splits of the adjoint.  No counterpart in the
  * reference (XLA picks its own launch shapes); the batched-scan workload asks

@@ -157,6 +157,11 @@ _SIGNATURES = {
     "ct_proj2d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_proj2d_fwd_noalloc": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_proj2d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_proj2d_check": (ctypes.c_int, [P]),
+    "ct_proj2d_errflag": (ctypes.c_int, []),
+    "ct_proj3d_errflag": (ctypes.c_int, []),
+    "ct_set_wait_poll_limit": (None, [ctypes.c_uint32]),
+    "ct_wait_poll_limit": (ctypes.c_uint32, []),
     "ct_proj2d_autotune": (ctypes.c_int, [P, c_int32, P, P, P, c_size_t, c_int32, P, P]),
     "ct_proj2d_schedule_get": (ctypes.c_int, [P, c_int32, P]),
     "ct_proj2d_schedule_clear": (None, []),
@@ -229,6 +234,16 @@ def call(name: str, *args) -> None:
         if st == CT_ERR_SHAPE:
             raise ValueError(str(exc)) from exc
         raise exc
+
+
+def check_device(stream) -> None:
+    """Raise CtError if a projector's device-side check fired since the last
+    check (a bounded wait ran out, or a span exceeded the plan: the guarded
+    work was skipped).  Synchronises `stream`."""
+    call("ct_proj2d_check", stream)
+    w3 = load().ct_proj3d_errflag()
+    if w3:
+        raise CtError(CT_ERR_UNSUPPORTED, "ct_proj3d_errflag", f"3D projector device check word {w3:#x}")
 
 
 def ptr(x) -> int:

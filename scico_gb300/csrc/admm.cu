@@ -1061,9 +1061,11 @@ void make_key(const Ctx& c, int32_t iter0, std::vector<unsigned char>& key) {
   put(&c.P.nd, sizeof(c.P.nd));
   put(&fresh, sizeof(fresh));
   put(c.P.desc, c.P.desc_size);
-  if (c.P.nd == 2) {  // the projector's schedule (the autotuner may record a new one)
+  if (c.P.nd == 2) {  // the projector's schedule (the autotuner may record a new one) and wait limit
     put(&c.P.proj.p2.vpc, sizeof(int));
     put(&c.P.proj.p2.nsplit, sizeof(int));
+    const uint32_t polls = ct::proj2d_wait_polls();
+    put(&polls, sizeof(polls));
   }
   put(&c.ws, sizeof(c.ws));
   put(&c.y, sizeof(c.y));

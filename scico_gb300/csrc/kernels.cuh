@@ -28,6 +28,8 @@ struct Sched2d {
 ct_status proj2d_check(const ct_geom2d* g, const char* who);
 Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch);  // recorded schedule, else default
 Proj2dPlan proj2d_plan_sched(const ct_geom2d* g, int batch, Sched2d s);
+// Current poll limit of the forward's strip-copy wait (ct_set_wait_poll_limit).
+uint32_t proj2d_wait_polls();
 // One-time per-process function attributes (large dynamic shared memory);
 // must run before any stream capture.
 ct_status proj2d_prepare(const Proj2dPlan& p);

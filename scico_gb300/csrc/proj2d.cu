@@ -30,6 +30,7 @@
 // |Px| < 2^22, checked per tile and view, with a floorf path otherwise):
 // full-rate FP32 operations instead of conversion instructions.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -57,6 +58,10 @@ constexpr int kAVC = 32;        // views staged per adjoint run
 constexpr int kAdjTargetCtas = 1216;  // 152 SMs x 8: view splits until the CTAs balance over the SMs
 constexpr int kAdjMinViewsPerSplit = 16;
 constexpr uint32_t kMaxPolls = 1u << 24;
+// Poll limit of the forward's strip-copy wait, read when a call launches
+// (ct_set_wait_poll_limit); a solver graph keeps the value it was captured
+// with.
+std::atomic<uint32_t> g_wait_polls{kMaxPolls};
 
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
@@ -253,6 +258,7 @@ struct FwdArgs {
   int L, LS, cspan;
   int n_chunks, vpc;
   int bulk;             // 1 = strip rows by cp.async.bulk
+  uint32_t max_polls;   // poll limit of the strip-copy wait
   int* errflag;
   const double* skip;
 };
@@ -342,9 +348,13 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   const int b = blockIdx.z;
   const float* im = a.img + (size_t)b * a.rows * a.cols;
 
+  const int vbeg = blockIdx.y * a.vpc;
+  const int vend = min(a.nv, vbeg + a.vpc);
+
   // ---- stage the 32 x 256 strip (zero outside the image) -------------------
   const int vrows = min(kT, a.rows - i0);
   const int vcols = min(kCW, a.cols - c0);
+  int timed_out = 0;
   if (a.bulk) {
     if (tid == 0) {
       ct::mbar_init(bar, 1);
@@ -363,8 +373,11 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       for (int c = lane; c < kRS; c += 32)
         if (r >= vrows || c >= vcols) strip[r * kRS + c] = 0.0f;
     fwd_view_params(a, vs, i0, c0, ch);
-    if (!ct::mbar_wait_bounded(bar, 0, kMaxPolls)) {
+    if (!ct::mbar_wait_bounded(bar, 0, a.max_polls)) {
+      timed_out = 1;
       if (tid == 0) atomicOr(a.errflag, 2);
+      // the copies were issued: let them land (default limit) before the
+      // CTA's shared memory is released
       ct::mbar_wait_bounded(bar, 0, kMaxPolls);
     }
   } else {
@@ -373,14 +386,21 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
         strip[r * kRS + c] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
     fwd_view_params(a, vs, i0, c0, ch);
   }
-  __syncthreads();
+  if (__syncthreads_or(timed_out)) {
+    // The strip is not known to be complete: skip the work and leave zeros
+    // in this CTA's strip bins, so the gather reads defined values.
+    for (int vi = warp; vi < vend - vbeg; vi += kFW) {
+      float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + vbeg + vi) * a.cspan;
+      const int n = min(vs->strip[vi].y, a.cspan);
+      for (int k = lane; k < n; k += 32) po[k] = 0.0f;
+    }
+    return;
+  }
 
   const int tj = ch * (kCW / kT) + warp;  // this warp's tile column
   const int j0 = tj * kT;
   const float fi = (float)(i0 + lane);
   const float fj0 = (float)j0;
-  const int vbeg = blockIdx.y * a.vpc;
-  const int vend = min(a.nv, vbeg + a.vpc);
   // this lane's tile row, kept in registers for all the CTA's views
   float xr[kT];
   {
@@ -856,6 +876,8 @@ bool sched_lookup(const ct_geom2d* g, int batch, SchedVal& out) {
   return true;
 }
 
+uint32_t proj2d_wait_polls() { return g_wait_polls.load(std::memory_order_relaxed); }
+
 Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   SchedVal v;
   return proj2d_plan_sched(g, batch, sched_lookup(g, batch, v) ? v.s : Sched2d{});
@@ -892,6 +914,7 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   a.n_chunks = p.n_chunks;
   a.vpc = p.vpc;
   a.bulk = ((g->cols & 3) == 0 && aligned(img, 16)) ? 1 : 0;
+  a.max_polls = g_wait_polls.load(std::memory_order_relaxed);
   a.errflag = errflag_ptr();
   a.skip = skip;
   if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
@@ -1181,6 +1204,27 @@ ct_status ct_proj2d_fwd_noalloc(const ct_geom2d* g, const float* img, float* sin
   // Every scratch element the second pass reads is written by the first
   // pass of the same call, so nothing needs clearing between calls.
   return ct::proj2d_fwd_launch(g, p, img, sino, batch, scratch, ct::as_stream(stream), nullptr);
+}
+
+void ct_set_wait_poll_limit(uint32_t polls) { g_wait_polls.store(polls, std::memory_order_relaxed); }
+
+uint32_t ct_wait_poll_limit(void) { return g_wait_polls.load(std::memory_order_relaxed); }
+
+ct_status ct_proj2d_check(ct_stream_t stream) {
+  ct_status st = ct::cuda_check(cudaStreamSynchronize(ct::as_stream(stream)), "ct_proj2d_check: synchronize");
+  if (st != CT_OK) return st;
+  int v = 0;
+  st = ct::cuda_check(cudaMemcpyFromSymbol(&v, g_proj2d_err, sizeof(int)), "ct_proj2d_check: read");
+  if (st != CT_OK) return st;
+  if (v == 0) return CT_OK;
+  const int zero = 0;
+  st = ct::cuda_check(cudaMemcpyToSymbol(g_proj2d_err, &zero, sizeof(int)), "ct_proj2d_check: clear");
+  if (st != CT_OK) return st;
+  if (v & 2)
+    return ct::fail(CT_ERR_TIMEOUT, "ct_proj2d_check: a forward strip copy wait ran out (error word 0x%x); "
+                    "the CTAs concerned skipped their work and wrote zeros", v);
+  return ct::fail(CT_ERR_UNSUPPORTED, "ct_proj2d_check: a %s span exceeded the plan (error word 0x%x); "
+                  "the work concerned was skipped", (v & 1) ? "forward tile" : "adjoint window", v);
 }
 
 // Diagnostic: returns (and clears) the projector's internal check word.

@@ -52,13 +52,13 @@ def main(argv=None):
     a = ap.parse_args(argv)
     dev = _device.require_cuda()
     if a.op.startswith("proj3d"):
-        return _proj3d(a, dev)
+        return print(json.dumps(proj3d(dev, a.op[7:], a.views, a.general, a.warmup, a.reps)))
     if a.op == "admm3d":
-        return _admm3d(a, dev)
+        return print(json.dumps(admm3d(dev, a.iters, a.warmup, a.reps, a.graph)))
     if a.op == "modl":
-        return _modl(a, dev)
+        return print(json.dumps(modl(dev, a.warmup, a.reps, a.recompute, a.autotune)))
     if a.op == "c3":
-        return _c3(a, dev)
+        return print(json.dumps(c3(dev, a.iters, a.warmup, a.reps, a.streams, a.autotune, a.plain)))
     c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
     A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
     g = A.geometry()
@@ -123,16 +123,17 @@ def _time(fn, s, warmup, reps):
     return statistics.median(ts), min(ts)
 
 
-def _proj3d(a, dev):
-    """3D projector on a Volume3D workload (random volume: the projector's
-    time does not depend on the values)."""
+def proj3d(dev, which="fwd", views=0, general=False, warmup=3, reps=20):
+    """3D projector on the 256^3 / 360-view workload (random volume: the
+    projector's time does not depend on the values); which = "fwd" or "adj",
+    views = first N views (0 = all), general = run the GENERAL kernels."""
     c = workloads.C5
     M = c.matrices()
-    if a.views:
-        M = M[: a.views]
+    if views:
+        M = M[:views]
     A = linop.XRayTransform3D(c.shape, M, c.det_shape)
     g = A.geometry()
-    if a.general:
+    if general:
         g.kind = _lib.CT_PROJ3D_GENERAL
     nv = len(M)
     vol = torch.rand(c.shape, generator=torch.Generator().manual_seed(0)).to(dev)
@@ -140,7 +141,7 @@ def _proj3d(a, dev):
     fwd_b, adj_b = A.workspace_bytes()
     ws = _device.workspace(max(fwd_b, adj_b))
     s = torch.cuda.current_stream()
-    if a.op == "proj3d_fwd":
+    if which == "fwd":
         fn = lambda: _lib.call("ct_proj3d_fwd", ctypes.addressof(g), vol.data_ptr(), proj.data_ptr(), 1,
                                ws.data_ptr(), ws.numel(), s.cuda_stream)
         out_bytes = 4.0 * proj.numel()
@@ -150,29 +151,29 @@ def _proj3d(a, dev):
         fn = lambda: _lib.call("ct_proj3d_adj", ctypes.addressof(g), proj.data_ptr(), out.data_ptr(), 1,
                                ws.data_ptr(), ws.numel(), s.cuda_stream)
         out_bytes = 4.0 * vol.numel()
-    t, tmin = _time(fn, s, a.warmup, a.reps)
+    t, tmin = _time(fn, s, warmup, reps)
     inter = c.n**3 * nv
-    print(json.dumps({"op": a.op, "config": "c5", "views": nv, "kind": "general" if a.general else A.kind,
-                      "median_s": t, "min_s": tmin, "interactions_per_s": inter / t,
-                      "alg_gbs": (4.0 * inter + out_bytes) / t / 1e9}))
+    return {"op": "proj3d_" + which, "config": "c5", "views": nv, "kind": "general" if general else A.kind,
+            "median_s": t, "min_s": tmin, "interactions_per_s": inter / t,
+            "alg_gbs": (4.0 * inter + out_bytes) / t / 1e9}
 
 
-def _admm3d(a, dev):
-    """--iters fused 3D ADMM-TV iterations on the 256^3, 360-view workload
-    (L1 + L2,1 on one FD, rho 1, CG <= 8).  Reports seconds per iteration and
-    the CG steps taken."""
+def admm3d(dev, iters=2, warmup=3, reps=20, graph=1):
+    """`iters` fused 3D ADMM-TV iterations on the 256^3, 360-view workload
+    (L1 + L2,1 on one FD, rho 1, CG <= 8), CUDA events per solve.  Reports
+    seconds per iteration and the CG steps taken."""
     c = workloads.C5
     A = linop.XRayTransform3D(c.shape, c.matrices(), c.det_shape)
     x_gt = torch.from_numpy(workloads.random_ellipsoids(c.n, c.n_ellipsoids, c.phantom_seed)).to(dev)
     y = A(x_gt)
     y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.noise_seed)).to(dev)
     g = A.geometry()
-    desc = _lib.AdmmTv3dDesc(g, a.iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam_l21, c.lam_l1, c.rho, 0.5, 1.0, a.graph)
+    desc = _lib.AdmmTv3dDesc(g, iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam_l21, c.lam_l1, c.rho, 0.5, 1.0, graph)
     n = _lib.c_size_t()
     _lib.call("ct_admm_tv3d_workspace", ctypes.addressof(desc), ctypes.addressof(n))
     ws = _device.workspace(n.value)
     x = torch.zeros(c.shape, device=dev)
-    itstat = torch.zeros((a.iters, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev)
+    itstat = torch.zeros((iters, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev)
     s = torch.cuda.current_stream()
 
     def fn():
@@ -180,14 +181,14 @@ def _admm3d(a, dev):
         _lib.call("ct_admm_tv3d_solve", ctypes.addressof(desc), y.data_ptr(), x.data_ptr(), itstat.data_ptr(), 0,
                   ws.data_ptr(), ws.numel(), s.cuda_stream)
 
-    t, tmin = _time(fn, s, a.warmup, a.reps)
+    t, tmin = _time(fn, s, warmup, reps)
     cg = itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()
-    print(json.dumps({"op": "admm3d", "config": "c5", "iters": a.iters, "graph": a.graph, "median_s": t,
-                      "s_per_iter": t / a.iters, "cg_steps": [int(v) for v in cg],
-                      "objective": [float(v) for v in itstat[:, _lib.CT_ITSTAT_OBJECTIVE].cpu().numpy()]}))
+    return {"op": "admm3d", "config": "c5", "iters": iters, "graph": graph, "median_s": t,
+            "s_per_iter": t / iters, "iters_per_s": iters / t, "cg_steps": [int(v) for v in cg],
+            "objective": [float(v) for v in itstat[:, _lib.CT_ITSTAT_OBJECTIVE].cpu().numpy()]}
 
 
-def _modl(a, dev):
+def modl(dev, warmup=3, reps=20, recompute=False, autotune=False):
     """One MoDL training step on the C4 batch (16 x 256^2, 180 views; 5
     blocks of CG(10) on A^T A + lmbda I, 3-layer 32-filter ResNet): forward
     with the MSE loss, then backward, each timed with CUDA events.
@@ -198,16 +199,16 @@ def _modl(a, dev):
     torch.backends.cuda.matmul.allow_tf32 = False
     c = workloads.C4
     H = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
-    schedule = H.autotune(batch=c.batch, reps=5) if a.autotune else H.schedule(batch=c.batch)
+    schedule = H.autotune(batch=c.batch, reps=5) if autotune else H.schedule(batch=c.batch)
     x_gt = torch.from_numpy(c.phantoms()).to(dev)
     y = H.project(x_gt)
     y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.phantom_seed)).to(dev)
     torch.manual_seed(c.weight_seed)
     net = inverse.MoDLNet(H, depth=c.depth, channels=1, num_filters=c.num_filters, block_depth=c.block_depth,
-                          lmbda_ini=c.lmbda_ini, cg_iter=c.cg_iter, cg_recompute=a.recompute).to(dev)
+                          lmbda_ini=c.lmbda_ini, cg_iter=c.cg_iter, cg_recompute=recompute).to(dev)
     s = torch.cuda.current_stream()
     fts, bts = [], []
-    for k in range(a.warmup + a.reps):
+    for k in range(warmup + reps):
         net.zero_grad(set_to_none=True)
         e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         e0.record(s)
@@ -216,27 +217,28 @@ def _modl(a, dev):
         loss.backward()
         e2.record(s)
         e2.synchronize()
-        if k >= a.warmup:
+        if k >= warmup:
             fts.append(e0.elapsed_time(e1) / 1e3)
             bts.append(e1.elapsed_time(e2) / 1e3)
     tf, tb = statistics.median(fts), statistics.median(bts)
     n_proj = c.batch * (c.depth * (c.cg_iter + 1) * 2 + 1)  # A and A^T applications per image in the forward
-    print(json.dumps({"op": "modl", "config": "c4", "batch": c.batch, "recompute": a.recompute,
-                      "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
-                      "images_per_s_train": c.batch / (tf + tb), "projector_applications_forward": n_proj,
-                      "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach()),
-                      "projector_schedule": schedule}))
+    return {"op": "modl", "config": "c4", "batch": c.batch, "recompute": recompute,
+            "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
+            "images_per_s_train": c.batch / (tf + tb), "projector_applications_forward": n_proj,
+            "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach()),
+            "projector_schedule": schedule}
 
 
-def _c3(a, dev):
-    """The 64 uneven scans (N 128..768, 90..720 views), --iters ADMM-TV
+def c3(dev, iters=50, warmup=3, reps=20, streams=0, autotune=False, plain=False):
+    """The 64 uneven scans (N 128..768, 90..720 views), `iters` ADMM-TV
     iterations each: one ct_admm_tv_solve_batch call against the same scans
     solved one after another with ct_admm_tv_solve (the reference's loop),
-    both from device-resident data, CUDA events."""
+    both from device-resident data, CUDA events.  plain: also the per-scan
+    loops without graphs and through the drop-in ADMM."""
     cfgs = workloads.batched_configs()
     n = len(cfgs)
     tune_s = 0.0
-    if a.autotune:
+    if autotune:
         import time
 
         t0 = time.perf_counter()
@@ -253,14 +255,14 @@ def _c3(a, dev):
         y = A(x_gt)
         y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.noise_seed)).to(dev)
         g = A.geometry()
-        d = _lib.AdmmTvDesc(g, a.iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam, 0.0, c.rho, 0.5, 1.0, 1)
+        d = _lib.AdmmTvDesc(g, iters, c.cg_maxiter, c.cg_tol, 0.0, c.lam, 0.0, c.rho, 0.5, 1.0, 1)
         nb = _lib.c_size_t()
         _lib.call("ct_admm_tv_workspace", ctypes.addressof(d), ctypes.addressof(nb))
         keep.append(A)
         ys.append(y)
         xs.append(torch.zeros((c.n, c.n), device=dev))
         wss.append(_device.workspace(nb.value))
-        its.append(torch.zeros((a.iters, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev))
+        its.append(torch.zeros((iters, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=dev))
         descs.append(d)
     P = ctypes.c_void_p
     D = (_lib.AdmmTvDesc * n)(*descs)
@@ -275,7 +277,7 @@ def _c3(a, dev):
         for x in xs:
             x.zero_()
         _lib.call("ct_admm_tv_solve_batch", ctypes.addressof(D), n, ctypes.addressof(Y), ctypes.addressof(X),
-                  ctypes.addressof(I), 0, ctypes.addressof(W), ctypes.addressof(B), a.streams, s.cuda_stream)
+                  ctypes.addressof(I), 0, ctypes.addressof(W), ctypes.addressof(B), streams, s.cuda_stream)
 
     def looped():
         for k in range(n):
@@ -283,8 +285,8 @@ def _c3(a, dev):
             _lib.call("ct_admm_tv_solve", ctypes.addressof(descs[k]), ys[k].data_ptr(), xs[k].data_ptr(),
                       its[k].data_ptr(), 0, wss[k].data_ptr(), wss[k].numel(), s.cuda_stream)
 
-    tb, _ = _time(batched, s, a.warmup, a.reps)
-    tl, _ = _time(looped, s, a.warmup, a.reps)
+    tb, _ = _time(batched, s, warmup, reps)
+    tl, _ = _time(looped, s, warmup, reps)
     inter = sum(c.n * c.n * c.n_views for c in cfgs)
     batched()
     torch.cuda.synchronize()
@@ -292,16 +294,16 @@ def _c3(a, dev):
     # projector work actually run: one forward/adjoint pair per CG step plus
     # the pair of each iteration's start (A x, A^T A x), skipped only when x
     # did not change
-    pairs = sum(float(cg[k].sum() + a.iters) * cfgs[k].n ** 2 * cfgs[k].n_views for k in range(n))
-    out = {"op": "c3", "scans": n, "iters": a.iters, "streams": a.streams, "batched_s": tb,
+    pairs = sum(float(cg[k].sum() + iters) * cfgs[k].n ** 2 * cfgs[k].n_views for k in range(n))
+    out = {"op": "c3", "scans": n, "iters": iters, "streams": streams, "batched_s": tb,
            "looped_s": tl, "speedup": tl / tb, "scans_per_s": n / tb, "interactions_per_application": inter,
            "mean_cg_iters": float(cg.mean()), "autotune_s": tune_s,
            "projection_pair_interactions": pairs}
-    if a.plain:
+    if plain:
         # the fused per-scan solver with every launch issued from the host
         for d in descs:
             d.use_graph = 0
-        tn, _ = _time(looped, s, 1, max(1, a.reps // 2))
+        tn, _ = _time(looped, s, 1, max(1, reps // 2))
         for d in descs:
             d.use_graph = 1
 
@@ -311,14 +313,14 @@ def _c3(a, dev):
             for k, c in enumerate(cfgs):
                 f = loss.SquaredL2Loss(y=ys[k], A=keep[k])
                 C = linop.FiniteDifference((c.n, c.n), append=0)
-                ADMM(f=f, g_list=[c.lam * functional.L21Norm()], C_list=[C], rho_list=[c.rho], maxiter=a.iters,
+                ADMM(f=f, g_list=[c.lam * functional.L21Norm()], C_list=[C], rho_list=[c.rho], maxiter=iters,
                      subproblem_solver=LinearSubproblemSolver(cg_kwargs={"tol": c.cg_tol, "maxiter": c.cg_maxiter}),
                      fused=False).solve()
 
         tg, _ = _time(generic, s, 0, 1)
         out.update({"looped_plain_launch_s": tn, "speedup_vs_plain_launch": tn / tb,
                     "looped_generic_s": tg, "speedup_vs_generic": tg / tb})
-    print(json.dumps(out))
+    return out
 
 
 if __name__ == "__main__":

@@ -305,7 +305,7 @@ class ADMM:
         _lib.call(run["fn"] + "_solve", _lib.ctypes.addressof(run["desc"]), st["y"].data_ptr(), run["x"].data_ptr(),
                   run["itstat"].data_ptr(), 0 if run["first"] else 1, st["ws"].data_ptr(), st["ws"].numel(),
                   _device.stream())
-        torch.cuda.current_stream().synchronize()
+        _lib.check_device(_device.stream())  # synchronises; raises if a device check skipped work
         self._fused_finish(run, time.perf_counter() - t0)
 
     # -- state (_common.py:222-258) --------------------------------------------
@@ -366,7 +366,7 @@ def solve_batch(solvers: List["ADMM"], n_streams: int = 0) -> List[torch.Tensor]
     _lib.call("ct_admm_tv_solve_batch", _lib.ctypes.addressof(descs), n, _lib.ctypes.addressof(ys),
               _lib.ctypes.addressof(xs), _lib.ctypes.addressof(its), 0 if runs[0]["first"] else 1,
               _lib.ctypes.addressof(wss), _lib.ctypes.addressof(nbs), int(n_streams), _device.stream())
-    torch.cuda.current_stream().synchronize()
+    _lib.check_device(_device.stream())  # synchronises; raises if a device check skipped work
     dt = time.perf_counter() - t0
     for s, r in zip(solvers, runs):
         s._fused_finish(r, dt)

@@ -30,3 +30,23 @@ def cuda(ctlib):
     if not torch.cuda.is_available():
         pytest.fail("GPU test run without a CUDA device")
     return torch.device("cuda", 0)
+
+
+@pytest.fixture(autouse=True)
+def _device_check_words(request):
+    """After every GPU test: the projectors' device error words must be 0
+    (a device check that fired and was not read by the test itself means
+    work was skipped silently)."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import torch
+
+    if not torch.cuda.is_available():
+        return
+    from scico_gb300 import _lib
+
+    lib = _lib.load()
+    torch.cuda.synchronize()
+    w2, w3 = lib.ct_proj2d_errflag(), lib.ct_proj3d_errflag()
+    assert w2 == 0 and w3 == 0, f"device check words left set: proj2d {w2:#x}, proj3d {w3:#x}"

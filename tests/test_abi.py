@@ -30,6 +30,19 @@ def test_exports_every_declared_symbol(ctlib):
     assert set(names) <= set(_lib.exported_symbols()), set(names) - set(_lib.exported_symbols())
 
 
+def test_wait_poll_limit_setting(ctlib):
+    """The strip-copy wait's poll limit is a host-side setting (no device
+    needed): default 2^24, any value settable, restored afterwards."""
+    old = ctlib.ct_wait_poll_limit()
+    assert old == 1 << 24
+    try:
+        ctlib.ct_set_wait_poll_limit(5)
+        assert ctlib.ct_wait_poll_limit() == 5
+    finally:
+        ctlib.ct_set_wait_poll_limit(old)
+    assert ctlib.ct_wait_poll_limit() == old
+
+
 def test_version_and_status(ctlib):
     assert b"sm_103a" in ctlib.ct_version()
     assert ctlib.ct_status_string(0) == b"ok"

@@ -135,6 +135,38 @@ def test_c2_properties(cuda):
     assert float((lhs - rhs).norm() / rhs.norm()) < 1e-6
 
 
+def test_c2_vs_oracle(cuda):
+    """512x512 / 360 / 725 (the benchmark geometry) at full size: forward of
+    the benchmark phantom and of a random image, adjoint of the phantom's
+    sinogram, each against the float64 oracle and against the float32 C
+    restatement of the reference's arithmetic (rel l2 <= 1e-5); adjoint of a
+    white-noise signed sinogram against the float32 restatement.  White noise
+    is not compared with float64 weights: where float32 and float64 Px fall
+    on different sides of an integer, a pixel reads a neighbouring bin, and
+    white-noise neighbours are unrelated values (3.6e-5 at this size); the
+    float32 restatement uses the reference's own weights."""
+    from oracle import ctref_c
+    from scico_gb300 import workloads
+
+    c = workloads.C2
+    H = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+    g = ctref.xray2d_defaults((c.n, c.n), c.angles, det_count=c.det_count)
+    G = ctref_c.Geometry((c.n, c.n), c.angles, det_count=c.det_count)
+    ctref_c.set_threads(ctref_c.default_threads())
+    rng = np.random.default_rng(12)
+    for x in (c.phantom(), rng.random((c.n, c.n)).astype(np.float32)):
+        y = H(torch.from_numpy(x).to(cuda)).cpu().numpy()
+        assert ctref.rel_l2(y, ctref.xray2d_project(x, g, np.float64)) <= 1e-5
+        assert ctref.rel_l2(y, G.project(x)) <= 1e-5
+    yp = G.project(c.phantom())
+    b = H.adj(torch.from_numpy(yp).to(cuda)).cpu().numpy()
+    assert ctref.rel_l2(b, ctref.xray2d_back_project(yp, g, np.float64)) <= 1e-5
+    assert ctref.rel_l2(b, G.back_project(yp)) <= 1e-5
+    ys = rng.standard_normal(H.output_shape).astype(np.float32)
+    b = H.adj(torch.from_numpy(ys).to(cuda)).cpu().numpy()
+    assert ctref.rel_l2(b, G.back_project(ys)) <= 1e-5
+
+
 def test_workspace_errors(cuda):
     H, _ = _op(dict(shape=(32, 32), nv=8))
     g = H.geometry()
