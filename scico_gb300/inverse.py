@@ -11,6 +11,9 @@
   step in the backward pass instead of keeping its intermediates.
 * :class:`ResNet` and :class:`MoDLNet` -- scico/flax/_models.py:121-193 and
   scico/flax/inverse.py:35-110 as torch modules on NCHW tensors.
+* :class:`ODPProxDnBlock`, :class:`ODPGrDescBlock` and :class:`ODPNet` --
+  the unrolled optimization with deep priors (scico/flax/inverse.py:161-462),
+  with the projector's VJPs in the data-fidelity gradient.
 """
 
 from __future__ import annotations
@@ -183,6 +186,79 @@ class MoDLNet(torch.nn.Module):
             z = self.resnet(x.unsqueeze(1)).squeeze(1)
             b = Ahb + lm * z
             x = cg_solver(gram, b, maxiter=self.cg_iter, batch_dims=1, recompute=self.cg_recompute)
+        return x
+
+
+class ODPProxDnBlock(torch.nn.Module):
+    """ODP proximal-gradient denoising block (scico/flax/inverse.py:161-226):
+    ``x = (ResNet(x) + alpha y) / (1 + alpha)`` with a trainable scalar
+    ``alpha`` (initial ``alpha_ini``).  The operator is the identity of the
+    denoising problem; :meth:`batch_op_adj` applies its adjoint."""
+
+    def __init__(self, operator, depth: int, channels: int, num_filters: int,
+                 kernel_size: Tuple[int, int] = (3, 3), strides: Tuple[int, int] = (1, 1),
+                 alpha_ini: float = 0.2):
+        super().__init__()
+        self.operator = operator
+        self.alpha = torch.nn.Parameter(torch.full((1,), float(alpha_ini)))
+        self.resnet = ResNet(depth, channels, num_filters, kernel_size, strides)
+
+    def batch_op_adj(self, y: torch.Tensor) -> torch.Tensor:
+        return y if self.operator is None else back_project(self.operator, y)
+
+    def forward(self, x: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+        a = self.alpha.to(x.dtype)
+        return (self.resnet(x.unsqueeze(1)).squeeze(1) + y * a) / (1.0 + a)
+
+
+class ODPGrDescBlock(torch.nn.Module):
+    r"""ODP gradient-descent block for an :math:`\ell_2` data term
+    (scico/flax/inverse.py:295-375): ``x = ResNet(x) - alpha A^T (A x - y)``
+    with a trainable scalar ``alpha``; ``A`` and ``A^T`` are the projector
+    and its adjoint (each other's vector-Jacobian products)."""
+
+    def __init__(self, operator, depth: int, channels: int, num_filters: int,
+                 kernel_size: Tuple[int, int] = (3, 3), strides: Tuple[int, int] = (1, 1),
+                 alpha_ini: float = 0.2):
+        super().__init__()
+        self.operator = operator
+        self.alpha = torch.nn.Parameter(torch.full((1,), float(alpha_ini)))
+        self.resnet = ResNet(depth, channels, num_filters, kernel_size, strides)
+
+    def batch_op_adj(self, y: torch.Tensor) -> torch.Tensor:
+        return back_project(self.operator, y)
+
+    def forward(self, x: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+        H = self.operator
+        r = project(H, x) - y
+        return self.resnet(x.unsqueeze(1)).squeeze(1) - self.alpha.to(x.dtype) * back_project(H, r)
+
+
+class ODPNet(torch.nn.Module):
+    """Unrolled optimization with deep priors (scico/flax/inverse.py:378-462):
+    ``x = A^T y``, then ``depth`` blocks, each with its own ResNet and
+    ``alpha``; the first block's ``alpha`` starts at ``alpha_ini`` and each
+    later one at half its predecessor's.  ``odp_block`` selects the block
+    (:class:`ODPProxDnBlock` by default, :class:`ODPGrDescBlock` for CT).
+    Input ``(batch, *A.output_shape)``, output ``(batch, *A.input_shape)``;
+    single-channel images."""
+
+    def __init__(self, operator, depth: int, channels: int, num_filters: int, block_depth: int,
+                 kernel_size: Tuple[int, int] = (3, 3), strides: Tuple[int, int] = (1, 1),
+                 alpha_ini: float = 0.5, odp_block=None):
+        super().__init__()
+        if channels != 1:
+            raise ValueError("ODPNet here reconstructs single-channel images (channels=1)")
+        block = ODPProxDnBlock if odp_block is None else odp_block
+        self.operator = operator
+        alphas = [alpha_ini / 2.0**k for k in range(depth)]
+        self.blocks = torch.nn.ModuleList(
+            block(operator, block_depth, channels, num_filters, kernel_size, strides, alpha_ini=a) for a in alphas)
+
+    def forward(self, y: torch.Tensor) -> torch.Tensor:
+        x = self.blocks[0].batch_op_adj(y)
+        for blk in self.blocks:
+            x = blk(x, y)
         return x
 
 

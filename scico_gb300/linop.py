@@ -171,6 +171,8 @@ class LinearOperator:
         if not np.isscalar(other) and not (isinstance(other, np.ndarray) and other.ndim == 0):
             return NotImplemented
         c = float(other)
+        if hasattr(self, "project") and hasattr(self, "back_project"):
+            return ScaledProjector(self, c)
         return LinearOperator(
             self.input_shape,
             self.output_shape,
@@ -214,6 +216,32 @@ def _scale(a, c: float):
     if isinstance(a, tuple):
         return tuple(_scale(u, c) for u in a)
     return a * c
+
+
+class ScaledProjector(LinearOperator):
+    """``c * A`` for a projector ``A`` (scico/linop/_linop.py:229-245): a
+    LinearOperator that also keeps A's batched ``project`` / ``back_project``
+    (scaled), so the scaled projector serves the differentiable networks as
+    A does (the reference's training scripts normalise A by 1 / N)."""
+
+    def __init__(self, A: LinearOperator, c: float):
+        self.base, self.scale = A, float(c)
+        super().__init__(A.input_shape, A.output_shape, eval_fn=lambda x: _scale(A(x), self.scale),
+                         adj_fn=lambda y: _scale(A.adj(y), self.scale), input_dtype=A.input_dtype,
+                         output_dtype=A.output_dtype)
+
+    def project(self, x):
+        return self.base.project(x) * self.scale
+
+    def back_project(self, y):
+        return self.base.back_project(y) * self.scale
+
+    def __mul__(self, other):
+        if not np.isscalar(other) and not (isinstance(other, np.ndarray) and other.ndim == 0):
+            return NotImplemented
+        return ScaledProjector(self.base, self.scale * float(other))
+
+    __rmul__ = __mul__
 
 
 class ComposedLinearOperator(LinearOperator):
