@@ -278,6 +278,44 @@ ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol,
                         int32_t batch, void* workspace, size_t workspace_bytes,
                         ct_stream_t stream);
 
+/*
+ * Launch schedule of the 3D projector.  No reference counterpart: scico
+ * runs the 3D projector through lax.map with a fixed view batch
+ * (scico/linop/xray/_xray3d.py:110-139).
+ */
+typedef struct ct_proj3d_schedule {
+  int32_t tile_groups; /* AXIS0 forward: tile groups (accumulators summed in group order) */
+  int32_t adj_splits;  /* adjoint: view splits (partial volumes summed in order) */
+  float fwd_us;        /* measured device time per forward call (0 if not measured) */
+  float adj_us;        /* measured device time per adjoint call (0 if not measured) */
+  int32_t tuned;       /* 1: recorded by ct_proj3d_autotune; 0: the planner's default */
+} ct_proj3d_schedule;
+
+/*
+ * Autotuner of the 3D projector: times the AXIS0 forward for tile-group
+ * counts 1..8 (GENERAL geometries have no forward schedule) and the adjoint
+ * with its split sum for 1, 2 and 4 view splits, on `stream` with CUDA
+ * events (one untimed call, then `reps` timed ones each), and records the
+ * fastest forward and, among adjoint timings within 3 % of the fastest, the
+ * fewest splits, in a process-wide table (mutex-guarded) keyed by the
+ * geometry's sizes and kind.  Later calls on that geometry (ct_proj3d_fwd /
+ * adj, the fused 3D solver) use the recorded schedule; results change only
+ * in summation order.  `vol` and `proj` are scratch arrays of the
+ * geometry's sizes (overwritten); the workspace must hold both sizes
+ * ct_proj3d_workspace reports, which cover every schedule the tuner may
+ * record.  Not inside a stream capture (CT_ERR_INVALID_ARG).
+ */
+ct_status ct_proj3d_autotune(const ct_geom3d* g, float* vol, float* proj,
+                             void* workspace, size_t workspace_bytes,
+                             int32_t reps, ct_stream_t stream,
+                             ct_proj3d_schedule* chosen);
+
+/* The schedule ct_proj3d_fwd/adj use for this geometry now. */
+ct_status ct_proj3d_schedule_get(const ct_geom3d* g, ct_proj3d_schedule* out);
+
+/* Forget every recorded 3D schedule (later calls use the planner's defaults). */
+void ct_proj3d_schedule_clear(void);
+
 /* ------------------------------------------------------------------------ */
 /* Finite differences (FiniteDifference / SingleAxisFiniteDifference)       */
 /* ------------------------------------------------------------------------ */

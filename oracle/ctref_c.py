@@ -67,15 +67,19 @@ class Geometry:
         self.nv, self.det = nv, self.g["ny"]
         self.cg = _Geom(self.shape[0], self.shape[1], nv, self.det, self.table.ctypes.data)
 
-    def project(self, x: np.ndarray) -> np.ndarray:
+    def project(self, x: np.ndarray, proj64: bool = False) -> np.ndarray:
+        """A x; proj64: sums accumulated in float64 and rounded once."""
         x = np.ascontiguousarray(x, dtype=self.dt)
         y = np.empty((self.nv, self.det), dtype=self.dt)
+        lib(self.f64).ref_set_proj64(1 if proj64 else 0)
         lib(self.f64).ref_proj2d_fwd(ctypes.addressof(self.cg), x.ctypes.data, y.ctypes.data)
         return y
 
-    def back_project(self, y: np.ndarray) -> np.ndarray:
+    def back_project(self, y: np.ndarray, proj64: bool = False) -> np.ndarray:
+        """A^T y; proj64 as for project."""
         y = np.ascontiguousarray(y, dtype=self.dt)
         x = np.empty(self.shape, dtype=self.dt)
+        lib(self.f64).ref_set_proj64(1 if proj64 else 0)
         lib(self.f64).ref_proj2d_adj(ctypes.addressof(self.cg), y.ctypes.data, x.ctypes.data)
         return x
 

@@ -131,6 +131,16 @@ class AdmmTvDesc(ctypes.Structure):
     ]
 
 
+class Proj3dSchedule(ctypes.Structure):
+    _fields_ = [
+        ("tile_groups", c_int32),
+        ("adj_splits", c_int32),
+        ("fwd_us", c_float),
+        ("adj_us", c_float),
+        ("tuned", c_int32),
+    ]
+
+
 class AdmmTv3dDesc(ctypes.Structure):
     _fields_ = [
         ("geom", Geom3D),
@@ -170,6 +180,9 @@ _SIGNATURES = {
     "ct_proj3d_workspace": (ctypes.c_int, [P, c_int32, P, P]),
     "ct_proj3d_fwd": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
     "ct_proj3d_adj": (ctypes.c_int, [P, P, P, c_int32, P, c_size_t, P]),
+    "ct_proj3d_autotune": (ctypes.c_int, [P, P, P, P, c_size_t, c_int32, P, P]),
+    "ct_proj3d_schedule_get": (ctypes.c_int, [P, P]),
+    "ct_proj3d_schedule_clear": (None, []),
     "ct_fd_out_count": (ctypes.c_int, [P, P]),
     "ct_fd_fwd": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_fd_adj": (ctypes.c_int, [P, P, P, c_int32, P]),

@@ -779,9 +779,9 @@ struct Projector {
   const ct_geom3d* g3 = nullptr;
   ct::Proj2dPlan p2{};
   ct::Proj3dPlan p3{};
-  size_t fwd_bytes() const { return nd == 2 ? p2.fwd_bytes : p3.fwd_bytes; }
+  size_t fwd_bytes() const { return nd == 2 ? p2.fwd_bytes : p3.fwd_ws_bytes; }
   // split area to reserve: the largest any recorded 2D schedule may use
-  size_t adj_ws_bytes() const { return nd == 2 ? p2.adj_ws_bytes : p3.adj_bytes; }
+  size_t adj_ws_bytes() const { return nd == 2 ? p2.adj_ws_bytes : p3.adj_ws_bytes; }
   int nsplit() const { return nd == 2 ? p2.nsplit : p3.nsplit; }
   ct_status prepare() const { return nd == 2 ? ct::proj2d_prepare(p2) : ct::proj3d_prepare(g3, p3); }
   ct_status fwd(const float* img, float* sino, void* ws, cudaStream_t s, const double* skip) const {

@@ -52,10 +52,21 @@ struct Proj3dPlan {
   // adjoint view splits (both kinds)
   int nsplit = 1, per_split = 0;
   size_t fwd_bytes = 0, adj_bytes = 0;
+  // the same for the largest tile-group / split counts a schedule may use
+  // (workspaces sized with these stay valid after ct_proj3d_autotune)
+  size_t fwd_ws_bytes = 0, adj_ws_bytes = 0;
+};
+
+// Launch schedule of the 3D projector: AXIS0 forward tile groups and
+// adjoint view splits (0 = the planner's default).
+struct Sched3d {
+  int G = 0;
+  int ns = 0;
 };
 
 ct_status proj3d_check(const ct_geom3d* g, const char* who);
-Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch);
+Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch);  // recorded schedule, else default
+Proj3dPlan proj3d_plan_sched(const ct_geom3d* g, Sched3d s);
 // One-time per-process function attributes; must run before any stream capture.
 ct_status proj3d_prepare(const ct_geom3d* g, const Proj3dPlan& p);
 // proj = A vol for one volume; `ws` holds p.fwd_bytes.  `skip` as for 2D.

@@ -37,6 +37,9 @@
 //    decides), so each output has a single owner and no atomics are needed.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "kernels.cuh"
@@ -690,49 +693,89 @@ ct_status proj3d_check(const ct_geom3d* g, const char* who) {
   return CT_OK;
 }
 
+// Largest schedule values the tuner tries: AXIS0 forward tile groups and
+// adjoint view splits.
+constexpr int kMaxGroups = 8;
+constexpr int kMaxSplits3d = 4;
+
 // The AXIS0 span bounds need max |M[1][1]| and |M[1][2]|; ct_proj3d_views
 // guarantees both <= 1, so the bounds are fixed.
-Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch) {
+Proj3dPlan proj3d_plan_sched(const ct_geom3d* g, Sched3d sc) {
   Proj3dPlan p;
   const int S = g->shape[0], NJ = g->shape[1], NK = g->shape[2], V = g->n_views;
   const int C = g->det_shape[1];
   const int sms = std::max(1, sm_count());
+  int ns = 1, ns_max = 1;
   if (g->kind == CT_PROJ3D_AXIS0) {
     p.Spad = (S + kFwdSlices - 1) / kFwdSlices * kFwdSlices;
     p.tiles_k = (NK + kTileK - 1) / kTileK;
     p.n_tiles = p.tiles_k * ((NJ + kTileJ - 1) / kTileJ);
     const long base = (long)(p.Spad / kFwdSlices) * ((V + p.vpc - 1) / p.vpc);
-    // tile groups: fill the GPU (two CTAs per SM) with a small last wave
-    const long slots = 2L * sms;
-    double best = -1.0;
-    for (int G = 1; G <= std::min(8, p.n_tiles); ++G) {
-      const double waves = (double)(base * G) / (double)slots;
-      const double score = std::min(1.0, waves) * waves / std::ceil(waves);
-      if (score > best + 1e-9) {
-        best = score;
-        p.G = G;
+    const int g_max = std::min(kMaxGroups, p.n_tiles);
+    if (sc.G > 0) {
+      p.G = std::min(sc.G, g_max);
+    } else {
+      // tile groups: fill the GPU (two CTAs per SM) with a small last wave
+      const long slots = 2L * sms;
+      double best = -1.0;
+      for (int G = 1; G <= g_max; ++G) {
+        const double waves = (double)(base * G) / (double)slots;
+        const double score = std::min(1.0, waves) * waves / std::ceil(waves);
+        if (score > best + 1e-9) {
+          best = score;
+          p.G = G;
+        }
       }
     }
     p.fwd_smem = sizeof(float) * (size_t)kOrd * kSvStride + sizeof(float2) * 8 * kOrd;
     p.fwd_bytes = round_up(sizeof(float) * (size_t)p.G * V * C * p.Spad, 256);
+    p.fwd_ws_bytes = round_up(sizeof(float) * (size_t)g_max * V * C * p.Spad, 256);
     const long ctas = (long)((NK + 31) / 32) * ((NJ + kAdjRows - 1) / kAdjRows) * (p.Spad / 32);
-    int ns = 1;
     if (ctas < kAdjTargetCtas) ns = (int)((kAdjTargetCtas + ctas - 1) / ctas);
-    ns = std::min(ns, std::max(1, V / 16));
-    p.per_split = (V + ns - 1) / ns;
-    p.nsplit = (V + p.per_split - 1) / p.per_split;
+    ns_max = std::max(1, V / 16);
   } else {
     const double n = (double)S * NJ * NK;
     const long ctas = (long)((n + 255) / 256);
-    int ns = 1;
     if (ctas < 4L * sms) ns = (int)((4L * sms + ctas - 1) / ctas);
-    ns = std::min(ns, std::max(1, V / 8));
-    p.per_split = (V + ns - 1) / ns;
-    p.nsplit = (V + p.per_split - 1) / p.per_split;
+    ns_max = std::max(1, V / 8);
   }
+  ns = std::min(ns, ns_max);
+  const int ns_ws = std::max(ns, std::min(kMaxSplits3d, ns_max));
+  if (sc.ns > 0) ns = std::min(sc.ns, ns_max);
+  p.per_split = (V + ns - 1) / ns;
+  p.nsplit = (V + p.per_split - 1) / p.per_split;
   p.adj_bytes = p.nsplit > 1 ? round_up(sizeof(float) * (size_t)p.nsplit * S * NJ * NK, 256) : 0;
-  (void)batch;
+  p.adj_ws_bytes = ns_ws > 1 ? round_up(sizeof(float) * (size_t)ns_ws * S * NJ * NK, 256) : 0;
+  p.adj_ws_bytes = std::max(p.adj_ws_bytes, p.adj_bytes);
   return p;
+}
+
+// Schedules recorded by ct_proj3d_autotune, keyed by the geometry's sizes
+// and kind.
+using Sched3dKey = std::tuple<int, int, int, int, int, int, int>;
+struct Sched3dVal {
+  Sched3d s;
+  float fwd_us = 0.0f, adj_us = 0.0f;
+};
+std::mutex g_sched3_mu;
+std::map<Sched3dKey, Sched3dVal> g_sched3;
+
+Sched3dKey sched3_key(const ct_geom3d* g) {
+  return Sched3dKey(g->shape[0], g->shape[1], g->shape[2], g->n_views, g->det_shape[0], g->det_shape[1], g->kind);
+}
+
+bool sched3_lookup(const ct_geom3d* g, Sched3dVal& out) {
+  std::lock_guard<std::mutex> lk(g_sched3_mu);
+  const auto it = g_sched3.find(sched3_key(g));
+  if (it == g_sched3.end()) return false;
+  out = it->second;
+  return true;
+}
+
+Proj3dPlan proj3d_plan(const ct_geom3d* g, int batch) {
+  (void)batch;  // one volume per launch; a batch runs the same plan per volume
+  Sched3dVal v;
+  return proj3d_plan_sched(g, sched3_lookup(g, v) ? v.s : Sched3d{});
 }
 
 ct_status need_ws(const char* who, size_t need, void* ws, size_t bytes) {
@@ -901,8 +944,8 @@ ct_status ct_proj3d_workspace(const ct_geom3d* g, int32_t batch, size_t* fwd_byt
   if (st != CT_OK) return st;
   if (batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_proj3d_workspace: batch=%d", batch);
   const ct::Proj3dPlan p = ct::proj3d_plan(g, batch);
-  if (fwd_bytes) *fwd_bytes = p.fwd_bytes;
-  if (adj_bytes) *adj_bytes = p.adj_bytes;
+  if (fwd_bytes) *fwd_bytes = p.fwd_ws_bytes;  // fit any schedule the autotuner may record
+  if (adj_bytes) *adj_bytes = p.adj_ws_bytes;
   return CT_OK;
 }
 
@@ -955,6 +998,130 @@ ct_status ct_proj3d_adj(const ct_geom3d* g, const float* proj, float* vol, int32
     }
   }
   return CT_OK;
+}
+
+ct_status ct_proj3d_autotune(const ct_geom3d* g, float* vol, float* proj, void* workspace,
+                             size_t workspace_bytes, int32_t reps, ct_stream_t stream,
+                             ct_proj3d_schedule* chosen) {
+  using namespace ct;
+  const char* who = "ct_proj3d_autotune";
+  ct_status st = proj3d_check(g, who);
+  if (st != CT_OK) return st;
+  if (!vol || !proj) return fail(CT_ERR_INVALID_ARG, "%s: null array", who);
+  if (reps <= 0) return fail(CT_ERR_INVALID_ARG, "%s: reps=%d", who, reps);
+  cudaStream_t s = as_stream(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  st = cuda_check(cudaStreamIsCapturing(s, &cap), "stream capture query");
+  if (st != CT_OK) return st;
+  if (cap != cudaStreamCaptureStatusNone) return fail(CT_ERR_INVALID_ARG, "%s: cannot measure inside a stream capture", who);
+  const Proj3dPlan p0 = proj3d_plan_sched(g, Sched3d{});
+  const size_t need = std::max(p0.fwd_ws_bytes, p0.adj_ws_bytes);
+  st = need_ws(who, need, workspace, workspace_bytes);
+  if (st != CT_OK) return st;
+  st = proj3d_prepare(g, p0);
+  if (st != CT_OK) return st;
+  const size_t vol_n = (size_t)g->shape[0] * g->shape[1] * g->shape[2];
+  float* part = static_cast<float*>(workspace);
+
+  auto timed = [&](auto&& fn, float& us) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ct_status r = cuda_check(cudaEventCreate(&e0), "autotune event");
+    if (r == CT_OK) r = cuda_check(cudaEventCreate(&e1), "autotune event");
+    if (r == CT_OK) r = fn();
+    if (r == CT_OK) r = cuda_check(cudaEventRecord(e0, s), "autotune event record");
+    for (int k = 0; k < reps && r == CT_OK; ++k) r = fn();
+    if (r == CT_OK) r = cuda_check(cudaEventRecord(e1, s), "autotune event record");
+    if (r == CT_OK) r = cuda_check(cudaEventSynchronize(e1), "autotune event sync");
+    float ms = 0.0f;
+    if (r == CT_OK) r = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "autotune elapsed time");
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    us = 1000.0f * ms / (float)reps;
+    return r;
+  };
+
+  // Ties (within kTie of the fastest) go to the smaller count: both counts set
+  // a summation order, so the choice should not flip between runs on noise.
+  constexpr float kTie = 1.03f;
+  auto pick = [&](const std::vector<std::pair<int, float>>& cand, int& val, float& us) {
+    float fastest = cand.front().second;
+    for (const auto& c : cand) fastest = std::min(fastest, c.second);
+    for (const auto& c : cand)
+      if (c.second <= kTie * fastest) {
+        val = c.first;
+        us = c.second;
+        return;
+      }
+  };
+  Sched3d best;
+  float best_f = 0.0f, best_a = 0.0f;
+  if (g->kind == CT_PROJ3D_AXIS0) {
+    std::vector<std::pair<int, float>> cand;
+    for (int G = 1; G <= std::min(kMaxGroups, p0.n_tiles); ++G) {
+      const Proj3dPlan p = proj3d_plan_sched(g, Sched3d{G, 0});
+      float us = 0.0f;
+      st = timed([&] { return proj3d_fwd_launch(g, p, vol, proj, workspace, s, nullptr); }, us);
+      if (st != CT_OK) return st;
+      cand.emplace_back(p.G, us);
+    }
+    pick(cand, best.G, best_f);
+  }
+  {
+    std::vector<std::pair<int, float>> cand;
+    int last = 0;
+    for (int ns = 1; ns <= kMaxSplits3d; ns *= 2) {
+      const Proj3dPlan p = proj3d_plan_sched(g, Sched3d{0, ns});
+      if (p.nsplit == last) continue;
+      last = p.nsplit;
+      float us = 0.0f;
+      st = timed(
+          [&] {
+            ct_status r = proj3d_adj_launch(g, p, proj, vol, part, s, nullptr);
+            if (r != CT_OK || p.nsplit == 1) return r;
+            const int blocks = (int)std::min<size_t>((vol_n + 255) / 256, 4096);
+            k_p3_sum_splits<<<blocks, 256, 0, s>>>(part, vol, vol_n, p.nsplit, vol_n);
+            return launch_check("k_p3_sum_splits");
+          },
+          us);
+      if (st != CT_OK) return st;
+      cand.emplace_back(p.nsplit, us);
+    }
+    pick(cand, best.ns, best_a);
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_sched3_mu);
+    g_sched3[sched3_key(g)] = Sched3dVal{best, best_f, best_a};
+  }
+  if (chosen) {
+    const Proj3dPlan p = proj3d_plan_sched(g, best);
+    chosen->tile_groups = g->kind == CT_PROJ3D_AXIS0 ? p.G : 0;
+    chosen->adj_splits = p.nsplit;
+    chosen->fwd_us = best_f;
+    chosen->adj_us = best_a;
+    chosen->tuned = 1;
+  }
+  return CT_OK;
+}
+
+ct_status ct_proj3d_schedule_get(const ct_geom3d* g, ct_proj3d_schedule* out) {
+  using namespace ct;
+  ct_status st = proj3d_check(g, "ct_proj3d_schedule_get");
+  if (st != CT_OK) return st;
+  if (!out) return fail(CT_ERR_INVALID_ARG, "ct_proj3d_schedule_get: null output");
+  Sched3dVal v{};
+  const bool tuned = sched3_lookup(g, v);
+  const Proj3dPlan p = proj3d_plan_sched(g, tuned ? v.s : Sched3d{});
+  out->tile_groups = g->kind == CT_PROJ3D_AXIS0 ? p.G : 0;
+  out->adj_splits = p.nsplit;
+  out->fwd_us = tuned ? v.fwd_us : 0.0f;
+  out->adj_us = tuned ? v.adj_us : 0.0f;
+  out->tuned = tuned ? 1 : 0;
+  return CT_OK;
+}
+
+void ct_proj3d_schedule_clear(void) {
+  std::lock_guard<std::mutex> lk(ct::g_sched3_mu);
+  ct::g_sched3.clear();
 }
 
 // Diagnostic: returns (and clears) the 3D projector's internal check word.

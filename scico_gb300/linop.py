@@ -632,6 +632,37 @@ class XRayTransform3D(LinearOperator):
                   _lib.ctypes.addressof(fwd), _lib.ctypes.addressof(adj))
         return int(fwd.value), int(adj.value)
 
+    def autotune(self, reps: int = 5) -> dict:
+        """Measure the 3D projector's launch schedules for this geometry
+        (AXIS0 forward tile groups, adjoint view splits) and record the
+        fastest, which every later projection and fused 3D solve on the same
+        geometry uses (``ct_proj3d_autotune``).  Runs on the current stream
+        and waits for it; not inside a stream capture.  No counterpart in the
+        reference.  Returns the chosen schedule and its measured times."""
+        g = self.geometry()
+        fwd_bytes, adj_bytes = self.workspace_bytes()
+        ws = _device.workspace(max(fwd_bytes, adj_bytes, 256))
+        vol = _device.empty(self.input_shape)
+        proj = _device.empty(self.output_shape)
+        vol.zero_()
+        out = _lib.Proj3dSchedule()
+        _lib.call("ct_proj3d_autotune", _lib.ctypes.addressof(g), vol.data_ptr(), proj.data_ptr(), ws.data_ptr(),
+                  ws.numel(), reps, _device.stream(), _lib.ctypes.addressof(out))
+        return self._schedule_dict(out)
+
+    def schedule(self) -> dict:
+        """The launch schedule projections of this geometry use now (recorded
+        by :meth:`autotune`, else the planner's default)."""
+        g = self.geometry()
+        out = _lib.Proj3dSchedule()
+        _lib.call("ct_proj3d_schedule_get", _lib.ctypes.addressof(g), _lib.ctypes.addressof(out))
+        return self._schedule_dict(out)
+
+    @staticmethod
+    def _schedule_dict(s) -> dict:
+        return {"tile_groups": int(s.tile_groups), "adj_splits": int(s.adj_splits), "fwd_us": float(s.fwd_us),
+                "adj_us": float(s.adj_us), "tuned": bool(s.tuned)}
+
     _batched = XRayTransform2D._batched
 
     def project(self, im) -> torch.Tensor:

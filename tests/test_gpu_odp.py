@@ -7,7 +7,8 @@ run in float64 on the dense matrix of the oracle's float64 projector
 central finite differences along 20 random directions on the float64 twin
 (<= 1e-3 of the directional derivative's size), and the float32 GPU
 gradients against the twin's (<= 1e-4).  Training: a short run of each
-unrolled network through train.BasicTrainer lowers the training loss."""
+unrolled network through train.BasicTrainer lowers the training loss
+(by a fifth or more in 30 steps)."""
 
 import numpy as np
 import pytest
@@ -109,5 +110,5 @@ def test_training_run_lowers_loss(cuda, kind):
     tr = train.BasicTrainer(cfg, net, _ct_data(Hn, 24, 1), _ct_data(Hn, 8, 2))
     _, stats = tr.train()
     assert tr.num_steps == 30 and len(stats) == 5
-    assert stats[-1]["Train_Loss"] < 0.5 * stats[0]["Train_Loss"], [r["Train_Loss"] for r in stats]
+    assert stats[-1]["Train_Loss"] < 0.8 * stats[0]["Train_Loss"], [r["Train_Loss"] for r in stats]
     assert all(np.isfinite(r["Eval_SNR"]) for r in stats)
