@@ -539,7 +539,9 @@ def _ncu_figures(name):
 def secondary(dev):
     """The other benchmark workloads at N = 1, each timed with CUDA events
     and its own clock samples: the 3D ADMM-TV solve (256^3, 360 views, 30
-    iterations, CG <= 8) and its forward projector; the 64 uneven scans (50
+    iterations, CG <= 8), the CG-free proximal ADMM split of the same
+    problem (native solver and generic loop) and the 3D forward projector;
+    the 64 uneven scans (50
     iterations each) in one batch call against the fused per-scan graph
     loop, the per-scan loop with plain launches and the drop-in ADMM loop;
     the unrolled-CG training step (16 x 256^2, 5 blocks x CG 10)."""
@@ -554,6 +556,11 @@ def secondary(dev):
     out["c5_admm_tv_3d"] = {"iters_per_s": a3["iters_per_s"], "s_per_solve": a3["median_s"],
                             "iterations": a3["iters"], "cg_steps_total": int(sum(a3["cg_steps"])),
                             "clocks": clk.result}
+    with ClockSampler(dev.index) as clk:
+        pd = opbench.padmm3d(dev, iters=20, warmup=1, reps=2)
+    out["c5_padmm_tv_3d"] = {"fused_s_per_iter": pd["fused_s_per_iter"], "generic_s_per_iter": pd["generic_s_per_iter"],
+                             "speedup": pd["speedup"], "iterations": pd["iters"], "clocks": clk.result}
+    torch.cuda.empty_cache()
     with ClockSampler(dev.index) as clk:
         p3 = opbench.proj3d(dev, "fwd", warmup=2, reps=5)
     out["c5_proj3d_fwd"] = {"launch_s": p3["median_s"], "achieved_gbs": p3["alg_gbs"],

@@ -527,6 +527,47 @@ ct_status ct_admm_tv3d_solve(const ct_admm_tv3d_desc* d, const float* y, float* 
                              double* itstat_dev, int32_t iter0, void* workspace,
                              size_t workspace_bytes, ct_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Fused proximal ADMM for CT-TV (ProximalADMM, scico/optimize/_padmm.py)    */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * The CG-free split of the reference's ct_3d_tv_padmm example
+ * (examples/scripts/ct_3d_tv_padmm.py:96-120): f = 0,
+ * A = VerticalStack((C, alpha D)), B = -I, c = 0,
+ * g = SeparableFunctional((SquaredL2Loss(y, scale), (lam / alpha) L21Norm)),
+ * C the 2D or 3D projector, D = FiniteDifference(append=0) over all axes.
+ * Iteration (_padmm.py:349-363):
+ *   x <- x - (1/mu) A^T(2u - u_old);  z <- prox_{g/(rho nu)}(z + (1/nu)(A x - z + u));
+ *   u <- u + A x - z
+ * in float32 with the reference's scalars rounded to float32, residuals in
+ * float64.  itstat: maxiter x 3 doubles {objective g0(z0) + g1(z1),
+ * primal ||A x - z||, dual ||z - z_old||}.
+ */
+typedef struct ct_padmm_tv_desc {
+  int32_t nd;          /* 2: geom2 (XRayTransform2D); 3: geom3 (XRayTransform3D) */
+  ct_geom2d geom2;
+  ct_geom3d geom3;
+  int32_t maxiter;     /* iterations per call                                    */
+  double lam;          /* g1 = (lam / alpha) ||z1||_{2,1}                         */
+  double alpha;        /* weight of D in A                                        */
+  double rho, mu, nu;  /* penalty; mu > ||A||^2, nu > ||B||^2 = 1                 */
+  double loss_scale;   /* g0 = loss_scale ||y - z0||^2 (0.5)                      */
+  int32_t use_graph;   /* 1: one iteration captured once as a graph and replayed */
+} ct_padmm_tv_desc;
+
+ct_status ct_padmm_tv_workspace(const ct_padmm_tv_desc* d, size_t* bytes);
+/* Byte offsets in the workspace of the state blocks z0 (sinogram-shaped),
+ * z1 (nd x image), u0, u1 (float32). */
+ct_status ct_padmm_tv_state(const ct_padmm_tv_desc* d, size_t* z0_offset,
+                            size_t* z1_offset, size_t* u0_offset,
+                            size_t* u1_offset);
+/* cont = 0: start from z = u = u_old = 0 and the given x; 1: continue from
+ * the workspace's state (x must be the previous call's result). */
+ct_status ct_padmm_tv_solve(const ct_padmm_tv_desc* d, const float* y, float* x,
+                            double* itstat_dev, int32_t cont, void* workspace,
+                            size_t workspace_bytes, ct_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,6 +157,22 @@ class AdmmTv3dDesc(ctypes.Structure):
     ]
 
 
+class PadmmTvDesc(ctypes.Structure):
+    _fields_ = [
+        ("nd", c_int32),
+        ("geom2", Geom2D),
+        ("geom3", Geom3D),
+        ("maxiter", c_int32),
+        ("lam", c_double),
+        ("alpha", c_double),
+        ("rho", c_double),
+        ("mu", c_double),
+        ("nu", c_double),
+        ("loss_scale", c_double),
+        ("use_graph", c_int32),
+    ]
+
+
 P = c_void_p
 _SIGNATURES = {
     "ct_version": (c_char_p, []),
@@ -201,6 +217,9 @@ _SIGNATURES = {
     "ct_admm_tv3d_workspace": (ctypes.c_int, [P, P]),
     "ct_admm_tv3d_state": (ctypes.c_int, [P, P, P, P]),
     "ct_admm_tv3d_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),
+    "ct_padmm_tv_workspace": (ctypes.c_int, [P, P]),
+    "ct_padmm_tv_state": (ctypes.c_int, [P, P, P, P, P]),
+    "ct_padmm_tv_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),
 }
 
 _lock = threading.Lock()

@@ -173,14 +173,7 @@ class LinearOperator:
         c = float(other)
         if hasattr(self, "project") and hasattr(self, "back_project"):
             return ScaledProjector(self, c)
-        return LinearOperator(
-            self.input_shape,
-            self.output_shape,
-            eval_fn=lambda x: _scale(self(x), c),
-            adj_fn=lambda y: _scale(self.adj(y), c),
-            input_dtype=self.input_dtype,
-            output_dtype=self.output_dtype,
-        )
+        return ScaledLinearOperator(self, c)
 
     __rmul__ = __mul__
 
@@ -218,11 +211,9 @@ def _scale(a, c: float):
     return a * c
 
 
-class ScaledProjector(LinearOperator):
-    """``c * A`` for a projector ``A`` (scico/linop/_linop.py:229-245): a
-    LinearOperator that also keeps A's batched ``project`` / ``back_project``
-    (scaled), so the scaled projector serves the differentiable networks as
-    A does (the reference's training scripts normalise A by 1 / N)."""
+class ScaledLinearOperator(LinearOperator):
+    """``c * A`` (scico/linop/_linop.py:229-245), keeping ``base`` (A) and
+    ``scale`` (c) so that solvers can recognise the operator."""
 
     def __init__(self, A: LinearOperator, c: float):
         self.base, self.scale = A, float(c)
@@ -230,18 +221,25 @@ class ScaledProjector(LinearOperator):
                          adj_fn=lambda y: _scale(A.adj(y), self.scale), input_dtype=A.input_dtype,
                          output_dtype=A.output_dtype)
 
+    def __mul__(self, other):
+        if not np.isscalar(other) and not (isinstance(other, np.ndarray) and other.ndim == 0):
+            return NotImplemented
+        return type(self)(self.base, self.scale * float(other))
+
+    __rmul__ = __mul__
+
+
+class ScaledProjector(ScaledLinearOperator):
+    """``c * A`` for a projector ``A``: also keeps A's batched ``project`` /
+    ``back_project`` (scaled), so the scaled projector serves the
+    differentiable networks as A does (the reference's training scripts
+    normalise A by 1 / N)."""
+
     def project(self, x):
         return self.base.project(x) * self.scale
 
     def back_project(self, y):
         return self.base.back_project(y) * self.scale
-
-    def __mul__(self, other):
-        if not np.isscalar(other) and not (isinstance(other, np.ndarray) and other.ndim == 0):
-            return NotImplemented
-        return ScaledProjector(self.base, self.scale * float(other))
-
-    __rmul__ = __mul__
 
 
 class ComposedLinearOperator(LinearOperator):

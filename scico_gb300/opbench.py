@@ -6,7 +6,9 @@ Ops: proj2d_fwd, proj2d_adj (one C-ABI call each, CUDA events per call),
 admm (one fused ADMM-TV solve of --iters iterations), proj3d_fwd and
 proj3d_adj (the 256^3, 360-view workload; --views N takes the first N views,
 --general runs the GENERAL kernels on it), admm3d (one fused 3D ADMM-TV
-solve of --iters iterations on that workload), modl (one MoDL training
+solve of --iters iterations on that workload), padmm3d (--iters proximal ADMM
+iterations of the CG-free 3D TV split, native solver and generic loop),
+modl (one MoDL training
 step, forward and backward, on the 16-slice batch), c3 (the 64 uneven scans
 solved in one batch call and in a loop).  Prints one JSON line
 with the median time, interactions/s and the algorithmic-byte bandwidth
@@ -30,8 +32,8 @@ from .optimize import ADMM, LinearSubproblemSolver
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--op", default="proj2d_fwd",
-                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d", "modl",
-                             "c3"])
+                    choices=["proj2d_fwd", "proj2d_adj", "admm", "proj3d_fwd", "proj3d_adj", "admm3d", "padmm3d",
+                             "modl", "c3"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
     ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
@@ -55,6 +57,8 @@ def main(argv=None):
         return print(json.dumps(proj3d(dev, a.op[7:], a.views, a.general, a.warmup, a.reps)))
     if a.op == "admm3d":
         return print(json.dumps(admm3d(dev, a.iters, a.warmup, a.reps, a.graph)))
+    if a.op == "padmm3d":
+        return print(json.dumps(padmm3d(dev, a.iters, a.warmup, a.reps)))
     if a.op == "modl":
         return print(json.dumps(modl(dev, a.warmup, a.reps, a.recompute, a.autotune)))
     if a.op == "c3":
@@ -186,6 +190,43 @@ def admm3d(dev, iters=2, warmup=3, reps=20, graph=1):
     return {"op": "admm3d", "config": "c5", "iters": iters, "graph": graph, "median_s": t,
             "s_per_iter": t / iters, "iters_per_s": iters / t, "cg_steps": [int(v) for v in cg],
             "objective": [float(v) for v in itstat[:, _lib.CT_ITSTAT_OBJECTIVE].cpu().numpy()]}
+
+
+def padmm3d(dev, iters=20, warmup=1, reps=2, generic=True):
+    """Proximal ADMM with the split of the reference's ct_3d_tv_padmm example
+    (A = (C; alpha D), B = -I, g = 1/2 ||y - z0||^2 + (lam / alpha) ||z1||_{2,1};
+    alpha 1e2, lam 2, rho 5e-3) on the 256^3 / 360-view workload: `iters`
+    iterations through the native solver (one graph replayed per iteration)
+    and, with `generic`, through the generic step loop, CUDA events around
+    each solve."""
+    from .functional import L21Norm, SeparableFunctional, ZeroFunctional
+    from .loss import SquaredL2Loss as L2
+    from .optimize import ProximalADMM
+
+    c = workloads.C5
+    C = linop.XRayTransform3D(c.shape, c.matrices(), c.det_shape)
+    x_gt = torch.from_numpy(c.phantom()).to(dev)
+    y = C(x_gt)
+    y = y + c.noise * y.abs().max() * torch.randn(y.shape, generator=torch.Generator().manual_seed(c.noise_seed)).to(dev)
+    alpha, lam, rho = 1e2, 2.0, 5e-3
+    D = linop.FiniteDifference(c.shape, append=0)
+    A = linop.VerticalStack((C, alpha * D))
+    mu, nu = ProximalADMM.estimate_parameters(A, maxiter=20, seed=0)
+    s = torch.cuda.current_stream()
+    out = {"op": "padmm3d", "config": "c5", "iters": iters, "mu": mu, "nu": nu}
+
+    def make(fused):
+        g = SeparableFunctional((L2(y=y), (lam / alpha) * L21Norm()))
+        return ProximalADMM(f=ZeroFunctional(), g=g, A=A, rho=rho, mu=mu, nu=nu, maxiter=iters, fused=fused)
+
+    for name, fused in (("fused", True), ("generic", False)):
+        if name == "generic" and not generic:
+            continue
+        t, _ = _time(lambda: make(fused).solve(), s, warmup, reps)
+        out[name + "_s_per_iter"] = t / iters
+    if generic:
+        out["speedup"] = out["generic_s_per_iter"] / out["fused_s_per_iter"]
+    return out
 
 
 def modl(dev, warmup=3, reps=20, recompute=False, autotune=False):

@@ -30,7 +30,7 @@ import numpy as np
 import torch
 
 from . import _device, _lib, linop
-from .functional import Functional, L1Norm, L21Norm, ScaledFunctional
+from .functional import Functional, L1Norm, L21Norm, ScaledFunctional, SeparableFunctional, ZeroFunctional
 from .loss import SquaredL2Loss, _sqnorm
 from .solver import cg as scico_cg
 
@@ -437,11 +437,23 @@ class ProximalADMM:
     reference's ct_3d_tv_padmm example.  Every operator application runs in
     the ctgpu kernels; ``A x`` is computed once per step and used for both
     the z-update and the u-update.
+
+    ``fused`` ("auto", True, False): that example's pattern -- f =
+    ZeroFunctional, A = VerticalStack((C, alpha * D)) with C an
+    XRayTransform2D/3D and D = FiniteDifference(append=0) over all axes,
+    g = SeparableFunctional((SquaredL2Loss(y), w * L21Norm())), B = None,
+    c = None, fast dual residual -- runs in the native solver
+    ``ct_padmm_tv_solve`` (one iteration captured as a CUDA graph, replayed
+    ``maxiter`` times, residuals and objective computed in its kernels);
+    every other problem runs the generic step loop.
     """
 
     def __init__(self, f: Functional, g: Functional, A: linop.LinearOperator, rho: float, mu: float, nu: float,
                  B: Optional[linop.LinearOperator] = None, c=None, x0=None, z0=None, u0=None,
-                 fast_dual_residual: bool = True, **kwargs):
+                 fast_dual_residual: bool = True, fused="auto", **kwargs):
+        self.fused = fused
+        self._fused_state = None
+        self._fused_ok = B is None and c is None and z0 is None and u0 is None and fast_dual_residual
         self.f, self.g, self.A = f, g, A
         self.B = -linop.Identity(A.output_shape) if B is None else B
         self.c = 0.0 if c is None else c
@@ -508,8 +520,94 @@ class ProximalADMM:
         self.u = _add(self.u, _minus_c(_add(Ax, self.B(self.z)), self.c))
         self._Ax = Ax
 
+    # -- fused native solver ------------------------------------------------
+    def _fused_plan(self):
+        """The ct_3d_tv_padmm pattern's parameters, or None."""
+        if not self._fused_ok or not isinstance(self.f, ZeroFunctional):
+            return None
+        A = self.A
+        if not isinstance(A, linop.VerticalStack) or len(A.ops) != 2:
+            return None
+        C, aD = A.ops
+        if not isinstance(C, (linop.XRayTransform2D, linop.XRayTransform3D)):
+            return None
+        if not isinstance(aD, linop.ScaledLinearOperator) or not isinstance(aD.base, linop.FiniteDifference):
+            return None
+        D = aD.base
+        shape = C.input_shape
+        if D.input_shape != shape or D.axes != tuple(range(len(shape))) or D.append != 0 or \
+                D.prepend is not None or D.circular or aD.scale == 0.0:
+            return None
+        g = self.g
+        if not isinstance(g, SeparableFunctional) or len(g.functional_list) != 2:
+            return None
+        g0, g1 = g.functional_list
+        if not isinstance(g0, SquaredL2Loss) or not g0.has_prox:
+            return None
+        if not isinstance(g1, ScaledFunctional) or not isinstance(g1.functional, L21Norm) or \
+                g1.functional.l2_axis != 0:
+            return None
+        return dict(C=C, alpha=aD.scale, lam=g1.scale * aD.scale, y=g0.y, scale=g0.scale)
+
+    def _solve_fused(self, plan):
+        C = plan["C"]
+        three = isinstance(C, linop.XRayTransform3D)
+        desc = _lib.PadmmTvDesc()
+        desc.nd = 3 if three else 2
+        if three:
+            desc.geom3 = C.geometry()
+        else:
+            desc.geom2 = C.geometry()
+        desc.maxiter = int(self.maxiter)
+        desc.lam, desc.alpha = float(plan["lam"]), float(plan["alpha"])
+        desc.rho, desc.mu, desc.nu = self.rho, self.mu, self.nu
+        desc.loss_scale = float(plan["scale"])
+        desc.use_graph = 1
+        first = self._fused_state is None
+        if first:
+            nb = _lib.c_size_t()
+            _lib.call("ct_padmm_tv_workspace", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(nb))
+            offs = [_lib.c_size_t() for _ in range(4)]
+            _lib.call("ct_padmm_tv_state", _lib.ctypes.addressof(desc), *[_lib.ctypes.addressof(o) for o in offs])
+            self._fused_state = dict(ws=_device.workspace(nb.value), offs=[o.value for o in offs])
+            self.x = self.x.contiguous().clone()
+        st = self._fused_state
+        y = plan["y"].contiguous()
+        itstat = _device.zeros((max(1, self.maxiter), 3), dtype=torch.float64)
+        t0 = time.perf_counter()
+        _lib.call("ct_padmm_tv_solve", _lib.ctypes.addressof(desc), y.data_ptr(), self.x.data_ptr(),
+                  itstat.data_ptr(), 0 if first else 1, st["ws"].data_ptr(), st["ws"].numel(), _device.stream())
+        _lib.check_device(_device.stream())
+        dt = time.perf_counter() - t0
+        # z and u as views of the solver state (sinogram block, difference block)
+        ws, (oz0, oz1, ou0, ou1) = st["ws"], st["offs"]
+        S, M = int(np.prod(C.output_shape)), len(C.input_shape) * int(np.prod(C.input_shape))
+
+        def view(off, n, shape):
+            return ws[off:off + 4 * n].view(torch.float32).view(shape)
+
+        dshape = (len(C.input_shape),) + tuple(C.input_shape)
+        self.z = (view(oz0, S, C.output_shape), view(oz1, M, dshape))
+        self.u = (view(ou0, S, C.output_shape), view(ou1, M, dshape))
+        self._Ax = None
+        rec = itstat.cpu().numpy()
+        for k in range(self.maxiter):
+            self.iterations.append(PADMMRecord(self.itnum + k, self._elapsed + dt * (k + 1) / self.maxiter,
+                                               float(rec[k, 0]), float(rec[k, 1]), float(rec[k, 2])))
+        self._elapsed += dt
+        self.itnum += self.maxiter
+        if self.nanstop and not self._working_vars_finite():
+            raise ValueError("NaN or Inf value encountered in a working variable during the fused solve.")
+        return self.x
+
     def solve(self, callback: Optional[Callable] = None):
         """Run ``maxiter`` iterations (Optimizer.solve, _common.py:287-320)."""
+        if self.fused is not False and callback is None:
+            plan = self._fused_plan()
+            if plan is None and self.fused is True:
+                raise ValueError("fused=True: the problem is not the fused CT-TV proximal ADMM pattern")
+            if plan is not None:
+                return self._solve_fused(plan)
         t0 = time.perf_counter()
         evaluatable = getattr(self.f, "has_eval", False) and getattr(self.g, "has_eval", False)
         for self.itnum in range(self.itnum, self.itnum + self.maxiter):

@@ -80,3 +80,59 @@ def test_padmm_3d_vs_oracle(cuda):
     adj = lambda v: ctref.xray3d_back_project(v, M32, shape, np.float32, np.float64)
     s, x, x64, _ = _padmm_case(cuda, H, fwd, adj, y, shape, iters=20)
     assert ctref.rel_l2(x, x64) <= 1e-4
+
+
+def _padmm_solver(cuda, H, y, shape, fused, lam=0.5, alpha=10.0, rho=0.05, iters=30, mu_nu=None):
+    D = linop.FiniteDifference(shape, append=0)
+    A = linop.VerticalStack((H, alpha * D))
+    mu, nu = mu_nu if mu_nu else ProximalADMM.estimate_parameters(A, maxiter=100, seed=0)
+    g = functional.SeparableFunctional((loss.SquaredL2Loss(y=torch.from_numpy(y).to(cuda)),
+                                        (lam / alpha) * functional.L21Norm()))
+    return ProximalADMM(f=functional.ZeroFunctional(), g=g, A=A, rho=rho, mu=mu, nu=nu, maxiter=iters,
+                        fused=fused), (mu, nu)
+
+
+@pytest.mark.parametrize("three", [False, True])
+def test_padmm_fused_matches_generic(cuda, three):
+    """The native solver (ct_padmm_tv_solve) against the generic step loop on
+    the same operators: the same arithmetic up to float32 rounding order."""
+    if three:
+        shape, det, nv = (8, 16, 16), (8, 23), 12
+        M = linop.XRayTransform3D.matrices_from_euler_angles(shape, det, "X",
+                                                             np.linspace(0, np.pi, nv, endpoint=False)[:, None])
+        H = linop.XRayTransform3D(shape, M, det)
+        x_gt = np.zeros(shape, np.float32)
+        x_gt[2:6, 4:12, 3:11] = 1.0
+    else:
+        shape = (32, 32)
+        H = linop.XRayTransform2D(shape, np.linspace(0, np.pi, 30, endpoint=False))
+        x_gt = workloads.random_ellipses(32, 5, 2)
+    y = H(torch.from_numpy(x_gt).to(cuda)).cpu().numpy()
+    a, mn = _padmm_solver(cuda, H, y, shape, fused=True)
+    xa = a.solve().cpu().numpy()
+    assert a._fused_state is not None  # the native path ran
+    b, _ = _padmm_solver(cuda, H, y, shape, fused=False, mu_nu=mn)
+    xb = b.solve().cpu().numpy()
+    assert ctref.rel_l2(xa, xb) <= 1e-5
+    ha, hb = a.history(transpose=True), b.history(transpose=True)
+    np.testing.assert_allclose(ha.Prml_Rsdl, hb.Prml_Rsdl, rtol=1e-4)
+    np.testing.assert_allclose(ha.Dual_Rsdl, hb.Dual_Rsdl, rtol=1e-4, atol=1e-9)
+    np.testing.assert_allclose(ha.Objective, hb.Objective, rtol=1e-5)
+    for za, zb in zip(a.z, b.z):
+        assert ctref.rel_l2(za.cpu().numpy(), zb.cpu().numpy()) <= 1e-5
+
+
+def test_padmm_fused_continuation(cuda):
+    """Two calls of 10 iterations continue from the solver state and give
+    exactly the iterates of one call of 20."""
+    shape = (32, 32)
+    H = linop.XRayTransform2D(shape, np.linspace(0, np.pi, 30, endpoint=False))
+    y = H(torch.from_numpy(workloads.random_ellipses(32, 5, 2)).to(cuda)).cpu().numpy()
+    a, mn = _padmm_solver(cuda, H, y, shape, fused=True, iters=20)
+    xa = a.solve()
+    b, _ = _padmm_solver(cuda, H, y, shape, fused=True, iters=10, mu_nu=mn)
+    b.solve()
+    xb = b.solve()
+    assert torch.equal(xa, xb)
+    assert len(b.history()) == 20
+    assert [r.Prml_Rsdl for r in a.history()] == [r.Prml_Rsdl for r in b.history()]
