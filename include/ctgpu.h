@@ -528,6 +528,45 @@ ct_status ct_admm_tv3d_solve(const ct_admm_tv3d_desc* d, const float* y, float* 
                              size_t workspace_bytes, ct_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Unrolled CG block of MoDL with a hand-written backward                   */
+/* (scico.flax.inverse.cg_solver, scico/flax/inverse.py:113-158)            */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * maxiter steps of CG on (gram_scale H^T H + lam I) x = b for nsys images
+ * sharing the 2D projector H, from x0 (or 0), float32 vectors and float64
+ * per-image scalars (the fixed-iteration solver the MoDL network unrolls,
+ * without a stopping test).  ct_cg_block_fwd records the iterates in a tape
+ * (recompute = 0) or only the step scalars (recompute = 1: the backward
+ * recomputes the iterates from the block's inputs b, lam, x0, its
+ * checkpoint).  ct_cg_block_bwd runs the reverse recurrence of the steps
+ * (the gradient of a loss through x) and returns the gradients of b, x0
+ * (optional) and lam (summed over the images, one float64 on the device).
+ * gram_scale is c^2 for a projector scaled by c.
+ */
+typedef struct ct_cg_block_desc {
+  ct_geom2d geom;
+  int32_t nsys;        /* images (batch)                                     */
+  int32_t maxiter;     /* CG steps                                           */
+  int32_t recompute;   /* 1: the backward recomputes the iterates            */
+  float gram_scale;    /* A = gram_scale H^T H + lam I                        */
+} ct_cg_block_desc;
+
+ct_status ct_cg_block_workspace(const ct_cg_block_desc* d, size_t* tape_bytes,
+                                size_t* workspace_bytes);
+/* b, x0 (may be NULL: zero), x: nsys x rows x cols. */
+ct_status ct_cg_block_fwd(const ct_cg_block_desc* d, const float* b, float lam,
+                          const float* x0, float* x, void* tape, size_t tape_bytes,
+                          void* workspace, size_t workspace_bytes,
+                          ct_stream_t stream);
+/* gx: gradient of the loss with respect to x; b is needed with recompute;
+ * x0 as given to the forward (NULL: zero); gx0 may be NULL. */
+ct_status ct_cg_block_bwd(const ct_cg_block_desc* d, const float* gx, const float* b,
+                          float lam, const float* x0, void* tape, size_t tape_bytes,
+                          float* gb, float* gx0, double* glam, void* workspace,
+                          size_t workspace_bytes, ct_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Fused proximal ADMM for CT-TV (ProximalADMM, scico/optimize/_padmm.py)    */
 /* ------------------------------------------------------------------------ */
 

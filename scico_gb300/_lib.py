@@ -157,6 +157,16 @@ class AdmmTv3dDesc(ctypes.Structure):
     ]
 
 
+class CgBlockDesc(ctypes.Structure):
+    _fields_ = [
+        ("geom", Geom2D),
+        ("nsys", c_int32),
+        ("maxiter", c_int32),
+        ("recompute", c_int32),
+        ("gram_scale", c_float),
+    ]
+
+
 class PadmmTvDesc(ctypes.Structure):
     _fields_ = [
         ("nd", c_int32),
@@ -217,6 +227,9 @@ _SIGNATURES = {
     "ct_admm_tv3d_workspace": (ctypes.c_int, [P, P]),
     "ct_admm_tv3d_state": (ctypes.c_int, [P, P, P, P]),
     "ct_admm_tv3d_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),
+    "ct_cg_block_workspace": (ctypes.c_int, [P, P, P]),
+    "ct_cg_block_fwd": (ctypes.c_int, [P, P, c_float, P, P, P, c_size_t, P, c_size_t, P]),
+    "ct_cg_block_bwd": (ctypes.c_int, [P, P, P, c_float, P, P, c_size_t, P, P, P, P, c_size_t, P]),
     "ct_padmm_tv_workspace": (ctypes.c_int, [P, P]),
     "ct_padmm_tv_state": (ctypes.c_int, [P, P, P, P, P]),
     "ct_padmm_tv_solve": (ctypes.c_int, [P, P, P, P, c_int32, P, c_size_t, P]),

@@ -878,6 +878,12 @@ bool sched_lookup(const ct_geom2d* g, int batch, SchedVal& out) {
 
 uint32_t proj2d_wait_polls() { return g_wait_polls.load(std::memory_order_relaxed); }
 
+ct_status proj2d_sum_splits(const float* part, float* out, size_t n, int nsplit, cudaStream_t s) {
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+  k_sum_splits<<<blocks, 256, 0, s>>>(part, out, n, nsplit, n);
+  return launch_check("k_sum_splits");
+}
+
 Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch) {
   SchedVal v;
   return proj2d_plan_sched(g, batch, sched_lookup(g, batch, v) ? v.s : Sched2d{});

@@ -9,6 +9,10 @@
   steps; independent systems along leading batch axes (the reference maps
   the solver over a batch with ``lax.map``); optional recomputation of each
   step in the backward pass instead of keeping its intermediates.
+* :func:`cg_block` -- the same fixed-iteration CG on H^T H + lam I for a
+  2D projector, in native kernels whose backward is the hand-written
+  reverse recurrence of the CG steps (optionally recomputing the iterates
+  from the block's inputs).
 * :class:`ResNet` and :class:`MoDLNet` -- scico/flax/_models.py:121-193 and
   scico/flax/inverse.py:35-110 as torch modules on NCHW tensors.
 * :class:`ODPProxDnBlock`, :class:`ODPGrDescBlock` and :class:`ODPNet` --
@@ -113,6 +117,87 @@ def cg_solver(A: Callable, b: torch.Tensor, x0: Optional[torch.Tensor] = None, m
     return x
 
 
+def _native_projector(H):
+    """(XRayTransform2D, gram scale) when H is a 2D projector or a scalar
+    multiple of one (the native CG block applies s H^T H), else None."""
+    from . import linop
+
+    if isinstance(H, linop.XRayTransform2D):
+        return H, 1.0
+    if isinstance(H, linop.ScaledProjector) and isinstance(H.base, linop.XRayTransform2D):
+        return H.base, H.scale * H.scale
+    return None
+
+
+class _CGBlock(torch.autograd.Function):
+    """maxiter fixed CG steps on (s H^T H + lam I) x = b in the native kernels
+    (ct_cg_block_fwd), with the hand-written reverse recurrence
+    (ct_cg_block_bwd) as the backward."""
+
+    @staticmethod
+    def forward(ctx, b, lam, x0, H2, gs, maxiter, recompute):
+        from . import _lib
+
+        b = b.contiguous()
+        lam32 = float(lam.detach().reshape(-1)[0].float())
+        desc = _lib.CgBlockDesc(H2.geometry(), b.shape[0], int(maxiter), int(bool(recompute)), float(gs))
+        tb, wb = _lib.c_size_t(), _lib.c_size_t()
+        _lib.call("ct_cg_block_workspace", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(tb),
+                  _lib.ctypes.addressof(wb))
+        tape = _device.workspace(tb.value)
+        ws = _device.workspace(wb.value)
+        x = torch.empty_like(b)
+        x0c = x0.contiguous() if x0 is not None else None
+        _lib.call("ct_cg_block_fwd", _lib.ctypes.addressof(desc), b.data_ptr(), lam32,
+                  x0c.data_ptr() if x0c is not None else None, x.data_ptr(), tape.data_ptr(), tape.numel(),
+                  ws.data_ptr(), ws.numel(), _device.stream())
+        ctx.desc, ctx.tape, ctx.lam32, ctx.wbytes = desc, tape, lam32, wb.value
+        ctx.lam_shape, ctx.lam_dtype = lam.shape, lam.dtype
+        ctx.has_x0 = x0c is not None
+        ctx.save_for_backward(b, x0c if x0c is not None else b)
+        return x
+
+    @staticmethod
+    def backward(ctx, gx):
+        from . import _lib
+
+        b, x0 = ctx.saved_tensors
+        x0 = x0 if ctx.has_x0 else None
+        gx = gx.contiguous()
+        gb = torch.empty_like(gx)
+        gx0 = torch.empty_like(gx) if (x0 is not None and ctx.needs_input_grad[2]) else None
+        glam = torch.zeros(1, dtype=torch.float64, device=gx.device)
+        ws = _device.workspace(ctx.wbytes)
+        _lib.call("ct_cg_block_bwd", _lib.ctypes.addressof(ctx.desc), gx.data_ptr(), b.data_ptr(), ctx.lam32,
+                  x0.data_ptr() if x0 is not None else None, ctx.tape.data_ptr(), ctx.tape.numel(), gb.data_ptr(),
+                  gx0.data_ptr() if gx0 is not None else None, glam.data_ptr(), ws.data_ptr(), ws.numel(),
+                  _device.stream())
+        glam_t = glam.to(ctx.lam_dtype).reshape(ctx.lam_shape) if ctx.needs_input_grad[1] else None
+        return gb, glam_t, gx0, None, None, None, None
+
+
+def cg_block(H, b: torch.Tensor, lam: torch.Tensor, x0: Optional[torch.Tensor] = None, maxiter: int = 10,
+             recompute: bool = False) -> torch.Tensor:
+    r"""``maxiter`` fixed conjugate-gradient steps on
+    :math:`(H^T H + \lambda I) \mb{x} = \mb{b}` for a batch of images
+    (leading axis of ``b``), each with its own step sizes -- the
+    data-consistency block of MoDL (scico/flax/inverse.py:113-158) -- in the
+    native kernels with a hand-written backward (``ct_cg_block_fwd`` /
+    ``ct_cg_block_bwd``): the reverse recurrence of the CG steps, not
+    autograd over the vector operations.  ``H`` is an XRayTransform2D or a
+    scalar multiple of one; ``lam`` a one-element tensor (a trainable
+    parameter).  ``recompute``: the forward keeps only the step scalars and
+    the backward recomputes the iterates from ``b``, ``lam`` and ``x0``.
+    Gradients flow to ``b``, ``lam`` and ``x0``."""
+    nat = _native_projector(H)
+    if nat is None:
+        raise TypeError("cg_block needs an XRayTransform2D (or a scalar multiple of one)")
+    H2, gs = nat
+    if b.ndim != 3 or tuple(b.shape[1:]) != tuple(H2.input_shape) or b.dtype != torch.float32:
+        raise ValueError(f"cg_block: b must be float32 (batch, *{tuple(H2.input_shape)}), got {tuple(b.shape)}")
+    return _CGBlock.apply(b, lam, x0, H2, gs, int(maxiter), bool(recompute))
+
+
 class ResNet(torch.nn.Module):
     """Convolutional net with a residual connection
     (scico/flax/_models.py:121-193): ``depth - 1`` blocks of convolution
@@ -158,12 +243,21 @@ class MoDLNet(torch.nn.Module):
     image.  The ResNet is shared by all blocks and ``lmbda`` is a trainable
     scalar, as in the reference.  Input: projections ``(batch, *A.output_shape)``;
     output: ``(batch, *A.input_shape)``.
+
+    ``cg_impl``: "native" (default where the operator is an XRayTransform2D
+    or a scalar multiple of one) runs each CG block as :func:`cg_block`, the
+    native kernels with the hand-written backward; "autograd" runs
+    :func:`cg_solver` (torch autograd over the unrolled vector operations),
+    which also serves any other operator.
     """
 
     def __init__(self, operator, depth: int, channels: int, num_filters: int, block_depth: int,
                  kernel_size: Tuple[int, int] = (3, 3), strides: Tuple[int, int] = (1, 1),
-                 lmbda_ini: float = 0.5, cg_iter: int = 10, cg_recompute: bool = False):
+                 lmbda_ini: float = 0.5, cg_iter: int = 10, cg_recompute: bool = False, cg_impl: str = "native"):
         super().__init__()
+        if cg_impl not in ("native", "autograd"):
+            raise ValueError(f"cg_impl must be 'native' or 'autograd', got {cg_impl!r}")
+        self.cg_native = cg_impl == "native" and _native_projector(operator) is not None
         if channels != 1:
             raise ValueError("MoDLNet here reconstructs single-channel images (channels=1)")
         self.operator = operator
@@ -185,7 +279,10 @@ class MoDLNet(torch.nn.Module):
         for _ in range(self.depth):
             z = self.resnet(x.unsqueeze(1)).squeeze(1)
             b = Ahb + lm * z
-            x = cg_solver(gram, b, maxiter=self.cg_iter, batch_dims=1, recompute=self.cg_recompute)
+            if self.cg_native and y.dtype == torch.float32:
+                x = cg_block(H, b, self.lmbda, maxiter=self.cg_iter, recompute=self.cg_recompute)
+            else:
+                x = cg_solver(gram, b, maxiter=self.cg_iter, batch_dims=1, recompute=self.cg_recompute)
         return x
 
 
