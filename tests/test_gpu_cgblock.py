@@ -3,11 +3,14 @@
 fixed-iteration CG run by torch autograd over the vector operations
 (inverse.cg_solver, scico/flax/inverse.py:113-158), on the GPU projector.
 
-Values and gradients (of b, lam and x0) agree to 1e-5 / 1e-4 where CG
-converges steadily (lam 10, or 3 steps at lam 0.1); at 10 unconverged steps
-with lam 0.1 both float32 implementations move apart by the rounding the
-recurrence amplifies, so the bar there is 3x the distance of each from a
-float64 run of the autograd recurrence on the float64 oracle matrix.
+Values and gradients (of b, lam and x0) agree to 1e-5 / 1e-4 while the
+residual stays well above float32 rounding (4 steps at lam 10, 3 steps at
+lam 0.1).  Where it does not -- 10 unconverged steps at lam 0.1, or 10
+steps at lam 10, by which CG has reached float32 round-off and the reverse
+recurrence divides by residual norms at the rounding floor -- any float32
+implementation's gradients are rounding-dominated, so the bar there is 3x
+the distance of the autograd float32 recurrence from a float64 run of the
+same recurrence on the float64 oracle matrix.
 Recomputation from the block's inputs reproduces the taped backward bit
 for bit; a second backward on the same tape gives the same gradients."""
 
@@ -51,7 +54,7 @@ def _both(H, b, lam_val, iters, x0=None, w_seed=3):
     return out
 
 
-@pytest.mark.parametrize("lam,iters", [(10.0, 10), (0.1, 3)])
+@pytest.mark.parametrize("lam,iters", [(10.0, 4), (0.1, 3)])
 @pytest.mark.parametrize("with_x0", [False, True])
 def test_cg_block_matches_autograd(cuda, lam, iters, with_x0):
     H, _ = _op()
@@ -64,17 +67,19 @@ def test_cg_block_matches_autograd(cuda, lam, iters, with_x0):
         assert _rel(a, c) <= 1e-4, (_rel(a, c), a.shape)
 
 
-def test_cg_block_unconverged_vs_float64(cuda):
-    """10 steps at lam 0.1: both float32 recurrences against float64."""
+@pytest.mark.parametrize("lam", [0.1, 10.0])
+def test_cg_block_ten_steps_vs_float64(cuda, lam):
+    """10 steps (unconverged at lam 0.1, at round-off at lam 10): both
+    float32 recurrences against float64."""
     H, g = _op(n=24, nv=16)
     gen = torch.Generator().manual_seed(2)
     b = torch.randn((2,) + H.input_shape, generator=gen).to(cuda)
-    (xn, gn), (xa, ga) = _both(H, b, 0.1, 10)
+    (xn, gn), (xa, ga) = _both(H, b, lam, 10)
     D = DenseOp(H, g, cuda)
     b64 = b.double().requires_grad_()
-    lam64 = torch.full((1,), 0.1, dtype=torch.float64, device=cuda, requires_grad=True)
-    gram = lambda v: inverse.back_project(D, inverse.project(D, v)) + lam64 * v
-    x64 = inverse.cg_solver(gram, b64, maxiter=10, batch_dims=1)
+    lam64 = torch.full((1,), lam, dtype=torch.float64, device=cuda, requires_grad=True)
+    gram64 = lambda v: inverse.back_project(D, inverse.project(D, v)) + lam64 * v
+    x64 = inverse.cg_solver(gram64, b64, maxiter=10, batch_dims=1)
     w = torch.randn(b.shape, generator=torch.Generator().manual_seed(3)).to(cuda).double()
     g64 = torch.autograd.grad((w * x64).sum(), [b64, lam64])
     fx = _rel(xa, x64.detach())
