@@ -7,12 +7,12 @@
 //
 // Forward (A), tile-owned pixel-driven sweep, two kernels:
 //   k_proj2d_fwd_strips  A CTA owns a strip of 32 image rows x 256 columns,
-//     copied once into padded shared memory with bulk (TMA) copies, and a run
-//     of views.  For each view the 8 warps take the strip's 8 32x32 tiles;
-//     lane r holds tile row r in registers and walks its 32 pixels in the
-//     direction in which k never decreases, carrying the running sums of the
-//     current bin and the next in registers and storing finished bins in its
-//     shared-memory partial row.  The 32 partial rows are summed in row
+//     loaded once as eight 32x32 tensor-map boxes (TMA, 128-B swizzle, zero
+//     fill outside the image), and a run of views.  For each view the 8
+//     warps take the strip's 8 tiles; lane r holds tile row r in registers
+//     and walks its 32 pixels in the direction in which k never decreases,
+//     carrying the running sums of the current bin and the next in registers
+//     and storing finished bins in its shared-memory partial row.  The 32 partial rows are summed in row
 //     order into the tile's bins; the warps need no barrier until every view
 //     of the run is done, then the 8 tiles are summed in tile order into the
 //     strip's bins of each view.
@@ -37,6 +37,8 @@
 #include <vector>
 #include <mutex>
 
+#include <cuda.h>  // CUtensorMap and the tensor-map encoder's types
+
 #include "common.cuh"
 #include "tma.cuh"
 
@@ -45,7 +47,6 @@ namespace {
 constexpr int kT = 32;          // forward tile edge: rows = lanes, columns = registers
 constexpr int kCW = 256;        // forward strip width (8 tiles)
 constexpr int kFW = 8;          // warps of a forward CTA (one tile each)
-constexpr int kRS = kCW + 4;    // strip row stride in floats: 16-B rows, conflict-free LDS.128
 constexpr int kFwdTargetCtas = 1824;
 constexpr int kLSDefault = 47;  // partial-row stride when projected pixels are at most one bin wide
 constexpr int kGL = 16;         // strips read per round by a forward gather warp
@@ -257,7 +258,7 @@ struct FwdArgs {
   int rows, cols, nv;
   int L, LS, cspan;
   int n_chunks, vpc;
-  int bulk;             // 1 = strip rows by cp.async.bulk
+  int tensor;           // 1 = strip tiles by tensor-map loads (the kernel's map parameter)
   uint32_t max_polls;   // poll limit of the strip-copy wait
   int* errflag;
   const double* skip;
@@ -272,14 +273,18 @@ __device__ __forceinline__ void strip_bins(const ViewParams& p, int i0, int c0, 
   span = (int)floorf(hi) - base + 2;
 }
 
-// Shared memory of k_proj2d_fwd_strips: a 16-B header (the copy barrier),
-// then one region used twice: first the 32 x kRS strip, then, once every lane
-// holds its tile row in registers, the partial rows [kFW][32][LS]; then the
-// tiles' bins of every view of the CTA's run [kMaxVpc][kFW][L]; then the
-// per-view parameters of the run (FwdViewSmem).
+// Shared memory of k_proj2d_fwd_strips, from the first 1024-B boundary of the
+// dynamic allocation: one region used twice, first the strip as kFW 32x32
+// tiles (4 KB each, 128-B swizzled: the 16-B chunk q of tile row r sits at
+// chunk q ^ (r & 7) of the row's 128 bytes), then, once every lane holds its
+// tile row in registers, the partial rows [kFW][32][LS]; then the tiles' bins
+// of every view of the CTA's run [kMaxVpc][kFW][L]; then the per-view
+// parameters of the run (FwdViewSmem); then the copy barrier.
 __host__ __device__ constexpr size_t fwd_region_floats(int LS) {
-  return (size_t)kT * kRS > (size_t)kFW * kT * LS ? (size_t)kT * kRS : (size_t)kFW * kT * LS;
+  return (size_t)kFW * kT * kT > (size_t)kFW * kT * LS ? (size_t)kFW * kT * kT : (size_t)kFW * kT * LS;
 }
+// Float offset of element (r, c) of a 32x32 tile in the swizzled layout.
+__host__ __device__ constexpr int swz(int r, int c) { return r * kT + ((((c >> 2) ^ (r & 7)) << 2) | (c & 3)); }
 constexpr int kMaxVpc = 16;  // views per forward CTA (upper bound of the plan's vpc)
 __host__ __device__ constexpr size_t fwd_tbins_floats(int L) { return (size_t)kMaxVpc * kFW * L; }
 struct FwdViewSmem {
@@ -331,47 +336,42 @@ __device__ __forceinline__ void fwd_view_params(const FwdArgs& a, FwdViewSmem* v
 // stride as a compile-time constant (its default-geometry value, so the row
 // sums address with immediates), or 0 for a.LS.
 template <int LSC>
-__global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs a) {
+__global__ void __launch_bounds__(kFW * 32, 3)
+    k_proj2d_fwd_strips(const FwdArgs a, const __grid_constant__ CUtensorMap tmap) {
   const int LS = LSC ? LSC : a.LS;
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
-  float* strip = reinterpret_cast<float*>(smem_raw + 16);            // [32][kRS]
-  float* part = strip;                                               // [kFW][32][LS]
-  float* tbins = strip + fwd_region_floats(LS);                      // [kMaxVpc][kFW][L]
+  const uint32_t sbase = ct::smem_u32(smem_raw);
+  float* tiles = reinterpret_cast<float*>(smem_raw + (((sbase + 1023u) & ~1023u) - sbase));  // [kFW][32][32]
+  float* part = tiles;                                               // [kFW][32][LS]
+  float* tbins = tiles + fwd_region_floats(LS);                      // [kMaxVpc][kFW][L]
   FwdViewSmem* vs = reinterpret_cast<FwdViewSmem*>(tbins + fwd_tbins_floats(a.L));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(vs + 1);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int s = blockIdx.x;
   const int ti = s / a.n_chunks, ch = s - ti * a.n_chunks;
   const int i0 = ti * kT, c0 = ch * kCW;
   const int b = blockIdx.z;
-  const float* im = a.img + (size_t)b * a.rows * a.cols;
 
   const int vbeg = blockIdx.y * a.vpc;
   const int vend = min(a.nv, vbeg + a.vpc);
 
-  // ---- stage the 32 x 256 strip (zero outside the image) -------------------
-  const int vrows = min(kT, a.rows - i0);
-  const int vcols = min(kCW, a.cols - c0);
+  // ---- stage the strip's tiles (zero outside the image) ---------------------
+  // Tiles that start right of the image are not loaded: their warps have
+  // nothing to do (span 0 in every view).
+  const int ntl = min(kFW, (a.cols - c0 + kT - 1) / kT);
   int timed_out = 0;
-  if (a.bulk) {
+  if (a.tensor) {
     if (tid == 0) {
       ct::mbar_init(bar, 1);
       ct::fence_barrier_init();
     }
     __syncthreads();
     if (tid == 0) {
-      const uint32_t row_bytes = (uint32_t)vcols * 4u;
-      ct::mbar_arrive_expect_tx(bar, row_bytes * (uint32_t)vrows);
-      for (int r = 0; r < vrows; ++r)
-        ct::bulk_g2s(strip + r * kRS, im + (size_t)(i0 + r) * a.cols + c0, row_bytes, bar);
+      ct::mbar_arrive_expect_tx(bar, (uint32_t)(ntl * kT * kT * 4));
+      for (int w = 0; w < ntl; ++w) ct::tensor_g2s_3d(tiles + w * kT * kT, &tmap, c0 + w * kT, i0, b, bar);
     }
-    // zero what the copies do not cover (disjoint addresses): warp w, rows
-    // w, w+8, ...
-    for (int r = warp; r < kT; r += kFW)
-      for (int c = lane; c < kRS; c += 32)
-        if (r >= vrows || c >= vcols) strip[r * kRS + c] = 0.0f;
     fwd_view_params(a, vs, i0, c0, ch);
     if (!ct::mbar_wait_bounded(bar, 0, a.max_polls)) {
       timed_out = 1;
@@ -381,9 +381,14 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
       ct::mbar_wait_bounded(bar, 0, kMaxPolls);
     }
   } else {
-    for (int r = warp; r < kT; r += kFW)
-      for (int c = lane; c < kRS; c += 32)
-        strip[r * kRS + c] = (r < vrows && c < vcols) ? __ldg(im + (size_t)(i0 + r) * a.cols + c0 + c) : 0.0f;
+    // the same layout by plain loads (rows not 16-B strided or image not
+    // 16-B aligned): consecutive threads read consecutive columns
+    const float* im = a.img + (size_t)b * a.rows * a.cols;
+    for (int e = tid; e < ntl * kT * kT; e += kFW * 32) {
+      const int w = e >> 10, r = (e >> 5) & 31, c = e & 31;
+      const int gi = i0 + r, gj = c0 + w * kT + c;
+      tiles[w * kT * kT + swz(r, c)] = (gi < a.rows && gj < a.cols) ? __ldg(im + (size_t)gi * a.cols + gj) : 0.0f;
+    }
     fwd_view_params(a, vs, i0, c0, ch);
   }
   if (__syncthreads_or(timed_out)) {
@@ -404,17 +409,17 @@ __global__ void __launch_bounds__(kFW * 32, 3) k_proj2d_fwd_strips(const FwdArgs
   // this lane's tile row, kept in registers for all the CTA's views
   float xr[kT];
   {
-    const float* row = strip + lane * kRS + warp * kT;
+    const float* row = tiles + warp * kT * kT + lane * kT;
 #pragma unroll
     for (int q = 0; q < kT / 4; ++q) {
-      const float4 f = *reinterpret_cast<const float4*>(row + 4 * q);
+      const float4 f = *reinterpret_cast<const float4*>(row + ((q ^ (lane & 7)) << 2));
       xr[4 * q] = f.x;
       xr[4 * q + 1] = f.y;
       xr[4 * q + 2] = f.z;
       xr[4 * q + 3] = f.w;
     }
   }
-  __syncthreads();  // the strip is dead from here: its bytes become partial rows
+  __syncthreads();  // the tiles are dead from here: their bytes become partial rows
   // From here to the combine every warp works alone on its tile: its partial
   // rows, its column products and its rows of the tile bins.
   float* wpart = part + warp * kT * LS;
@@ -763,8 +768,46 @@ int* errflag_ptr() {
   return cached[dev];
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null where the driver does not provide it.
+using TensorMapEncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                       const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                       CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+TensorMapEncodeFn tensor_map_encoder() {
+  static const TensorMapEncodeFn fn = []() -> TensorMapEncodeFn {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<TensorMapEncodeFn>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of a float32 image batch [batch][rows][cols] read as 32x32 boxes
+// with 128-B swizzle and zero fill outside the image.  Needs 16-B strided
+// rows and a 16-B aligned base; false where the map cannot be made.
+bool encode_image_map(CUtensorMap* m, const float* img, int rows, int cols, int batch) {
+  if ((cols & 3) != 0 || !ct::aligned(img, 16)) return false;
+  const TensorMapEncodeFn enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)batch};
+  const cuuint64_t strides[2] = {(cuuint64_t)cols * 4u, (cuuint64_t)rows * cols * 4u};
+  const cuuint32_t box[3] = {(cuuint32_t)kT, (cuuint32_t)kT, 1u};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(img), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 size_t fwd_smem_bytes(int LS, int L) {
-  return 16 + sizeof(float) * (fwd_region_floats(LS) + fwd_tbins_floats(L)) + sizeof(FwdViewSmem);
+  // up to 1008 bytes to the first 1024-B boundary (the allocation starts
+  // 16-B aligned), then the region, tile bins, view parameters and barrier
+  return 1008 + sizeof(float) * (fwd_region_floats(LS) + fwd_tbins_floats(L)) + sizeof(FwdViewSmem) + 16;
 }
 
 size_t adj_smem_bytes(int W) {
@@ -919,16 +962,18 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   a.cspan = p.cspan;
   a.n_chunks = p.n_chunks;
   a.vpc = p.vpc;
-  a.bulk = ((g->cols & 3) == 0 && aligned(img, 16)) ? 1 : 0;
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  a.tensor = encode_image_map(&tmap, img, g->rows, g->cols, batch) ? 1 : 0;
   a.max_polls = g_wait_polls.load(std::memory_order_relaxed);
   a.errflag = errflag_ptr();
   a.skip = skip;
   if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
   dim3 g1(p.n_strips, p.fwd_groups, batch);
   if (p.LS == kLSDefault)
-    k_proj2d_fwd_strips<kLSDefault><<<g1, kFW * 32, p.fwd_smem, s>>>(a);
+    k_proj2d_fwd_strips<kLSDefault><<<g1, kFW * 32, p.fwd_smem, s>>>(a, tmap);
   else
-    k_proj2d_fwd_strips<0><<<g1, kFW * 32, p.fwd_smem, s>>>(a);
+    k_proj2d_fwd_strips<0><<<g1, kFW * 32, p.fwd_smem, s>>>(a, tmap);
   ct_status st = launch_check("k_proj2d_fwd_strips");
   if (st != CT_OK) return st;
   dim3 g2(g->n_views, (g->det_count + 255) / 256, batch);

@@ -1,5 +1,6 @@
-// Bulk global->shared copies (cp.async.bulk, the TMA engine) completing on
-// an mbarrier, with a bounded wait.  Inline PTX for sm_90+ (sm_103a here).
+// Bulk and tensor-map global->shared copies (cp.async.bulk{,.tensor}, the TMA
+// engine) completing on an mbarrier, with a bounded wait.  Inline PTX for
+// sm_90+ (sm_103a here).
 #pragma once
 
 #include <stdint.h>
@@ -33,6 +34,20 @@ __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, u
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
           smem_u32(dst_smem)),
       "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Tiled tensor-map load of one box at element coordinates (x, y, z) into
+// shared memory, completing the box's bytes on `bar` (elements outside the
+// tensor are filled with zeros and counted).  x * element size must be a
+// multiple of 16 bytes; `tmap` is the address of a __grid_constant__
+// CUtensorMap kernel parameter.
+__device__ __forceinline__ void tensor_g2s_3d(void* dst_smem, const void* tmap, int x, int y, int z,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+      "%4}], [%5];" ::"r"(smem_u32(dst_smem)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
 

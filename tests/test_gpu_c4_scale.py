@@ -17,12 +17,19 @@ oracle's float64 weight matrix held as a sparse CSR matrix on the GPU
   directions lands at 1e-3 .. 4e-3 whatever the step (1e-5 .. 1e-7, where
   rounding takes over), so that case is held to median <= 2e-3 and worst
   <= 1e-2 and its numbers are reported.
-* float32 GPU network (the library's projector): its gradient against the
-  float64 twin's, within 3x the distance of the float32 twin (the same
-  sparse matrix rounded to float32) from the float64 one -- five blocks of
-  unconverged CG amplify float32 rounding for any float32 implementation.
+* float32 GPU network (the library's projector) with the benchmark's
+  CG(10): its gradient against the float64 twin's, within 3x the distance
+  of the float32 twin (the same sparse matrix rounded to float32) from the
+  float64 one.  Both are far (measured 0.68 relative, output 3 %): A^T A +
+  0.1 I has lambda_max ~ 6.3e4, so float32 rounding of A p (eps |A p|)
+  divided by lambda_min = 0.1 moves the iterate by ~eps kappa ~ 4 % once CG
+  has resolved the large eigencomponents (after ~6 steps); this holds for
+  any float32 evaluation of A, with float64 CG vectors too (2.5 %).
 * float32 GPU network by central finite differences (step 1e-3): reported,
   and held to 3x the same check run on the float32 twin.
+* The GPU network's gradient at CG(6), where float32 is still accurate
+  (float32 and float64 gradients 2e-4 apart), against central finite
+  differences of the float64 twin: 1e-3.
 Each test prints one C4SCALE line with its measurements.
 """
 
@@ -108,10 +115,14 @@ def _setup(cuda):
     return _STATE
 
 
-def _net(c, op, dtype=torch.float32):
+def _net(c, op, dtype=torch.float32, cg_iter=None, act="relu"):
     torch.manual_seed(c.weight_seed)
     net = inverse.MoDLNet(op, depth=c.depth, channels=1, num_filters=c.num_filters, block_depth=c.block_depth,
-                          lmbda_ini=c.lmbda_ini, cg_iter=c.cg_iter)
+                          lmbda_ini=c.lmbda_ini, cg_iter=c.cg_iter if cg_iter is None else cg_iter)
+    if act == "silu":
+        for i, m in enumerate(net.resnet.body):
+            if isinstance(m, torch.nn.ReLU):
+                net.resnet.body[i] = torch.nn.SiLU()
     return net.to(_STATE["x_gt"].device).to(dtype)
 
 
@@ -147,11 +158,7 @@ def _fd_errors(f, params, n_dir=20, eps=1e-6, seed=0):
 def test_c4_float64_twin_finite_differences(cuda, act):
     st = _setup(cuda)
     c = st["c"]
-    net = _net(c, st["S64"], torch.float64)
-    if act == "silu":
-        for i, m in enumerate(net.resnet.body):
-            if isinstance(m, torch.nn.ReLU):
-                net.resnet.body[i] = torch.nn.SiLU()
+    net = _net(c, st["S64"], torch.float64, act=act)
     yd, xd = st["y"].double(), st["x_gt"].double()
     eps = 1e-5 if act == "silu" else 1e-6
     errs = _fd_errors(lambda: ((net(yd) - xd) ** 2).mean(), list(net.parameters()), n_dir=20, eps=eps)
@@ -207,3 +214,53 @@ def test_c4_gpu_finite_differences(cuda):
     e_32 = _fd_check(loss(t32), list(t32.parameters()), n_dir=20, eps=1e-3)
     _report("f32_fd", {"worst_rel_gpu": e_gpu, "worst_rel_f32_twin": e_32, "directions": 20, "eps": 1e-3})
     assert e_gpu <= 3 * e_32 + 1e-3, (e_gpu, e_32)
+
+
+@pytest.mark.parametrize("act", ["silu", "relu"])
+def test_c4_gpu_gradient_vs_float64_finite_differences(cuda, act):
+    """The GPU network's own gradient (float32, native CG blocks with the
+    hand-written backward) against central finite differences of the float64
+    twin, along 20 random directions, at the workload's sizes with CG(6):
+    the longest CG in which float32 rounding of A p (relative eps |A p|,
+    divided by lambda_min = 0.1 in the small-eigenvalue directions of
+    A^T A + 0.1 I, lambda_max ~ 6.3e4) has not yet taken over -- float32 and
+    float64 gradients agree to ~2e-4 at CG(5..6), 6e-4 at CG(7), 8e-3 at
+    CG(8) and not at all at CG(10), for any float32 evaluation of A.  Held to
+    1e-3 with the smooth activation; with the ReLUs, whose kinks limit
+    central differences, to median 1e-3 and worst 1e-2."""
+    st = _setup(cuda)
+    c = st["c"]
+    y, x_gt = st["y"], st["x_gt"]
+    gpu = _net(c, st["H"], cg_iter=6, act=act)
+    t64 = _net(c, st["S64"], torch.float64, cg_iter=6, act=act)
+    t64.load_state_dict(gpu.state_dict())
+    assert gpu.cg_native
+    pg, p64 = list(gpu.parameters()), list(t64.parameters())
+    grads = torch.autograd.grad(((gpu(y) - x_gt) ** 2).mean(), pg)
+    gnorm = torch.sqrt(sum((gi.double() ** 2).sum() for gi in grads)).item()
+    yd, xd = y.double(), x_gt.double()
+    f = lambda: ((t64(yd) - xd) ** 2).mean()
+    eps = 1e-5 if act == "silu" else 1e-6
+    gen = torch.Generator().manual_seed(0)
+    errs = []
+    with torch.no_grad():
+        for _ in range(20):
+            d = [torch.randn(p.shape, generator=gen, dtype=torch.float64).to(p.device) for p in p64]
+            ad = sum((gi.double() * di).sum() for gi, di in zip(grads, d)).item()
+            for p, di in zip(p64, d):
+                p.add_(eps * di)
+            fp = f().item()
+            for p, di in zip(p64, d):
+                p.sub_(2 * eps * di)
+            fm = f().item()
+            for p, di in zip(p64, d):
+                p.add_(eps * di)
+            fd = (fp - fm) / (2 * eps)
+            errs.append(abs(ad - fd) / max(abs(fd), abs(ad), gnorm, 1e-30))
+    worst, med = max(errs), float(np.median(errs))
+    _report("gpu_vs_f64_fd_cg6_" + act, {"worst_rel": worst, "median_rel": med, "directions": 20, "eps": eps,
+                                         "cg_iter": 6})
+    if act == "silu":
+        assert worst <= 1e-3, worst
+    else:
+        assert med <= 1e-3 and worst <= 1e-2, (med, worst)
