@@ -71,13 +71,105 @@ __device__ __forceinline__ size_t axis_stride(const Shape3& sh, int k) {
   return st;
 }
 
+// Quad path (n[ND-1] % 4 == 0, every array 16-B aligned, N < 2^31): a
+// thread takes four consecutive elements along the last axis with 128-bit
+// loads and stores; the per-element arithmetic is the scalar path's, in the
+// same order.
+__device__ __forceinline__ float4 ld4(const float* __restrict__ p, size_t e) {
+  return *reinterpret_cast<const float4*>(p + e);
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, size_t e, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(p + e) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void unpack4(const float4 a, float (&v)[4]) {
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+}
+template <int ND>
+__device__ __forceinline__ void coords32(uint32_t e, const Shape3& sh, int (&c)[ND]) {
+  uint32_t r = e;
+#pragma unroll
+  for (int k = ND - 1; k >= 0; --k) {
+    const uint32_t q = r / (uint32_t)sh.n[k];
+    c[k] = (int)(r - q * (uint32_t)sh.n[k]);
+    r = q;
+  }
+}
+
+// Compensated (Kahan) float32 running sum: each thread's partial sums of the
+// residual norms and objective terms, combined over the grid in float64.
+// Per element the terms are float32 products; the compensation keeps a
+// partial sum of a few hundred terms within a few units of rounding, as a
+// float64 accumulation would, without float64 arithmetic per element (the
+// float64 pipe of this GPU runs at a small fraction of the float32 rate).
+struct KSum {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = ct::fsub(v, c);
+    const float t = ct::fadd(s, y);
+    c = ct::fsub(ct::fsub(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 // x <- x - (1/mu) (A^T t)(e):  A^T t = C^T t0 + alpha D^T t1, the adjoint's
 // view splits summed in order, D^T with the append=0 boundaries, axes in
 // order (linop/_stack.py:71-72, _diff.py).
 template <int ND>
 __global__ void __launch_bounds__(NT)
     k_pd_x(float* __restrict__ x, const float* __restrict__ adj, int nsplit, const float* __restrict__ t1,
-           Shape3 sh, size_t N, Scal s) {
+           Shape3 sh, size_t N, Scal s, int vec) {
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords32<ND>((uint32_t)e0, sh, c);
+      float ct[4], dt[4], xv[4];
+      unpack4(ld4(adj, e0), ct);
+      for (int q = 1; q < nsplit; ++q) {
+        float v[4];
+        unpack4(ld4(adj, (size_t)q * N + e0), v);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ct[j] = ct::fadd(ct[j], v[j]);
+      }
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        const float* tk = t1 + (size_t)k * N;
+        float fc[4], lo[4], hi[4];
+        unpack4(ld4(tk, e0), fc);
+        if (k < ND - 1) {
+          const size_t st = axis_stride<ND>(sh, k);
+          if (c[k] >= 1) {
+            unpack4(ld4(tk, e0 - st), lo);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) lo[j] = 0.0f;
+          }
+          const bool h = c[k] <= sh.n[k] - 2;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) hi[j] = h ? fc[j] : 0.0f;
+        } else {
+          const int cl = c[ND - 1], nl = sh.n[ND - 1];
+          lo[0] = cl >= 1 ? tk[e0 - 1] : 0.0f;
+          lo[1] = fc[0];
+          lo[2] = fc[1];
+          lo[3] = fc[2];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) hi[j] = cl + j <= nl - 2 ? fc[j] : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dt[j] = k == 0 ? ct::fsub(lo[j], hi[j]) : ct::fadd(dt[j], ct::fsub(lo[j], hi[j]));
+      }
+      unpack4(ld4(x, e0), xv);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        xv[j] = ct::fsub(xv[j], ct::fmul(s.inv_mu, ct::fadd(ct[j], ct::fmul(s.alpha, dt[j]))));
+      st4(x, e0, xv);
+    }
+    return;
+  }
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     float ct = adj[e];
     for (int q = 1; q < nsplit; ++q) ct = ct::fadd(ct, adj[(size_t)q * N + e]);
@@ -97,27 +189,48 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-// Sinogram block: a = (C x)[e];  pz = z0 + (1/nu)((a - z0) + u0);
+// Sinogram block, one element: a = (C x)[e];  pz = z0 + (1/nu)((a - z0) + u0);
 // z0' = (c y + pz) / (c + 1);  u0' = (u0 + a) - z0';  t0 = 2 u0' - u0.
+__device__ __forceinline__ void zu0_elem(float a, float z, float u, float ye, const Scal& s, float& zn, float& un,
+                                         float& tn, KSum& prim, KSum& dual, KSum& g0) {
+  const float pz = ct::fadd(z, ct::fmul(s.inv_nu, ct::fadd(ct::fsub(a, z), u)));
+  zn = __fdiv_rn(ct::fadd(ct::fmul(s.c, ye), pz), s.c1);
+  un = ct::fsub(ct::fadd(u, a), zn);
+  tn = ct::fsub(ct::fmul(2.0f, un), u);
+  const float r = ct::fsub(a, zn), d = ct::fsub(zn, z), q = ct::fsub(ye, zn);
+  prim.add(ct::fmul(r, r));
+  dual.add(ct::fmul(d, d));
+  g0.add(ct::fmul(q, q));
+}
+
 __global__ void __launch_bounds__(NT)
     k_pd_zu0(const float* __restrict__ ax, const float* __restrict__ y, float* __restrict__ z0,
              float* __restrict__ u0, float* __restrict__ t0, size_t S, Scal s, double* __restrict__ slots,
-             double* __restrict__ partials, unsigned int* __restrict__ ticket) {
-  double prim = 0.0, dual = 0.0, g0 = 0.0;
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < S; e += (size_t)gridDim.x * NT) {
-    const float a = ax[e], z = z0[e], u = u0[e], ye = y[e];
-    const float pz = ct::fadd(z, ct::fmul(s.inv_nu, ct::fadd(ct::fsub(a, z), u)));
-    const float zn = __fdiv_rn(ct::fadd(ct::fmul(s.c, ye), pz), s.c1);
-    const float un = ct::fsub(ct::fadd(u, a), zn);
-    z0[e] = zn;
-    u0[e] = un;
-    t0[e] = ct::fsub(ct::fmul(2.0f, un), u);
-    const double r = (double)a - (double)zn, d = (double)zn - (double)z, q = (double)ye - (double)zn;
-    prim += r * r;
-    dual += d * d;
-    g0 += q * q;
+             double* __restrict__ partials, unsigned int* __restrict__ ticket, int vec) {
+  KSum prim, dual, g0;
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < S; e0 += 4 * (size_t)gridDim.x * NT) {
+      float a[4], z[4], u[4], ye[4], zn[4], un[4], tn[4];
+      unpack4(ld4(ax, e0), a);
+      unpack4(ld4(z0, e0), z);
+      unpack4(ld4(u0, e0), u);
+      unpack4(ld4(y, e0), ye);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) zu0_elem(a[j], z[j], u[j], ye[j], s, zn[j], un[j], tn[j], prim, dual, g0);
+      st4(z0, e0, zn);
+      st4(u0, e0, un);
+      st4(t0, e0, tn);
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < S; e += (size_t)gridDim.x * NT) {
+      float zn, un, tn;
+      zu0_elem(ax[e], z0[e], u0[e], y[e], s, zn, un, tn, prim, dual, g0);
+      z0[e] = zn;
+      u0[e] = un;
+      t0[e] = tn;
+    }
   }
-  double v[3] = {prim, dual, g0}, out[3];
+  double v[3] = {prim.value(), dual.value(), g0.value()}, out[3];
   if (ct::grid_reduce_last<NT, 3>(v, partials, ticket, out)) {
     slots[P_PRIMAL2] = out[0];
     slots[P_DUAL2] = out[1];
@@ -125,50 +238,122 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-// FD block: ax_k = alpha (D x)_k;  pz_k = z1_k + (1/nu)((ax_k - z1_k) + u1_k);
-// z1' = L2,1 prox of pz with threshold thr (_norm.py:254-263);
-// u1_k' = (u1_k + ax_k) - z1_k';  t1_k = 2 u1_k' - u1_k.  The last block adds
-// the sinogram block's sums and writes the iteration's record.
+// FD block, one element: ax_k = alpha (D x)_k;
+// pz_k = z1_k + (1/nu)((ax_k - z1_k) + u1_k); z1' = L2,1 prox of pz with
+// threshold thr (_norm.py:254-263); u1_k' = (u1_k + ax_k) - z1_k';
+// t1_k = 2 u1_k' - u1_k.
+template <int ND>
+__device__ __forceinline__ void zu1_elem(const float (&ax)[ND], const float (&z)[ND], const float (&u)[ND],
+                                         const Scal& s, float (&zn)[ND], float (&un)[ND], float (&tn)[ND],
+                                         KSum& prim, KSum& dual, KSum& g1) {
+  float pz[ND];
+  float ss = 0.0f;
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    pz[k] = ct::fadd(z[k], ct::fmul(s.inv_nu, ct::fadd(ct::fsub(ax[k], z[k]), u[k])));
+    ss = k == 0 ? ct::fmul(pz[k], pz[k]) : ct::fadd(ss, ct::fmul(pz[k], pz[k]));
+  }
+  const float len = __fsqrt_rn(ss);
+  float nl = ct::fsub(len, s.thr);
+  nl = ct::fmul(0.5f, ct::fadd(nl, fabsf(nl)));
+  float zz = 0.0f;
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    zn[k] = ct::fmul(nl, len != 0.0f ? __fdiv_rn(pz[k], len) : 0.0f);
+    un[k] = ct::fsub(ct::fadd(u[k], ax[k]), zn[k]);
+    tn[k] = ct::fsub(ct::fmul(2.0f, un[k]), u[k]);
+    const float r = ct::fsub(ax[k], zn[k]), d = ct::fsub(zn[k], z[k]);
+    prim.add(ct::fmul(r, r));
+    dual.add(ct::fmul(d, d));
+    zz = k == 0 ? ct::fmul(zn[k], zn[k]) : ct::fadd(zz, ct::fmul(zn[k], zn[k]));
+  }
+  g1.add(__fsqrt_rn(zz));
+}
+
+// FD block over the grid; the last block adds the sinogram block's sums and
+// writes the iteration's record.
 template <int ND>
 __global__ void __launch_bounds__(NT)
     k_pd_zu1(const float* __restrict__ x, float* __restrict__ z1, float* __restrict__ u1, float* __restrict__ t1,
              Shape3 sh, size_t N, Scal s, double* __restrict__ itstat, int maxiter, double* __restrict__ slots,
-             double* __restrict__ partials, unsigned int* __restrict__ ticket) {
-  double prim = 0.0, dual = 0.0, g1 = 0.0;
-  for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-    int c[ND];
-    coords<ND>(e, sh, c);
-    const float xc = x[e];
-    float ax[ND], z[ND], u[ND], pz[ND];
-    float ss = 0.0f;
+             double* __restrict__ partials, unsigned int* __restrict__ ticket, int vec) {
+  KSum prim, dual, g1;
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords32<ND>((uint32_t)e0, sh, c);
+      float xc[4], ax[ND][4], z[ND][4], u[ND][4];
+      unpack4(ld4(x, e0), xc);
 #pragma unroll
-    for (int k = 0; k < ND; ++k) {
-      const float xn = c[k] <= sh.n[k] - 2 ? x[e + axis_stride<ND>(sh, k)] : xc;
-      ax[k] = ct::fmul(s.alpha, ct::fsub(xn, xc));
-      z[k] = z1[(size_t)k * N + e];
-      u[k] = u1[(size_t)k * N + e];
-      pz[k] = ct::fadd(z[k], ct::fmul(s.inv_nu, ct::fadd(ct::fsub(ax[k], z[k]), u[k])));
-      ss = k == 0 ? ct::fmul(pz[k], pz[k]) : ct::fadd(ss, ct::fmul(pz[k], pz[k]));
-    }
-    const float len = __fsqrt_rn(ss);
-    float nl = ct::fsub(len, s.thr);
-    nl = ct::fmul(0.5f, ct::fadd(nl, fabsf(nl)));
-    double zz = 0.0;
+      for (int k = 0; k < ND; ++k) {
+        float nx[4];
+        if (k < ND - 1) {
+          if (c[k] <= sh.n[k] - 2) {
+            unpack4(ld4(x, e0 + axis_stride<ND>(sh, k)), nx);
+          } else {
 #pragma unroll
-    for (int k = 0; k < ND; ++k) {
-      const float zn = ct::fmul(nl, len != 0.0f ? __fdiv_rn(pz[k], len) : 0.0f);
-      const float un = ct::fsub(ct::fadd(u[k], ax[k]), zn);
-      z1[(size_t)k * N + e] = zn;
-      u1[(size_t)k * N + e] = un;
-      t1[(size_t)k * N + e] = ct::fsub(ct::fmul(2.0f, un), u[k]);
-      const double r = (double)ax[k] - (double)zn, d = (double)zn - (double)z[k];
-      prim += r * r;
-      dual += d * d;
-      zz += (double)zn * (double)zn;
+            for (int j = 0; j < 4; ++j) nx[j] = xc[j];
+          }
+        } else {
+          const int cl = c[ND - 1], nl = sh.n[ND - 1];
+          nx[0] = cl <= nl - 2 ? xc[1] : xc[0];
+          nx[1] = cl + 1 <= nl - 2 ? xc[2] : xc[1];
+          nx[2] = cl + 2 <= nl - 2 ? xc[3] : xc[2];
+          nx[3] = cl + 3 <= nl - 2 ? x[e0 + 4] : xc[3];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ax[k][j] = ct::fmul(s.alpha, ct::fsub(nx[j], xc[j]));
+        unpack4(ld4(z1, (size_t)k * N + e0), z[k]);
+        unpack4(ld4(u1, (size_t)k * N + e0), u[k]);
+      }
+      float zn[ND][4], un[ND][4], tn[ND][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float a1[ND], z1v[ND], u1v[ND], zo[ND], uo[ND], to[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+          a1[k] = ax[k][j];
+          z1v[k] = z[k][j];
+          u1v[k] = u[k][j];
+        }
+        zu1_elem<ND>(a1, z1v, u1v, s, zo, uo, to, prim, dual, g1);
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+          zn[k][j] = zo[k];
+          un[k][j] = uo[k];
+          tn[k][j] = to[k];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        st4(z1, (size_t)k * N + e0, zn[k]);
+        st4(u1, (size_t)k * N + e0, un[k]);
+        st4(t1, (size_t)k * N + e0, tn[k]);
+      }
     }
-    g1 += sqrt(zz);
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e, sh, c);
+      const float xc = x[e];
+      float ax[ND], z[ND], u[ND], zn[ND], un[ND], tn[ND];
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        const float xn = c[k] <= sh.n[k] - 2 ? x[e + axis_stride<ND>(sh, k)] : xc;
+        ax[k] = ct::fmul(s.alpha, ct::fsub(xn, xc));
+        z[k] = z1[(size_t)k * N + e];
+        u[k] = u1[(size_t)k * N + e];
+      }
+      zu1_elem<ND>(ax, z, u, s, zn, un, tn, prim, dual, g1);
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        z1[(size_t)k * N + e] = zn[k];
+        u1[(size_t)k * N + e] = un[k];
+        t1[(size_t)k * N + e] = tn[k];
+      }
+    }
   }
-  double v[3] = {prim, dual, g1}, out[3];
+  double v[3] = {prim.value(), dual.value(), g1.value()}, out[3];
   if (ct::grid_reduce_last<NT, 3>(v, partials, ticket, out)) {
     const int it = (int)slots[P_ITER];
     if (itstat && it < maxiter) {
@@ -296,25 +481,35 @@ ct_status enqueue_iteration(const Ctx& c, cudaStream_t s) {
   else
     CT_TRY(ct::proj3d_adj_launch(&c.d->geom3, P.p3, c.at<float>(c.L.off_t0), adj, part, s, nullptr));
   const float* a = nsplit(P) > 1 ? part : adj;
+  float* t1 = c.at<float>(c.L.off_t1);
+  float* z1 = c.at<float>(c.L.off_z1);
+  float* u1 = c.at<float>(c.L.off_u1);
+  // quads along the last axis: its length a multiple of 4, 32-bit indices
+  const bool rows4 = P.sh.n[P.nd - 1] % 4 == 0 && P.N < (size_t(1) << 31);
+  const int vx = rows4 && ct::quad_ok(P.N, c.x, a, t1) ? 1 : 0;
+  const int vz1 = rows4 && ct::quad_ok(P.N, c.x, z1, u1, t1) ? 1 : 0;
   if (P.nd == 2)
-    k_pd_x<2><<<NB, NT, 0, s>>>(c.x, a, nsplit(P), c.at<float>(c.L.off_t1), P.sh, P.N, P.sc);
+    k_pd_x<2><<<NB, NT, 0, s>>>(c.x, a, nsplit(P), t1, P.sh, P.N, P.sc, vx);
   else
-    k_pd_x<3><<<NB, NT, 0, s>>>(c.x, a, nsplit(P), c.at<float>(c.L.off_t1), P.sh, P.N, P.sc);
+    k_pd_x<3><<<NB, NT, 0, s>>>(c.x, a, nsplit(P), t1, P.sh, P.N, P.sc, vx);
   CT_TRY(ct::launch_check("k_pd_x"));
   // C x
   if (P.nd == 2)
     CT_TRY(ct::proj2d_fwd_launch(&c.d->geom2, P.p2, c.x, sinox, 1, c.at<float>(c.L.off_fwd), s, nullptr));
   else
     CT_TRY(ct::proj3d_fwd_launch(&c.d->geom3, P.p3, c.x, sinox, c.at<void>(c.L.off_fwd), s, nullptr));
-  k_pd_zu0<<<NB, NT, 0, s>>>(sinox, c.y, c.at<float>(c.L.off_z0), c.at<float>(c.L.off_u0),
-                             c.at<float>(c.L.off_t0), P.S, P.sc, c.slots(), c.partials(), c.ticket());
+  float* z0 = c.at<float>(c.L.off_z0);
+  float* u0 = c.at<float>(c.L.off_u0);
+  float* t0 = c.at<float>(c.L.off_t0);
+  k_pd_zu0<<<NB, NT, 0, s>>>(sinox, c.y, z0, u0, t0, P.S, P.sc, c.slots(), c.partials(), c.ticket(),
+                             ct::quad_ok(P.S, sinox, c.y, z0, u0, t0));
   CT_TRY(ct::launch_check("k_pd_zu0"));
   if (P.nd == 2)
-    k_pd_zu1<2><<<NB, NT, 0, s>>>(c.x, c.at<float>(c.L.off_z1), c.at<float>(c.L.off_u1), c.at<float>(c.L.off_t1),
-                                  P.sh, P.N, P.sc, c.itstat, c.d->maxiter, c.slots(), c.partials(), c.ticket());
+    k_pd_zu1<2><<<NB, NT, 0, s>>>(c.x, z1, u1, t1, P.sh, P.N, P.sc, c.itstat, c.d->maxiter, c.slots(), c.partials(),
+                                  c.ticket(), vz1);
   else
-    k_pd_zu1<3><<<NB, NT, 0, s>>>(c.x, c.at<float>(c.L.off_z1), c.at<float>(c.L.off_u1), c.at<float>(c.L.off_t1),
-                                  P.sh, P.N, P.sc, c.itstat, c.d->maxiter, c.slots(), c.partials(), c.ticket());
+    k_pd_zu1<3><<<NB, NT, 0, s>>>(c.x, z1, u1, t1, P.sh, P.N, P.sc, c.itstat, c.d->maxiter, c.slots(), c.partials(),
+                                  c.ticket(), vz1);
   return ct::launch_check("k_pd_zu1");
 }
 
