@@ -65,6 +65,22 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM = 6800.0
 
 
+def solve_launches(cg_its):
+    """Kernel launches of one fused solve whose iterations ran cg_its CG
+    steps: A^T y, its split sum, z/u init and the call reset (4); per
+    iteration k_rhs, the projections of x when CG moved x in the previous
+    iteration or it is the first (forward strips and gather, residual,
+    adjoint: the graph's conditional IF node), the CG start, the CG loop body
+    (the graph's WHILE node runs it exactly CG_It times: forward strips and
+    gather, adjoint, lhs, CG update, direction = 6) and the z/u update; the
+    itstat epilogue (rhs, forward strips and gather, residual, record = 5).
+    CG_It comes from the solve's own itstat records."""
+    n = 4 + 5
+    for i, k in enumerate(cg_its):
+        dirty = i == 0 or cg_its[i - 1] > 0
+        n += 1 + (4 if dirty else 0) + 1 + 6 * k + 1
+    return n
+
 def _args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -474,16 +490,8 @@ def run_gpu(args):
         except Exception as exc:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
-    # Kernel launches of one solve: A^T y, its split sum, z/u init and the
-    # call reset (4); per iteration the pre phase (rhs, forward strips and
-    # gather, residual, itstat, adjoint, CG start = 7), the CG loop body (the
-    # graph's WHILE node runs it exactly CG_It times: forward strips and
-    # gather, adjoint, lhs, CG update, direction = 6), the z/u update and the
-    # ADMM loop step (2);
-    # the itstat epilogue (rhs, forward strips and gather, residual, itstat =
-    # 5).  CG_It comes from the solve's own itstat records.
     cg_its = [int(v) for v in itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()]
-    launches_per_step = 4 + sum(7 + 6 * k + 2 for k in cg_its) + 5
+    launches_per_step = solve_launches(cg_its)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -709,7 +717,7 @@ def run_gpu_3d(args):
                              f"to {k:.1f} + 2 pairs per ADMM iteration ({per_iter:.1f} s per iteration)"}
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
-    launches_per_step = 4 + sum(7 + 6 * k + 2 for k in cg_its) + 5  # as the 2D solver; projector = 2 kernels
+    launches_per_step = solve_launches(cg_its)  # as the 2D solver: forward 2 kernels, adjoint 1
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

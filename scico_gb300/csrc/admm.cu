@@ -11,17 +11,19 @@
 //
 // Per outer iteration (each kernel below is one launch; with graphs the
 // whole solve is captured once into a CUDA graph -- set-up, the iterations
-// as a conditional WHILE node that k_admm_next keeps running for maxiter
+// as a conditional WHILE node that k_zu keeps running for maxiter
 // iterations, the statistics epilogue -- and launched once per call; a batch
 // of scans is one graph with one such branch per scan):
 //   k_rhs         rhs = c A^T y + sum_i rho D^T(z_i - u_i); also the dual
 //                 residual ||sum_i rho D^T(z_i - z_i_old)|| of the previous
 //                 iteration
 //   A x           forward projection of the current x, k_resid2 gives
-//                 ||A x - y||^2 for the previous iteration's objective
-//   k_itstat      writes the previous iteration's itstat record
-//   A^T, k_lhs_finish<INIT>   lhs(x) = c A^T A x + rho D^T D x, r = rhs - lhs(x),
-//                 p = r, CG scalars (num, ||b||, tolerance) in float64
+//                 ||A x - y||^2 for the previous iteration's objective, then
+//                 A^T (A x); in the graph these three form a conditional IF
+//                 node that k_rhs opens only when CG moved x
+//   k_lhs_finish<INIT>   writes the previous iteration's itstat record, then
+//                 lhs(x) = c A^T A x + rho D^T D x, r = rhs - lhs(x), p = r,
+//                 CG scalars (num, ||b||, tolerance) in float64
 //   CG loop       A p, A^T, k_lhs_finish<PAP> (Ap, <p,Ap>), CG update,
 //                 direction.  In the graph the loop is a conditional WHILE
 //                 node whose condition the device sets (CG start and each
@@ -29,7 +31,9 @@
 //                 iterations; without a graph, cg_maxiter copies are launched
 //                 and become no-ops once CG has converged
 //   k_zu          Dx, z_i = prox(Dx + u_i), u_i += Dx - z_i, primal residual
-//                 and g_i(z_i) partial sums
+//                 and g_i(z_i) partial sums; in the graph its last block
+//                 counts the iteration and sets the iteration loop's
+//                 condition
 // lhs(x) and A x are kept from the last CG start while x is unchanged (no CG
 // step ran since): the deterministic kernels would recompute the same bits,
 // so the projections of x are skipped then.
@@ -353,12 +357,17 @@ __global__ void __launch_bounds__(NT) k_scale_splits(const float* __restrict__ s
   }
 }
 
+// In the solve graph (use_dirty != 0) k_rhs also sets the condition of the
+// iteration's projection node (a conditional IF node): run the projections of
+// x only when CG moved x since lhs(x) and A x were last computed.
 template <int ND>
 __global__ void __launch_bounds__(NT)
     k_rhs(const float* __restrict__ atyc, const float* __restrict__ z, const float* __restrict__ u,
           const float* __restrict__ dz, float* __restrict__ rhs, Shape3 sh, size_t N, TermParams tp,
           double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
-          int vec) {
+          int vec, cudaGraphConditionalHandle dirty, int use_dirty) {
+  if (use_dirty && blockIdx.x == 0 && threadIdx.x == 0)
+    cudaGraphSetConditional(dirty, slots[S_XCLEAN] == 0.0 ? 1u : 0u);
   double acc[1] = {0.0};
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
@@ -443,34 +452,46 @@ __global__ void __launch_bounds__(NT)
   if (ct::grid_sumk_last<NT, 1>(acc, partials, ticket, tot)) slots[S_RESID2] = tot[0];
 }
 
-// Writes the itstat record of the previous iteration (if there is one).
-__global__ void k_itstat(double* __restrict__ itstat, double* __restrict__ slots, int max_records,
-                         double scale, double lam21, double lam1, int final_call) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (slots[S_HAVE_PREV] != 0.0) {
-    const int rec = (int)slots[S_REC];
-    if (itstat && rec < max_records) {
-      double* o = itstat + (size_t)rec * CT_ITSTAT_FIELDS;
-      const double* cg = slots + S_CG;
-      o[CT_ITSTAT_OBJECTIVE] = scale * slots[S_RESID2] + lam21 * slots[S_G21] + lam1 * slots[S_G1];
-      o[CT_ITSTAT_PRIMAL] = sqrt(slots[S_PRIMAL2]);
-      o[CT_ITSTAT_DUAL] = sqrt(slots[S_DUAL2]);
-      o[CT_ITSTAT_CG_ITERS] = cg[CT_CG_ITERS];
-      o[CT_ITSTAT_CG_RELRES] = sqrt(cg[CT_CG_NUM]) / cg[CT_CG_BNORM];
-      o[5] = 0.0;
-      o[6] = 0.0;
-      o[7] = 0.0;
-    }
-    slots[S_REC] = (double)(rec + 1);
+// Where and how the itstat records are written.
+struct RecParams {
+  double* itstat;
+  int max_records;
+  double scale, lam21, lam1;
+};
+
+// Writes the itstat record of the previous iteration (if there is one), from
+// the slots and the CG scalars as that iteration left them (one thread).
+__device__ __forceinline__ void write_record(const RecParams& rp, double* __restrict__ slots) {
+  if (slots[S_HAVE_PREV] == 0.0) return;
+  const int rec = (int)slots[S_REC];
+  if (rp.itstat && rec < rp.max_records) {
+    double* o = rp.itstat + (size_t)rec * CT_ITSTAT_FIELDS;
+    const double* cg = slots + S_CG;
+    o[CT_ITSTAT_OBJECTIVE] = rp.scale * slots[S_RESID2] + rp.lam21 * slots[S_G21] + rp.lam1 * slots[S_G1];
+    o[CT_ITSTAT_PRIMAL] = sqrt(slots[S_PRIMAL2]);
+    o[CT_ITSTAT_DUAL] = sqrt(slots[S_DUAL2]);
+    o[CT_ITSTAT_CG_ITERS] = cg[CT_CG_ITERS];
+    o[CT_ITSTAT_CG_RELRES] = sqrt(cg[CT_CG_NUM]) / cg[CT_CG_BNORM];
+    o[5] = 0.0;
+    o[6] = 0.0;
+    o[7] = 0.0;
   }
-  slots[S_HAVE_PREV] = final_call ? 0.0 : slots[S_HAVE_PREV];
+  slots[S_REC] = (double)(rec + 1);
+}
+
+// The last record of a call (the statistics epilogue).
+__global__ void k_itstat_final(RecParams rp, double* __restrict__ slots) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  write_record(rp, slots);
+  slots[S_HAVE_PREV] = 0.0;
 }
 
 // lhs(q) = sum_i rho D^T D q + c A^T A q, from the adjoint output (or its
 // view splits).  INIT (q = x): r = rhs - lhs(x), p = r and the CG start
 // scalars; lhs(x) is stored in lhsx, or read from it while x is unchanged
-// (slots[S_XCLEAN]).  PAP: Ap = lhs(q) and <q, Ap>.  In a graph with a
-// conditional CG loop, INIT sets the loop condition.
+// (slots[S_XCLEAN]); before the CG scalars are reset the last block writes
+// the previous iteration's itstat record.  PAP: Ap = lhs(q) and <q, Ap>.  In
+// a graph with a conditional CG loop, INIT sets the loop condition.
 template <int ND, bool INIT>
 __global__ void __launch_bounds__(NT)
     k_lhs_finish(const float* __restrict__ adj, int nsplit, const float* __restrict__ q, Shape3 sh,
@@ -478,7 +499,7 @@ __global__ void __launch_bounds__(NT)
                  float* __restrict__ p, float* __restrict__ lhsx, double* __restrict__ slots,
                  double* __restrict__ cg, double tol, double atol, int maxiter,
                  double* __restrict__ partials, unsigned int* __restrict__ ticket,
-                 cudaGraphConditionalHandle cond, int use_cond, int vec) {
+                 cudaGraphConditionalHandle cond, int use_cond, int vec, RecParams rp) {
   if (!INIT && cg[CT_CG_DONE] != 0.0) return;
   const bool cached = INIT && slots[S_XCLEAN] != 0.0;
   double acc[2] = {0.0, 0.0};
@@ -558,6 +579,7 @@ __global__ void __launch_bounds__(NT)
   double tot[2];
   if (ct::grid_sumk_last<NT, 2>(acc, partials, ticket, tot)) {
     if (INIT) {
+      write_record(rp, slots);
       const double bn = sqrt(tot[1]);
       const double thr = fmax(tol * bn, atol);
       cg[CT_CG_NUM] = tot[0];
@@ -706,11 +728,15 @@ __device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* __restri
   }
 }
 
+// In the solve graph (use_loop != 0) the last block also ends the iteration:
+// it counts it and keeps the graph's iteration loop (a conditional WHILE
+// node) running while fewer than maxiter iterations have run.
 template <int ND>
 __global__ void __launch_bounds__(NT)
     k_zu(const float* __restrict__ x, float* __restrict__ z, float* __restrict__ u, float* __restrict__ dz,
          Shape3 sh, size_t N, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
-         unsigned int* __restrict__ ticket, int vec) {
+         unsigned int* __restrict__ ticket, int vec, cudaGraphConditionalHandle loop, int use_loop,
+         int maxiter) {
   double acc[3] = {0.0, 0.0, 0.0};  // primal, g21, g1
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
@@ -737,6 +763,11 @@ __global__ void __launch_bounds__(NT)
     slots[S_G1] = tot[2];
     slots[S_HAVE_PREV] = 1.0;
     if (slots[S_CG + CT_CG_ITERS] > 0.0) slots[S_XCLEAN] = 0.0;  // CG moved x
+    if (use_loop) {
+      const double it = slots[S_ITER] + 1.0;
+      slots[S_ITER] = it;
+      cudaGraphSetConditional(loop, it < (double)maxiter ? 1u : 0u);
+    }
   }
 }
 
@@ -747,14 +778,6 @@ __global__ void k_reset_call(double* __restrict__ slots) {
   slots[S_ITER] = 0.0;
 }
 
-// End of one ADMM iteration in the solve graph: count it and keep the
-// graph's iteration loop (a conditional WHILE node) running while fewer than
-// maxiter iterations have run.
-__global__ void k_admm_next(double* __restrict__ slots, int maxiter, cudaGraphConditionalHandle h) {
-  const double it = slots[S_ITER] + 1.0;
-  slots[S_ITER] = it;
-  cudaGraphSetConditional(h, it < (double)maxiter ? 1u : 0u);
-}
 
 // ---------------------------------------------------------------------------
 
@@ -943,39 +966,54 @@ const float* backproject(const Ctx& c, const float* sino, cudaStream_t s, const 
   return c.P.proj.nsplit() > 1 ? part : adj;
 }
 
-// The three phases of one ADMM iteration.  cond/use_cond: the conditional
-// handle of the graph's CG loop (use_cond = 0 outside such a graph).
-ct_status enqueue_pre(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
-  const int nd = c.P.nd;
-  const size_t N = c.P.N;
-  float* r = c.at<float>(c.L.off_r);
-  float* p = c.at<float>(c.L.off_p);
-  float* rhs = c.at<float>(c.L.off_rhs);
+RecParams rec_params(const Ctx& c) {
+  return RecParams{c.itstat, c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21, c.P.prm.lam_l1};
+}
+
+// The phases of one ADMM iteration:
+//   rhs   k_rhs (with dirty/use_dirty: sets the condition of the graph's
+//         projection node)
+//   proj  A x, ||A x - y||^2 and A^T (A x) -- each a no-op while x is
+//         unchanged (in the solve graph the phase is a conditional IF node
+//         that runs only when x changed)
+//   init  k_lhs_finish<INIT>: the previous iteration's record, CG start;
+//         cond/use_cond: the conditional handle of the graph's CG loop
+//   CG    enqueue_cg_step per step
+//   post  k_zu (with loop/use_loop: ends the graph's iteration)
+ct_status enqueue_rhs(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle dirty, int use_dirty) {
+  CT_LAUNCH_ND(c.P.nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
+               c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N, c.tp,
+               c.slots(), c.partials(), c.ticket(), c.vi, dirty, use_dirty);
+  return ct::launch_check("k_rhs");
+}
+
+ct_status enqueue_proj(const Ctx& c, cudaStream_t s) {
   float* sinox = c.at<float>(c.L.off_sinox);
   const double* clean = c.slots() + S_XCLEAN;
-  CT_LAUNCH_ND(nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
-               c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), rhs, c.P.sh, N, c.tp, c.slots(),
-               c.partials(), c.ticket(), c.vi);
-  CT_TRY(ct::launch_check("k_rhs"));
   CT_TRY(project(c, c.x, sinox, s, clean));
   k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket(), c.vs);
   CT_TRY(ct::launch_check("k_resid2"));
-  k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21,
-                            c.P.prm.lam_l1, 0);
-  CT_TRY(ct::launch_check("k_itstat"));
   ct_status st;
-  const float* adj = backproject(c, sinox, s, clean, st);
-  CT_TRY(st);
-  if (nd == 2)
+  backproject(c, sinox, s, clean, st);
+  return st;
+}
+
+ct_status enqueue_init(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
+  const size_t N = c.P.N;
+  const float* adj = c.P.proj.nsplit() > 1 ? c.at<float>(c.L.off_adjpart) : c.at<float>(c.L.off_adj);
+  float* r = c.at<float>(c.L.off_r);
+  float* p = c.at<float>(c.L.off_p);
+  float* rhs = c.at<float>(c.L.off_rhs);
+  if (c.P.nd == 2)
     k_lhs_finish<2, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
                                             c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
                                             c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
-                                            cond, use_cond, c.vi);
+                                            cond, use_cond, c.vi, rec_params(c));
   else
     k_lhs_finish<3, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
                                             c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
                                             c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
-                                            cond, use_cond, c.vi);
+                                            cond, use_cond, c.vi, rec_params(c));
   return ct::launch_check("k_lhs_finish<init>");
 }
 
@@ -993,43 +1031,44 @@ ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHand
   if (c.P.nd == 2)
     k_lhs_finish<2, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
                                              nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
-                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi);
+                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi,
+                                             RecParams{});
   else
     k_lhs_finish<3, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
                                              nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
-                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi);
+                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi,
+                                             RecParams{});
   CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
   CT_TRY(ct::cg_update_launch(c.x, r, p, ap, N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond));
   return ct::cg_direction_launch(p, r, N, c.cg(), c.ws + c.L.off_red, s);
 }
 
-ct_status enqueue_post(const Ctx& c, cudaStream_t s) {
+ct_status enqueue_post(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle loop, int use_loop) {
   CT_LAUNCH_ND(c.P.nd, k_zu, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-               c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp, c.slots(), c.partials(), c.ticket(), c.vi);
+               c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp, c.slots(), c.partials(), c.ticket(), c.vi, loop,
+               use_loop, c.P.prm.maxiter);
   return ct::launch_check("k_zu");
 }
 
 // One iteration as plain launches (no graph): cg_maxiter CG steps that turn
 // into no-ops once CG has converged.
 ct_status enqueue_iteration(const Ctx& c, cudaStream_t s) {
-  CT_TRY(enqueue_pre(c, s, 0, 0));
+  CT_TRY(enqueue_rhs(c, s, 0, 0));
+  CT_TRY(enqueue_proj(c, s));
+  CT_TRY(enqueue_init(c, s, 0, 0));
   for (int it = 0; it < c.P.prm.cg_maxiter; ++it) CT_TRY(enqueue_cg_step(c, s, 0, 0));
-  return enqueue_post(c, s);
+  return enqueue_post(c, s, 0, 0);
 }
 
 // Statistics of the last iteration: dual residual (k_rhs), objective.
 ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
   float* sinox = c.at<float>(c.L.off_sinox);
-  CT_LAUNCH_ND(c.P.nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
-               c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N,
-               c.tp, c.slots(), c.partials(), c.ticket(), c.vi);
-  CT_TRY(ct::launch_check("k_rhs"));
+  CT_TRY(enqueue_rhs(c, s, 0, 0));
   CT_TRY(project(c, c.x, sinox, s, c.slots() + S_XCLEAN));
   k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket(), c.vs);
   CT_TRY(ct::launch_check("k_resid2"));
-  k_itstat<<<1, 32, 0, s>>>(c.itstat, c.slots(), c.P.prm.maxiter, c.P.prm.loss_scale, c.P.prm.lam_l21,
-                            c.P.prm.lam_l1, 1);
-  return ct::launch_check("k_itstat");
+  k_itstat_final<<<1, 32, 0, s>>>(rec_params(c), c.slots());
+  return ct::launch_check("k_itstat_final");
 }
 
 // Executable iteration graphs, one per problem (key: dimension, descriptor
@@ -1097,12 +1136,31 @@ ct_status capture_into(cudaStream_t cs, cudaGraph_t graph, const std::vector<cud
   return CT_OK;
 }
 
+// Conditional node of type `type` on `handle` after `deps` in `graph`; its
+// body graph is returned in `body`.
+ct_status add_conditional(cudaGraph_t graph, const std::vector<cudaGraphNode_t>& deps,
+                          cudaGraphConditionalHandle handle, cudaGraphConditionalNodeType type,
+                          cudaGraphNode_t& node, cudaGraph_t& body) {
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = handle;
+  np.conditional.type = type;
+  np.conditional.size = 1;
+  CT_TRY(ct::cuda_check(cudaGraphAddNode(&node, graph, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                         &np),
+                        "conditional node"));
+  body = np.conditional.phGraph_out[0];
+  return CT_OK;
+}
+
 // Append one whole solve to `graph`, independent of every other node:
 // the state set-up (iter0 == 0) and k_reset_call, then the ADMM loop as a
-// conditional WHILE node whose body is one iteration -- the pre-phase
-// kernels, the CG loop as a nested WHILE node (its start and every CG
-// update set its condition on the device: run while CG has not converged),
-// the z/u update and k_admm_next -- then the statistics epilogue.
+// conditional WHILE node whose body is one iteration -- k_rhs, the
+// projections of x as a conditional IF node (run when CG moved x), the CG
+// start, the CG loop as a nested WHILE node (its start and every CG update
+// set its condition on the device: run while CG has not converged), and the
+// z/u update, whose last block counts the iteration and sets the loop's
+// condition -- then the statistics epilogue.
 ct_status append_solve(const Ctx& c, int32_t iter0, cudaStream_t cs, cudaGraph_t graph) {
   const Params& prm = c.P.prm;
   std::vector<cudaGraphNode_t> tail;
@@ -1122,42 +1180,29 @@ ct_status append_solve(const Ctx& c, int32_t iter0, cudaStream_t cs, cudaGraph_t
     k_reset_call<<<1, 1, 0, s>>>(c.slots());
     return ct::launch_check("k_reset_call");
   }));
-  if (prm.maxiter > 0) {
-    cudaGraphConditionalHandle loop = 0;
-    CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&loop, graph, 1, cudaGraphCondAssignDefault),
-                          "loop handle"));
-    cudaGraphNodeParams lp = {};
-    lp.type = cudaGraphNodeTypeConditional;
-    lp.conditional.handle = loop;
-    lp.conditional.type = cudaGraphCondTypeWhile;
-    lp.conditional.size = 1;
-    cudaGraphNode_t lnode = nullptr;
-    CT_TRY(ct::cuda_check(cudaGraphAddNode(&lnode, graph, tail.data(), nullptr, tail.size(), &lp), "loop node"));
-    cudaGraph_t body = lp.conditional.phGraph_out[0];
-    cudaGraphConditionalHandle cg = 0;
-    CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&cg, body, 0, cudaGraphCondAssignDefault),
-                          "CG handle"));
-    std::vector<cudaGraphNode_t> pre;
-    CT_TRY(capture_into(cs, body, {}, pre, [&](cudaStream_t s) { return enqueue_pre(c, s, cg, 1); }));
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = cg;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t cnode = nullptr;
-    CT_TRY(ct::cuda_check(cudaGraphAddNode(&cnode, body, pre.data(), nullptr, pre.size(), &cp), "CG node"));
-    std::vector<cudaGraphNode_t> unused;
-    CT_TRY(capture_into(cs, cp.conditional.phGraph_out[0], {}, unused,
-                        [&](cudaStream_t s) { return enqueue_cg_step(c, s, cg, 1); }));
-    CT_TRY(capture_into(cs, body, {cnode}, unused, [&](cudaStream_t s) -> ct_status {
-      CT_TRY(enqueue_post(c, s));
-      k_admm_next<<<1, 1, 0, s>>>(c.slots(), prm.maxiter, loop);
-      return ct::launch_check("k_admm_next");
-    }));
-    tail.assign(1, lnode);
-  } else {
-    return CT_OK;  // no iteration: no statistics either
-  }
+  if (prm.maxiter <= 0) return CT_OK;  // no iteration: no statistics either
+  cudaGraphConditionalHandle loop = 0;
+  CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&loop, graph, 1, cudaGraphCondAssignDefault),
+                        "loop handle"));
+  cudaGraphNode_t lnode = nullptr;
+  cudaGraph_t body = nullptr;
+  CT_TRY(add_conditional(graph, tail, loop, cudaGraphCondTypeWhile, lnode, body));
+  cudaGraphConditionalHandle dirty = 0, cg = 0;
+  CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&dirty, body, 0, cudaGraphCondAssignDefault),
+                        "projection handle"));
+  CT_TRY(ct::cuda_check(cudaGraphConditionalHandleCreate(&cg, body, 0, cudaGraphCondAssignDefault),
+                        "CG handle"));
+  std::vector<cudaGraphNode_t> nodes, unused;
+  CT_TRY(capture_into(cs, body, {}, nodes, [&](cudaStream_t s) { return enqueue_rhs(c, s, dirty, 1); }));
+  cudaGraphNode_t pnode = nullptr, cnode = nullptr;
+  cudaGraph_t pbody = nullptr, cbody = nullptr;
+  CT_TRY(add_conditional(body, nodes, dirty, cudaGraphCondTypeIf, pnode, pbody));
+  CT_TRY(capture_into(cs, pbody, {}, unused, [&](cudaStream_t s) { return enqueue_proj(c, s); }));
+  CT_TRY(capture_into(cs, body, {pnode}, nodes, [&](cudaStream_t s) { return enqueue_init(c, s, cg, 1); }));
+  CT_TRY(add_conditional(body, nodes, cg, cudaGraphCondTypeWhile, cnode, cbody));
+  CT_TRY(capture_into(cs, cbody, {}, unused, [&](cudaStream_t s) { return enqueue_cg_step(c, s, cg, 1); }));
+  CT_TRY(capture_into(cs, body, {cnode}, unused, [&](cudaStream_t s) { return enqueue_post(c, s, loop, 1); }));
+  tail.assign(1, lnode);
   std::vector<cudaGraphNode_t> end;
   return capture_into(cs, graph, tail, end, [&](cudaStream_t s) { return enqueue_epilogue(c, s); });
 }

@@ -139,7 +139,12 @@ __global__ void __launch_bounds__(NT)
     if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
     return;
   }
-  const double alpha = s[CT_CG_NUM] / s[CT_CG_PAP];
+  // one float64 division per block (float64 runs at a small fraction of
+  // the float32 rate on this GPU), shared through shared memory
+  __shared__ double alpha_s;
+  if (threadIdx.x == 0) alpha_s = s[CT_CG_NUM] / s[CT_CG_PAP];
+  __syncthreads();
+  const double alpha = alpha_s;
   const float af = (float)alpha;
   double rr = 0.0;
   if (vec) {
