@@ -495,28 +495,25 @@ __global__ void __launch_bounds__(kFW * 32, 3)
   }
   __syncthreads();
   // ---- combine the 8 tiles in tile order into the strip's bins, every view
-  // of the run: warp w takes views w, w + 8; bin k of the strip gets the
-  // tiles whose span covers it ------------------------------------------------
+  // of the run: warp w takes views w, w + 8 and adds the tiles' bins one
+  // tile after the other into a row of the (now dead) partial-row region
+  // (32 LS >= cspan floats per warp), lane = bin; bin k of the strip is
+  // 0 + the covering tiles in tile order ------------------------------------
+  float* acc = part + warp * kT * LS;
   for (int vi = warp; vi < vend - vbeg; vi += kFW) {
-    int toff[kFW], tspan[kFW];
-#pragma unroll
-    for (int w = 0; w < kFW; ++w) {
-      const int4 tp = vs->tile[vi][w];
-      toff[w] = tp.z;
-      tspan[w] = tp.y;
-    }
     const float* tb = tbins + (size_t)vi * kFW * a.L;
     float* po = a.part + (((size_t)b * gridDim.x + s) * a.nv + vbeg + vi) * a.cspan;
     const int n = min(vs->strip[vi].y, a.cspan);
-    for (int k = lane; k < n; k += 32) {
-      float acc = 0.0f;
-#pragma unroll
-      for (int w = 0; w < kFW; ++w) {
-        const int o = k - toff[w];
-        if ((unsigned)o < (unsigned)tspan[w]) acc += tb[w * a.L + o];
-      }
-      po[k] = acc;
+    for (int k = lane; k < n; k += 32) acc[k] = 0.0f;
+    __syncwarp();
+#pragma unroll 1
+    for (int w = 0; w < kFW; ++w) {
+      const int4 tp = vs->tile[vi][w];  // base, span, offset in the strip, floor path
+      for (int k = lane; k < tp.y; k += 32) acc[tp.z + k] += tb[w * a.L + k];
+      __syncwarp();  // the next tile may add to the same bins
     }
+    for (int k = lane; k < n; k += 32) po[k] = acc[k];
+    __syncwarp();  // read before the next view zeroes the row
   }
 }
 
