@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(NT)
           int vec, cudaGraphConditionalHandle dirty, int use_dirty) {
   if (use_dirty && blockIdx.x == 0 && threadIdx.x == 0)
     cudaGraphSetConditional(dirty, slots[S_XCLEAN] == 0.0 ? 1u : 0u);
-  double acc[1] = {0.0};
+  ct::KSum ks;  // dual residual
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
       int c[ND];
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(NT)
       }
       st4(rhs, e0, val);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[0] += (double)dv[j] * (double)dv[j];
+      for (int j = 0; j < 4; ++j) ks.add(ct::fmul(dv[j], dv[j]));
     }
   } else {
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
@@ -404,9 +404,10 @@ __global__ void __launch_bounds__(NT)
       dv = (t == 0) ? w : ct::fadd(dv, w);
     }
     rhs[e] = val;
-    acc[0] += (double)dv * (double)dv;
+    ks.add(ct::fmul(dv, dv));
   }
   }
+  double acc[1] = {ks.value()};
   double tot[1];
   if (ct::grid_sumk_last<NT, 1>(acc, partials, ticket, tot)) slots[S_DUAL2] = tot[0];
 }
@@ -416,7 +417,7 @@ __global__ void __launch_bounds__(NT)
              double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
              int vec) {
   if (slots[S_XCLEAN] != 0.0) return;  // x unchanged: S_RESID2 is current
-  double acc[1] = {0.0};
+  ct::KSum ks;
   if (vec) {
     // two quads per step for more loads in flight
     const size_t stride = 4 * (size_t)gridDim.x * NT;
@@ -432,22 +433,23 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const float d = ct::fsub(a[j], b[j]);
-        acc[0] += (double)d * (double)d;
+        ks.add(ct::fmul(d, d));
       }
       if (two) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const float d = ct::fsub(a2[j], b2[j]);
-          acc[0] += (double)d * (double)d;
+          ks.add(ct::fmul(d, d));
         }
       }
     }
   } else {
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
       const float d = ct::fsub(y[e], sino[e]);
-      acc[0] += (double)d * (double)d;
+      ks.add(ct::fmul(d, d));
     }
   }
+  double acc[1] = {ks.value()};
   double tot[1];
   if (ct::grid_sumk_last<NT, 1>(acc, partials, ticket, tot)) slots[S_RESID2] = tot[0];
 }
@@ -630,7 +632,7 @@ __device__ __forceinline__ void prox_nd(int kind, float thr, const float (&v)[ND
 template <int ND>
 __device__ __forceinline__ void zu_el(const float (&d)[ND], float* __restrict__ z, float* __restrict__ u,
                                       float* __restrict__ dz, size_t e, size_t N, const TermParams& tp,
-                                      double (&acc)[3]) {
+                                      ct::KSum (&acc)[3]) {
   for (int t = 0; t < tp.ng; ++t) {
     const size_t o = (size_t)t * ND * N;
     float zo[ND], v[ND], zn[ND];
@@ -645,26 +647,26 @@ __device__ __forceinline__ void zu_el(const float (&d)[ND], float* __restrict__ 
       v[k] = ct::fadd(ck, u[o + k * N + e]);
     }
     prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
-    double pr = 0.0;
+    float pr = 0.0f;
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
       z[o + k * N + e] = zn[k];
       u[o + k * N + e] = ct::fsub(v[k], zn[k]);
       dz[o + k * N + e] = ct::fsub(zn[k], zo[k]);
-      const double pk = (double)d[k] - (double)zn[k];
-      pr = k == 0 ? pk * pk : pr + pk * pk;
+      const float pk = ct::fsub(d[k], zn[k]);
+      pr = k == 0 ? ct::fmul(pk, pk) : ct::fadd(pr, ct::fmul(pk, pk));
     }
-    acc[0] += (double)tp.rho * pr;
+    acc[0].add(ct::fmul(tp.rho, pr));
     if (tp.kind[t] == 0) {
       float s2 = ct::fmul(zn[0], zn[0]);
 #pragma unroll
       for (int k = 1; k < ND; ++k) s2 = ct::fadd(s2, ct::fmul(zn[k], zn[k]));
-      acc[1] += (double)__fsqrt_rn(s2);
+      acc[1].add(__fsqrt_rn(s2));
     } else {
-      double a1 = fabs((double)zn[0]);
+      float a1 = fabsf(zn[0]);
 #pragma unroll
-      for (int k = 1; k < ND; ++k) a1 += fabs((double)zn[k]);
-      acc[2] += a1;
+      for (int k = 1; k < ND; ++k) a1 = ct::fadd(a1, fabsf(zn[k]));
+      acc[2].add(a1);
     }
   }
 }
@@ -674,7 +676,7 @@ __device__ __forceinline__ void zu_el(const float (&d)[ND], float* __restrict__ 
 template <int ND>
 __device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* __restrict__ z, float* __restrict__ u,
                                         float* __restrict__ dz, size_t e0, size_t N, const TermParams& tp,
-                                        double (&acc)[3]) {
+                                        ct::KSum (&acc)[3]) {
   for (int t = 0; t < tp.ng; ++t) {
     const size_t o = (size_t)t * ND * N;
     float zo[ND][4], uo[ND][4];
@@ -697,26 +699,26 @@ __device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* __restri
         v[k] = ct::fadd(ck, uo[k][j]);
       }
       prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
-      double pr = 0.0;
+      float pr = 0.0f;
 #pragma unroll
       for (int k = 0; k < ND; ++k) {
         zn4[k][j] = zn[k];
         un4[k][j] = ct::fsub(v[k], zn[k]);
         dz4[k][j] = ct::fsub(zn[k], zo[k][j]);
-        const double pk = (double)d[k][j] - (double)zn[k];
-        pr = k == 0 ? pk * pk : pr + pk * pk;
+        const float pk = ct::fsub(d[k][j], zn[k]);
+        pr = k == 0 ? ct::fmul(pk, pk) : ct::fadd(pr, ct::fmul(pk, pk));
       }
-      acc[0] += (double)tp.rho * pr;
+      acc[0].add(ct::fmul(tp.rho, pr));
       if (tp.kind[t] == 0) {
         float s2 = ct::fmul(zn[0], zn[0]);
 #pragma unroll
         for (int k = 1; k < ND; ++k) s2 = ct::fadd(s2, ct::fmul(zn[k], zn[k]));
-        acc[1] += (double)__fsqrt_rn(s2);
+        acc[1].add(__fsqrt_rn(s2));
       } else {
-        double a1 = fabs((double)zn[0]);
+        float a1 = fabsf(zn[0]);
 #pragma unroll
-        for (int k = 1; k < ND; ++k) a1 += fabs((double)zn[k]);
-        acc[2] += a1;
+        for (int k = 1; k < ND; ++k) a1 = ct::fadd(a1, fabsf(zn[k]));
+        acc[2].add(a1);
       }
     }
 #pragma unroll
@@ -737,7 +739,7 @@ __global__ void __launch_bounds__(NT)
          Shape3 sh, size_t N, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
          unsigned int* __restrict__ ticket, int vec, cudaGraphConditionalHandle loop, int use_loop,
          int maxiter) {
-  double acc[3] = {0.0, 0.0, 0.0};  // primal, g21, g1
+  ct::KSum ks[3];  // primal, g21, g1
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
       int c[ND];
@@ -745,7 +747,7 @@ __global__ void __launch_bounds__(NT)
       float xc[4], d[ND][4];
       unpack4(ld4(x, e0), xc);
       d_at4<ND>(x, xc, c, e0, sh, d);
-      zu_quad<ND>(d, z, u, dz, e0, N, tp, acc);
+      zu_quad<ND>(d, z, u, dz, e0, N, tp, ks);
     }
   } else {
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
@@ -753,9 +755,10 @@ __global__ void __launch_bounds__(NT)
       coords<ND>(e, sh, c);
       float d[ND];
       d_at<ND>(x, c, e, sh, d);
-      zu_el<ND>(d, z, u, dz, e, N, tp, acc);
+      zu_el<ND>(d, z, u, dz, e, N, tp, ks);
     }
   }
+  double acc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
   double tot[3];
   if (ct::grid_sumk_last<NT, 3>(acc, partials, ticket, tot)) {
     slots[S_PRIMAL2] = tot[0];

@@ -61,6 +61,24 @@ __device__ __forceinline__ void boxcar2d(float px, float width, float inv_width,
   w = dist < width ? fmul(dist, inv_width) : 1.0f;
 }
 
+// Compensated (Kahan) float32 running sum: a thread's partial sum of
+// statistics terms (residual norms, objective terms), combined over the grid
+// in float64.  The compensation keeps a partial sum of hundreds of float32
+// terms within a few units of rounding, as a float64 accumulation would,
+// without float64 arithmetic per element (the float64 pipe of this GPU runs
+// at a small fraction of the float32 rate).  The CG dot products, which
+// steer the iteration, stay float64 per element.
+struct KSum {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = __fsub_rn(v, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 // ---------------------------------------------------------------------------
 // Deterministic float64 grid reduction of K simultaneous sums.  Every block
 // reduces its threads' values (fixed shuffle tree, warps in order) and

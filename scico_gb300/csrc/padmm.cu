@@ -98,23 +98,6 @@ __device__ __forceinline__ void coords32(uint32_t e, const Shape3& sh, int (&c)[
   }
 }
 
-// Compensated (Kahan) float32 running sum: each thread's partial sums of the
-// residual norms and objective terms, combined over the grid in float64.
-// Per element the terms are float32 products; the compensation keeps a
-// partial sum of a few hundred terms within a few units of rounding, as a
-// float64 accumulation would, without float64 arithmetic per element (the
-// float64 pipe of this GPU runs at a small fraction of the float32 rate).
-struct KSum {
-  float s = 0.0f, c = 0.0f;
-  __device__ __forceinline__ void add(float v) {
-    const float y = ct::fsub(v, c);
-    const float t = ct::fadd(s, y);
-    c = ct::fsub(ct::fsub(t, s), y);
-    s = t;
-  }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
 // x <- x - (1/mu) (A^T t)(e):  A^T t = C^T t0 + alpha D^T t1, the adjoint's
 // view splits summed in order, D^T with the append=0 boundaries, axes in
 // order (linop/_stack.py:71-72, _diff.py).
@@ -192,7 +175,7 @@ __global__ void __launch_bounds__(NT)
 // Sinogram block, one element: a = (C x)[e];  pz = z0 + (1/nu)((a - z0) + u0);
 // z0' = (c y + pz) / (c + 1);  u0' = (u0 + a) - z0';  t0 = 2 u0' - u0.
 __device__ __forceinline__ void zu0_elem(float a, float z, float u, float ye, const Scal& s, float& zn, float& un,
-                                         float& tn, KSum& prim, KSum& dual, KSum& g0) {
+                                         float& tn, ct::KSum& prim, ct::KSum& dual, ct::KSum& g0) {
   const float pz = ct::fadd(z, ct::fmul(s.inv_nu, ct::fadd(ct::fsub(a, z), u)));
   zn = __fdiv_rn(ct::fadd(ct::fmul(s.c, ye), pz), s.c1);
   un = ct::fsub(ct::fadd(u, a), zn);
@@ -207,7 +190,7 @@ __global__ void __launch_bounds__(NT)
     k_pd_zu0(const float* __restrict__ ax, const float* __restrict__ y, float* __restrict__ z0,
              float* __restrict__ u0, float* __restrict__ t0, size_t S, Scal s, double* __restrict__ slots,
              double* __restrict__ partials, unsigned int* __restrict__ ticket, int vec) {
-  KSum prim, dual, g0;
+  ct::KSum prim, dual, g0;
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < S; e0 += 4 * (size_t)gridDim.x * NT) {
       float a[4], z[4], u[4], ye[4], zn[4], un[4], tn[4];
@@ -245,7 +228,7 @@ __global__ void __launch_bounds__(NT)
 template <int ND>
 __device__ __forceinline__ void zu1_elem(const float (&ax)[ND], const float (&z)[ND], const float (&u)[ND],
                                          const Scal& s, float (&zn)[ND], float (&un)[ND], float (&tn)[ND],
-                                         KSum& prim, KSum& dual, KSum& g1) {
+                                         ct::KSum& prim, ct::KSum& dual, ct::KSum& g1) {
   float pz[ND];
   float ss = 0.0f;
 #pragma unroll
@@ -277,7 +260,7 @@ __global__ void __launch_bounds__(NT)
     k_pd_zu1(const float* __restrict__ x, float* __restrict__ z1, float* __restrict__ u1, float* __restrict__ t1,
              Shape3 sh, size_t N, Scal s, double* __restrict__ itstat, int maxiter, double* __restrict__ slots,
              double* __restrict__ partials, unsigned int* __restrict__ ticket, int vec) {
-  KSum prim, dual, g1;
+  ct::KSum prim, dual, g1;
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
       int c[ND];
