@@ -24,6 +24,7 @@ from __future__ import annotations
 import collections
 import math
 import time
+import weakref
 from typing import Any, Callable, List, Optional
 
 import numpy as np
@@ -58,7 +59,10 @@ class LinearSubproblemSolver:
             raise TypeError(f"LinearSubproblemSolver requires f to be a SquaredL2Loss; got {type(admm.f)}.")
         if not isinstance(admm.f.A, linop.LinearOperator):
             raise TypeError(f"LinearSubproblemSolver requires f.A to be a LinearOperator; got {type(admm.f.A)}.")
-        self.admm = admm
+        # a weak reference: the solver owns its subproblem solver, and a cycle
+        # would keep a finished solver's device buffers alive until the
+        # garbage collector runs
+        self.admm = weakref.proxy(admm)
         lhs = None
         for rho, C in zip(admm.rho_list, admm.C_list):  # :222-224
             t = rho * C.gram_op
@@ -118,11 +122,12 @@ class ADMM:
         self.subproblem_solver = subproblem_solver
         self.subproblem_solver.internal_init(self)
         if x0 is None:
-            x0 = _device.zeros(C_list[0].input_shape)
-        self.x = _device.to_device(x0, shape=C_list[0].input_shape, name="x0").clone()
-        self.z_list = [C(self.x) for C in C_list]  # z_init (:297-315)
-        self.z_list_old = list(self.z_list)
-        self.u_list = [_zeros_like(z) for z in self.z_list]  # u_init (:317-332)
+            self.x = _device.zeros(C_list[0].input_shape)
+        else:
+            self.x = _device.to_device(x0, shape=C_list[0].input_shape, name="x0").clone()
+        # z_list = z_init (:297-315), z_list_old, u_list = u_init (:317-332):
+        # made on first use (the fused solver initialises its own state)
+        self._zu = {}
         # Optimizer.__init__ (_common.py:117-135)
         self.itnum = kwargs.pop("iter0", 0)
         self.maxiter = kwargs.pop("maxiter", 100)
@@ -133,11 +138,45 @@ class ADMM:
             raise TypeError(f"Unrecognized keyword argument(s) {', '.join(kwargs)}")
         self.itstat_display = bool(itstat_options.get("display", False))
         self.itstat_period = int(itstat_options.get("period", 1))
-        self.iterations: List[IterationRecord] = []
+        self._iters: List[IterationRecord] = []
+        self._pending_records = []  # fused solves' itstat arrays, turned into records on first use
         self._fused_state = None
         self._elapsed = 0.0
 
-    # -- reference quantities (_admm.py:210-295) ------------------------------
+    @property
+    def iterations(self) -> List[IterationRecord]:
+        for rec, it0, el0, dt in self._pending_records:
+            m = len(rec)
+            for k in range(m):
+                r = rec[k]
+                self._iters.append(IterationRecord(it0 + k, el0 + dt * (k + 1) / m, float(r[_lib.CT_ITSTAT_OBJECTIVE]),
+                                                   float(r[_lib.CT_ITSTAT_PRIMAL]), float(r[_lib.CT_ITSTAT_DUAL]),
+                                                   int(r[_lib.CT_ITSTAT_CG_ITERS]),
+                                                   float(r[_lib.CT_ITSTAT_CG_RELRES])))
+        self._pending_records = []
+        return self._iters
+
+    @iterations.setter
+    def iterations(self, v: List[IterationRecord]):
+        self._pending_records = []
+        self._iters = list(v)
+
+    # -- z and u state (made on first use) --------------------------------------
+    def _zu_get(self, key):
+        zu = self._zu
+        if "z_list" not in zu:
+            zu["z_list"] = [C(self.x) for C in self.C_list]  # before any step: x = x0
+        if key == "u_list" and key not in zu:
+            zu[key] = [_zeros_like(z) for z in zu["z_list"]]
+        if key == "z_list_old" and key not in zu:
+            zu[key] = list(zu["z_list"])
+        return zu[key]
+
+    z_list = property(lambda self: self._zu_get("z_list"), lambda self, v: self._zu.__setitem__("z_list", v))
+    z_list_old = property(lambda self: self._zu_get("z_list_old"),
+                          lambda self, v: self._zu.__setitem__("z_list_old", v))
+    u_list = property(lambda self: self._zu_get("u_list"), lambda self, v: self._zu.__setitem__("u_list", v))
+
     def objective(self, x=None, z_list=None) -> float:
         if (x is None) != (z_list is None):
             raise ValueError("Both or neither of arguments 'x' and 'z_list' must be supplied.")
@@ -187,7 +226,7 @@ class ADMM:
         return True
 
     def _record(self, rec: IterationRecord):
-        self.iterations.append(rec)
+        self.iterations.append(rec)  # (pending fused records first, in order)
         if self.itstat_display and (rec.Iter % self.itstat_period == 0):
             print("  ".join(f"{k}={v:.4g}" if isinstance(v, float) else f"{k}={v}" for k, v in rec._asdict().items()))
 
@@ -286,13 +325,16 @@ class ADMM:
         us = ws[st["uoff"]:st["uoff"] + st["nt"] * nd * N * 4].view(torch.float32).view(st["nt"], nd, *A.input_shape)
         self.z_list = [zs[k] for k in plan["order"]]
         self.u_list = [us[k] for k in plan["order"]]
-        rec = itstat.cpu().numpy()
-        for k in range(self.maxiter):
-            r = rec[k]
-            self._record(IterationRecord(self.itnum + k, self._elapsed + dt * (k + 1) / self.maxiter,
-                                         float(r[_lib.CT_ITSTAT_OBJECTIVE]), float(r[_lib.CT_ITSTAT_PRIMAL]),
-                                         float(r[_lib.CT_ITSTAT_DUAL]), int(r[_lib.CT_ITSTAT_CG_ITERS]),
-                                         float(r[_lib.CT_ITSTAT_CG_RELRES])))
+        rec = itstat.cpu().numpy()[: self.maxiter]
+        if self.itstat_display:
+            for k in range(self.maxiter):
+                r = rec[k]
+                self._record(IterationRecord(self.itnum + k, self._elapsed + dt * (k + 1) / self.maxiter,
+                                             float(r[_lib.CT_ITSTAT_OBJECTIVE]), float(r[_lib.CT_ITSTAT_PRIMAL]),
+                                             float(r[_lib.CT_ITSTAT_DUAL]), int(r[_lib.CT_ITSTAT_CG_ITERS]),
+                                             float(r[_lib.CT_ITSTAT_CG_RELRES])))
+        else:
+            self._pending_records.append((rec, self.itnum, self._elapsed, dt))
         self._elapsed += dt
         self.itnum += self.maxiter
         if self.nanstop and not self._working_vars_finite():
