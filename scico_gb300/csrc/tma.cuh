@@ -1,6 +1,6 @@
-// Bulk and tensor-map global->shared copies (cp.async.bulk{,.tensor}, the TMA
-// engine) completing on an mbarrier, with a bounded wait.  Inline PTX for
-// sm_90+ (sm_103a here).
+// Tensor-map global->shared copies (cp.async.bulk.tensor, the TMA engine)
+// completing on an mbarrier, with a bounded wait.  Inline PTX for sm_90+
+// (sm_103a here).
 #pragma once
 
 #include <stdint.h>
@@ -24,17 +24,6 @@ __device__ __forceinline__ void fence_barrier_init() {
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
-}
-
-// 1-D bulk copy of `bytes` (multiple of 16; both addresses 16-B aligned)
-// from global to shared memory, completing `bytes` transactions on `bar`.
-__device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst_smem)),
-      "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
 }
 
 // Tiled tensor-map load of one box at element coordinates (x, y, z) into

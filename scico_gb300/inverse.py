@@ -22,6 +22,7 @@
 
 from __future__ import annotations
 
+import math
 from typing import Callable, Optional, Tuple
 
 import torch
@@ -314,6 +315,58 @@ class ODPProxDnBlock(torch.nn.Module):
         return (self.resnet(x.unsqueeze(1)).squeeze(1) + y * a) / (1.0 + a)
 
 
+def _gram_norm(operator, maxiter: int = 100, seed: int = 0) -> float:
+    """||A||_2 = sqrt(largest eigenvalue of A^T A) by power iteration
+    (scico/linop/_util.py:27-76, 79-110) on the operator's batched
+    ``project`` / ``back_project``: normalized random start, per step
+    ``Av = A^T A v``, ``mu = <v, Av> / ||v||^2``, ``v = Av / ||Av||``; sums in
+    float64."""
+    gen = torch.Generator().manual_seed(seed)
+    v = torch.randn((1,) + tuple(operator.input_shape), generator=gen)
+    v = v / torch.linalg.vector_norm(v.double()).float()
+    mu = 0.0
+    with torch.no_grad():
+        for _ in range(maxiter):
+            Av = operator.back_project(operator.project(v))
+            v = v.to(Av.device)
+            nav = float(torch.linalg.vector_norm(Av.double()))
+            if nav == 0.0:  # a zero operator
+                return 0.0
+            mu = float((v.double() * Av.double()).sum()) / float((v.double() ** 2).sum())
+            v = Av / nav
+    return math.sqrt(max(mu, 0.0))
+
+
+class ODPProxDcnvBlock(torch.nn.Module):
+    """ODP proximal-gradient deconvolution block (scico/flax/inverse.py:
+    228-313) for an operator A with batched ``project`` / ``back_project``
+    (a circular convolution in the reference's use).  ||A|| is computed once
+    by power iteration on A^T A; the block returns, as the reference
+    computes it, the inverse real DFT over the two image axes of the real
+    DFT of ``alpha A^T y + ResNet(x)`` divided by
+    ``scale = 1 / (alpha ||A||^2 + 1)``, with a trainable scalar ``alpha``
+    (initial ``alpha_ini``)."""
+
+    def __init__(self, operator, depth: int, channels: int, num_filters: int,
+                 kernel_size: Tuple[int, int] = (3, 3), strides: Tuple[int, int] = (1, 1),
+                 alpha_ini: float = 0.99):
+        super().__init__()
+        self.operator = operator
+        self.operator_norm = _gram_norm(operator)
+        self.alpha = torch.nn.Parameter(torch.full((1,), float(alpha_ini)))
+        self.resnet = ResNet(depth, channels, num_filters, kernel_size, strides)
+
+    def batch_op_adj(self, y: torch.Tensor) -> torch.Tensor:
+        return back_project(self.operator, y)
+
+    def forward(self, x: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+        a = self.alpha.to(x.dtype)
+        scale = 1.0 / (a * self.operator_norm ** 2 + 1.0)
+        v = a * self.batch_op_adj(y) + self.resnet(x.unsqueeze(1)).squeeze(1)
+        f = torch.fft.rfftn(v, dim=(-2, -1)) / scale
+        return torch.fft.irfftn(f, s=v.shape[-2:], dim=(-2, -1))
+
+
 class ODPGrDescBlock(torch.nn.Module):
     r"""ODP gradient-descent block for an :math:`\ell_2` data term
     (scico/flax/inverse.py:295-375): ``x = ResNet(x) - alpha A^T (A x - y)``
@@ -342,7 +395,8 @@ class ODPNet(torch.nn.Module):
     ``x = A^T y``, then ``depth`` blocks, each with its own ResNet and
     ``alpha``; the first block's ``alpha`` starts at ``alpha_ini`` and each
     later one at half its predecessor's.  ``odp_block`` selects the block
-    (:class:`ODPProxDnBlock` by default, :class:`ODPGrDescBlock` for CT).
+    (:class:`ODPProxDnBlock` by default, :class:`ODPGrDescBlock` for CT,
+    :class:`ODPProxDcnvBlock` for deconvolution).
     Input ``(batch, *A.output_shape)``, output ``(batch, *A.input_shape)``;
     single-channel images."""
 

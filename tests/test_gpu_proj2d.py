@@ -102,6 +102,22 @@ def test_batch_and_determinism(cuda):
         assert torch.equal(bb[k], H.T(yb[k].contiguous()))
 
 
+@pytest.mark.parametrize("shape", [(64, 96), (70, 130), (37, 300)])
+def test_forward_staging_paths_identical(cuda, shape):
+    """The forward stages its strip tiles by tensor-map loads when the image
+    rows are 16-B strided and the image 16-B aligned, by plain loads into
+    the same layout otherwise: both give the same bits (an image 4 bytes
+    past an aligned address takes the plain path)."""
+    H, g = _op(dict(shape=shape, nv=23))
+    rng = np.random.default_rng(4)
+    x = torch.from_numpy(rng.random(shape).astype(np.float32)).to(cuda)
+    buf = torch.zeros(x.numel() + 4, device=cuda)
+    xs = buf[1:1 + x.numel()].view(shape)
+    xs.copy_(x)
+    assert xs.data_ptr() % 16 == 4
+    assert torch.equal(H(xs), H(x))
+
+
 def test_c1_full_size(cuda):
     """256x256, 180 views, 363 bins: parity against the float64 oracle."""
     from scico_gb300 import workloads

@@ -86,3 +86,54 @@ def test_odp_training_loop_cpu(tmp_path):
     tr2.train()
     for a, b in zip(net.state_dict().values(), net2.state_dict().values()):
         assert torch.equal(a, b)
+
+
+class _CircConvOp:
+    """Circular convolution with a small blur kernel through the real DFT,
+    with the projector interface (project / back_project on batched
+    tensors)."""
+
+    def __init__(self, n, seed=0):
+        g = torch.Generator().manual_seed(seed)
+        k = torch.zeros((n, n))
+        k[:3, :3] = torch.rand((3, 3), generator=g)
+        k /= k.sum()
+        self.kf = torch.fft.rfft2(k)
+        self.input_shape = self.output_shape = (n, n)
+
+    def project(self, v):
+        return torch.fft.irfft2(torch.fft.rfft2(v) * self.kf, s=self.input_shape)
+
+    def back_project(self, w):
+        return torch.fft.irfft2(torch.fft.rfft2(w) * self.kf.conj(), s=self.input_shape)
+
+
+def test_odp_deconvolution_block():
+    """ODPProxDcnvBlock (scico/flax/inverse.py:228-313): ||A|| by power
+    iteration equals the largest |K(f)| of the circular convolution, and the
+    block's output is (alpha A^T y + ResNet(x)) (alpha ||A||^2 + 1) through the
+    DFT round trip."""
+    torch.manual_seed(0)
+    op = _CircConvOp(16)
+    blk = inverse.ODPProxDcnvBlock(op, depth=2, channels=1, num_filters=4, alpha_ini=0.7)
+    assert blk.operator_norm == pytest.approx(float(op.kf.abs().max()), rel=1e-4)
+    x = torch.rand((3, 16, 16))
+    y = op.project(torch.rand((3, 16, 16)))
+    out = blk(x, y)
+    a = 0.7
+    ref = (a * op.back_project(y) + blk.resnet(x.unsqueeze(1)).squeeze(1)) * (a * blk.operator_norm ** 2 + 1)
+    assert float((out - ref).norm() / ref.norm()) <= 1e-5
+    g = torch.autograd.grad(out.sum(), [blk.alpha])[0]
+    assert torch.isfinite(g).all()
+
+
+def test_odp_deconvolution_training_cpu():
+    torch.manual_seed(0)
+    op = _CircConvOp(8)
+    net = inverse.ODPNet(op, depth=2, channels=1, num_filters=4, block_depth=2, alpha_ini=0.05,
+                         odp_block=inverse.ODPProxDcnvBlock)
+    cfg = {"device": "cpu", "seed": 1, "opt_type": "ADAM", "batch_size": 4, "num_epochs": 6,
+           "base_learning_rate": 1e-2, "log_every_steps": 6, "checkpointing": False}
+    tr = train.BasicTrainer(cfg, net, _toy_data(op, 16, 2), _toy_data(op, 8, 3))
+    state, stats = tr.train()
+    assert stats[-1]["Train_Loss"] < stats[0]["Train_Loss"]
