@@ -65,6 +65,19 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM = 6800.0
 
 
+def solve_projections(cg_its):
+    """Projector applications (forward or adjoint calls that run) of one
+    fused solve: A^T y once; A x and A^T A x in the first iteration and after
+    every iteration whose CG moved x; one pair per CG step; A x in the
+    epilogue when the last CG moved x.  The reference's loop applies 4 per
+    iteration (A^T y, the CG start's pair, the objective's A x) and 2 per CG
+    step."""
+    n = 1 + (1 if cg_its and cg_its[-1] > 0 else 0)
+    for i, k in enumerate(cg_its):
+        n += (2 if i == 0 or cg_its[i - 1] > 0 else 0) + 2 * k
+    return n
+
+
 def solve_launches(cg_its):
     """Kernel launches of one fused solve whose iterations ran cg_its CG
     steps: A^T y, its split sum, z/u init and the call reset (4); per
@@ -312,6 +325,7 @@ def run_reference(args):
         "solve_s": total_t, "cg_steps_total": int(sum(r["cg"])),
         "iterations_with_cg_steps": int(sum(1 for k in r["cg"] if k > 0)),
         "projector_applications": int(4 * c.maxiter + 2 * sum(r["cg"])), "final_objective": r["objective"],
+        "ms_per_cg_step": 1e3 * total_t / max(1, int(sum(r["cg"]))),
         "ref_precision": args.ref_precision,
     }
     print(json.dumps(line), flush=True)
@@ -522,6 +536,8 @@ def run_gpu(args):
             "final_objective": objective,
             "cg_steps_total": int(sum(cg_its)),
             "iterations_with_cg_steps": int(sum(1 for k in cg_its if k > 0)),
+            "projector_applications": solve_projections(cg_its),
+            "ms_per_cg_step": 1e3 * t_max / args.steps / max(1, int(sum(cg_its))),
         }
         if not args.no_secondary and world == 1:
             del ws, pws, flush
