@@ -113,6 +113,32 @@ def test_xray2d_mass_and_adjoint():
     assert abs(a - b) / max(abs(a), abs(b)) < 1e-5
 
 
+def _reference_code_cases():
+    z = np.load(GOLDEN / "xray2d_reference_code.npz")
+    for k in range(len([n for n in z.files if n.endswith("_image")])):
+        p = f"c{k}_"
+        g = ctref.xray2d_defaults(tuple(int(v) for v in z[p + "shape"]), z[p + "angles"],
+                                  dx=tuple(float(v) for v in z[p + "dx"]), det_count=int(z[p + "det"]))
+        yield k, z, p, g
+
+
+def test_xray2d_oracle_is_the_reference_code():
+    """The float32 2D projector oracle against the reference's own
+    _calc_weights / _project / _back_project (scico/linop/xray/_xray2d.py:
+    223-351) executed under a float32 jax.numpy stand-in
+    (tests/golden/make_xray2d_reference.py): bit-identical weights, detector
+    indices, projections and back projections on five geometries."""
+    n = 0
+    for k, z, p, g in _reference_code_cases():
+        if p + "inds" in z.files:
+            inds, w = ctref.xray2d_calc_weights(g)
+            assert np.array_equal(inds, z[p + "inds"]) and np.array_equal(w, z[p + "weights"]), k
+        assert np.array_equal(ctref.xray2d_project(z[p + "image"], g, np.float32), z[p + "project"]), k
+        assert np.array_equal(ctref.xray2d_back_project(z[p + "sino_in"], g, np.float32), z[p + "back_project"]), k
+        n += 1
+    assert n == 5
+
+
 def test_xray2d_f32_vs_f64():
     rng = np.random.default_rng(4)
     im = rng.random((20, 20)).astype(np.float32)
