@@ -45,6 +45,8 @@ class JArr(np.ndarray):
     def __array_ufunc__(self, ufunc, method, *inputs, **kwargs):
         args = [np.asarray(a) if isinstance(a, np.ndarray) else a for a in inputs]
         floats = [a.dtype for a in args if isinstance(a, np.ndarray) and a.dtype.kind == "f"]
+        if not floats and any(isinstance(a, float) for a in args):
+            floats = [np.dtype(np.float32)]  # a weak python float meets integers: float32
         if floats:
             ft = np.result_type(*floats)
             args = [a.astype(ft) if isinstance(a, np.ndarray) and a.dtype.kind in "iub" and ufunc.nin == 2 else a
@@ -108,7 +110,7 @@ class _At:
 
         class _Upd:
             @staticmethod
-            def add(v):
+            def add(v, mode=None):
                 # jax.numpy scatter: negative indices count from the end,
                 # updates at out-of-range indices are dropped; the others are
                 # added one after another in index order
@@ -158,12 +160,33 @@ class _JNP:
     def arange(n):
         return _wrap(np.arange(n, dtype=np.int32))
 
+    class _MGrid:
+        def __getitem__(self, idx):
+            return _wrap(np.mgrid[idx].astype(np.int32))
+
+    mgrid = _MGrid()
+
     def __getattr__(self, name):  # min, max, abs, floor, minimum, where, sum
         fn = getattr(np, name)
         return lambda *a, **k: _wrap(fn(*[np.asarray(x) if isinstance(x, np.ndarray) else x for x in a], **k))
 
 
+class _LAX:
+    @staticmethod
+    def map(f, xs, batch_size=None):
+        return _wrap(np.stack([np.asarray(f(_wrap(np.asarray(x)))) for x in np.asarray(xs)]))
+
+    @staticmethod
+    def scan(f, init, xs):
+        carry = init
+        for k in range(len(np.asarray(xs[0]))):
+            carry, _ = f(carry, tuple(_wrap(np.asarray(a)[k]) for a in xs))
+        return carry, None
+
+
 class _JAX:
+    lax = _LAX
+
     @staticmethod
     def jit(f=None, **_):
         return f if f is not None else (lambda g: g)
