@@ -161,6 +161,29 @@ def test_xray3d_oracle_is_the_reference_code():
                               z[p + "back_project"]), k
 
 
+def test_cg_oracle_is_the_reference_code():
+    """The oracle's CG (scico.solver.cg restated) against scico's own cg
+    (scico/solver.py:326-405) executed under the float32 jax.numpy stand-in
+    on the ADMM-TV x-update system rho D^T D + A^T A with the reference's
+    own projector code (tests/golden/make_cg_reference.py): bit-identical
+    iterates, step counts and relative residuals, stopped by the tolerance
+    (32 steps) and by maxiter (6)."""
+    z = np.load(GOLDEN / "cg_reference_code.npz")
+    for k in range(2):
+        p = f"c{k}_"
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        g = ctref.xray2d_defaults((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
+
+        def A(v):
+            dtd = ctref.fd_adj(ctref.fd_eval(v, axes=None, append=0), v.shape, axes=None, append=0)
+            ata = ctref.xray2d_back_project(ctref.xray2d_project(v, g, np.float32), g, np.float32)
+            return np.float32(2.0) * dtd + np.float32(1.0) * ata
+
+        x, info = ctref.cg(A, z[p + "b"], z[p + "x0"], tol=float(z[p + "tol"]), maxiter=int(z[p + "maxiter"]))
+        assert np.array_equal(x, z[p + "x"]), k
+        assert info["num_iter"] == int(z[p + "num_iter"]) and info["rel_res"] == float(z[p + "rel_res"]), k
+
+
 def test_xray2d_f32_vs_f64():
     rng = np.random.default_rng(4)
     im = rng.random((20, 20)).astype(np.float32)
