@@ -313,9 +313,15 @@ def fd_eval(x: np.ndarray, axes=None, prepend=None, append=None, circular=False)
 
 
 def fd_single_adj(d: np.ndarray, n: int, axis: int, prepend=None, append=None, circular=False) -> np.ndarray:
-    """Adjoint of fd_single (the transpose that jax.linear_transpose builds,
-    scico/_core.py:140-153), written as the telescoped sum over the positions
-    of the extended line that hold x[t]."""
+    """Adjoint of fd_single as jax.linear_transpose builds it from _eval
+    (scico/linop/_diff.py:236-272, scico/_core.py:140-153).  jnp.diff forms
+    the extended line e (prepend / append copies concatenated to x) and
+    d = e[1:] - e[:-1]; its transpose gives e the cotangent
+    ce[q] = pad(d, (1, 0))[q] + pad(-d, (0, 1))[q] = d[q-1] - d[q] (a missing
+    term is 0), and x[t] receives ce[q] of every position q holding x[t],
+    summed in float32: one position for interior samples, two at a copied
+    end (prepend=0 at t=0, append=0 at t=n-1), three for a single-sample
+    axis with both (summed in position order)."""
     d = np.moveaxis(np.asarray(d), axis, 0)
     M = d.shape[0]
     out = np.zeros((n,) + d.shape[1:], dtype=d.dtype)
@@ -325,12 +331,17 @@ def fd_single_adj(d: np.ndarray, n: int, axis: int, prepend=None, append=None, c
         return np.moveaxis(out, 0, axis)
     P = 1 if prepend is not None else 0
     z = np.zeros(d.shape[1:], dtype=d.dtype)
+
+    def ce(q):
+        return (d[q - 1] if 0 <= q - 1 < M else z) - (d[q] if 0 <= q < M else z)
+
     for t in range(n):
         qa = 0 if (prepend == 0 and t == 0) else t + P
         qb = n + P if (append == 0 and t == n - 1) else t + P
-        lo = d[qa - 1] if 0 <= qa - 1 < M else z
-        hi = d[qb] if 0 <= qb < M else z
-        out[t] = lo - hi
+        v = ce(qa)
+        for q in range(qa + 1, qb + 1):
+            v = v + ce(q)
+        out[t] = v
     return np.moveaxis(out, 0, axis)
 
 

@@ -108,10 +108,12 @@ __global__ void k_fd_fwd(const float* __restrict__ x, float* __restrict__ out, F
   }
 }
 
-// Adjoint: x[t] = sum over blocks (axis order) of
-//   [0 <= qa-1 < M] d[qa-1] - [0 <= qb < M] d[qb]
-// where [qa, qb] is the run of extended-line positions holding x[t]
-// (positions of one run telescope, so only its end points remain).
+// Adjoint, as jax.linear_transpose builds it from the forward's jnp.diff:
+// extended-line position q gets the cotangent ce[q] = d[q-1] - d[q] (a term
+// outside 0..M-1 is 0), and x[t] = sum over blocks (axis order) of the sum,
+// in position order, of ce[q] over the run [qa, qb] of positions holding
+// x[t] -- one position inside the line, two at an end copied by prepend=0 /
+// append=0 (the float32 sum (d[0] - d[1]) - d[0] is not -d[1] in general).
 __global__ void k_fd_adj(const float* __restrict__ d, float* __restrict__ x, FdParams p,
                          int batch) {
   const size_t total = p.in_count * batch;
@@ -144,9 +146,13 @@ __global__ void k_fd_adj(const float* __restrict__ d, float* __restrict__ x, FdP
       } else {
         const int qa = (p.prepend == 0 && t == 0) ? 0 : t + P;
         const int qb = (p.append == 0 && t == n - 1) ? n + P : t + P;
-        const float lo = (qa - 1 >= 0 && qa - 1 < B.M) ? __ldg(line + (size_t)(qa - 1) * stride) : 0.0f;
-        const float hi = (qb >= 0 && qb < B.M) ? __ldg(line + (size_t)qb * stride) : 0.0f;
-        v = ct::fsub(lo, hi);
+        auto ce = [&](int q) {
+          const float lo = (q - 1 >= 0 && q - 1 < B.M) ? __ldg(line + (size_t)(q - 1) * stride) : 0.0f;
+          const float hi = (q >= 0 && q < B.M) ? __ldg(line + (size_t)q * stride) : 0.0f;
+          return ct::fsub(lo, hi);
+        };
+        v = ce(qa);
+        for (int q = qa + 1; q <= qb; ++q) v = ct::fadd(v, ce(q));
       }
       acc = (k == 0) ? v : ct::fadd(acc, v);
     }

@@ -74,6 +74,45 @@ def test_golden_admm(cuda):
 
 
 @pytest.mark.parametrize("fused", [False, True])
+def test_reference_code_admm(cuda, fused):
+    """Against the iterates of scico's own ADMM / LinearSubproblemSolver / cg /
+    L21Norm / FiniteDifference / projector code run under the float32
+    jax.numpy stand-in (tests/golden/admm_reference_code.npz).  Case 0 (CG
+    stopped by its tolerance): x within 1e-4 rel l2 after every iteration
+    and the objective to 1e-4.  Case 1 (CG capped at 10): within 3x the
+    distance at which the same-precision oracle (float32 vectors, float64
+    dots, as here) ends from the reference code, plus 1e-4."""
+    z = np.load(GOLDEN / "admm_reference_code.npz")
+    for k in range(2):
+        p = f"c{k}_"
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        ang = np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32)
+        X, its = z[p + "x"], len(z[p + "x"])
+        kw = dict(lam21=float(z[p + "lam"]), rho=float(z[p + "rho"]), cg_tol=float(z[p + "cg_tol"]),
+                  cg_maxiter=int(z[p + "cg_maxiter"]))
+        obj_ref = z[p + "itstat"][:, 0]
+        if k == 0:
+            fx = fo = 0.0
+        else:
+            g = ctref.xray2d_defaults((n, n), ang)
+            xm, hm, _, _ = _oracle(z[p + "y"], (n, n), g, dtype=np.float32, dot_dtype=np.float64,
+                                   lam_l21=kw["lam21"], rho=kw["rho"], maxiter=its, cg_tol=kw["cg_tol"],
+                                   cg_maxiter=kw["cg_maxiter"])
+            fx = ctref.rel_l2(xm, X[-1])
+            fo = float(np.max(np.abs(np.array([h["Objective"] for h in hm]) / obj_ref - 1)))
+        s = _solver(cuda, ang, z[p + "y"], (n, n), maxiter=its, fused=fused, **kw)
+        x = s.solve().cpu().numpy()
+        ex = ctref.rel_l2(x, X[-1])
+        eo = float(np.max(np.abs(np.array(s.history(transpose=True).Objective) / obj_ref - 1)))
+        assert ex <= 3 * fx + 1e-4, (k, ex, fx)
+        assert eo <= 3 * fo + 1e-4, (k, eo, fo)
+        if k == 0:
+            for it in range(1, its):  # every intermediate iterate of the tolerance-stopped case
+                xi = _solver(cuda, ang, z[p + "y"], (n, n), maxiter=it, fused=fused, **kw).solve().cpu().numpy()
+                assert ctref.rel_l2(xi, X[it - 1]) <= 1e-4, (it, ctref.rel_l2(xi, X[it - 1]))
+
+
+@pytest.mark.parametrize("fused", [False, True])
 @pytest.mark.parametrize("terms", ["l21", "l1", "both"])
 def test_admm_converged_vs_oracle(cuda, fused, terms):
     x_gt, ang, g, y = _problem()

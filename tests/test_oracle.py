@@ -73,6 +73,40 @@ def test_fd_adjoint_dot(shape, mode):
         np.testing.assert_allclose(np.sum(d * r), np.sum(x * back), rtol=1e-12)
 
 
+@pytest.mark.parametrize("shape", [(1,), (2,), (16,), (5, 6, 7)])
+@pytest.mark.parametrize("mode", ["none", "pre0", "pre1", "app0", "app1", "both00", "both01", "circ"])
+def test_fd_adjoint_is_the_jax_transpose(shape, mode):
+    """The oracle's single-axis adjoint against the transpose jax builds for
+    jnp.diff (scico obtains FiniteDifference.adj by jax.linear_transpose of
+    _eval, scico/linop/_diff.py:236-272): the extended line's cotangent
+    pad(d, (1, 0)) + pad(-d, (0, 1)), its x part, plus the cotangents of the
+    copied end samples; float32, bit for bit, on arbitrary d (not only on
+    the range of D, where the copied ends hold 0)."""
+    kw = dict(none={}, pre0=dict(prepend=0), pre1=dict(prepend=1), app0=dict(append=0),
+              app1=dict(append=1), both00=dict(prepend=0, append=0), both01=dict(prepend=0, append=1),
+              circ=dict(circular=True))[mode]
+    pre, app, circ = kw.get("prepend"), kw.get("append"), kw.get("circular", False)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(shape).astype(np.float32)
+    for ax in range(len(shape)):
+        n = shape[ax]
+        d = ctref.fd_single(x, ax, pre, app, circ)
+        r = rng.standard_normal(d.shape).astype(np.float32)
+        ct = np.moveaxis(r, ax, 0)
+        zero = np.zeros((1,) + ct.shape[1:], np.float32)
+        ce = np.concatenate([zero, ct]) + np.concatenate([-ct, zero])
+        P = 1 if pre is not None else 0
+        want = ce[P:P + n].copy()
+        if pre == 0:
+            want[0] = ce[0] + want[0]
+        if app == 0:
+            want[n - 1] = want[n - 1] + ce[n + P]
+        if circ:
+            want[0] = want[0] + ce[n]
+        got = ctref.fd_single_adj(r, n, ax, pre, app, circ)
+        assert np.array_equal(got, np.moveaxis(want, 0, ax)), (ax, mode)
+
+
 def test_xray2d_angle0_sums_rows():
     """Angle 0 sums image rows (_xray2d.py:66-70): exact with unit pixels."""
     rng = np.random.default_rng(1)
@@ -182,6 +216,39 @@ def test_cg_oracle_is_the_reference_code():
         x, info = ctref.cg(A, z[p + "b"], z[p + "x0"], tol=float(z[p + "tol"]), maxiter=int(z[p + "maxiter"]))
         assert np.array_equal(x, z[p + "x"]), k
         assert info["num_iter"] == int(z[p + "num_iter"]) and info["rel_res"] == float(z[p + "rel_res"]), k
+
+
+def _admm_case(z, k):
+    p = f"c{k}_"
+    n, nv = int(z[p + "n"]), int(z[p + "nv"])
+    g = ctref.xray2d_defaults((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
+    kw = dict(lam_l21=float(z[p + "lam"]), rho=float(z[p + "rho"]), cg_tol=float(z[p + "cg_tol"]),
+              cg_maxiter=int(z[p + "cg_maxiter"]))
+    return p, n, g, kw
+
+
+def test_admm_oracle_is_the_reference_code():
+    """The oracle's ADMM-TV against scico's own ADMM.step, LinearSubproblemSolver
+    .compute_rhs/.solve, cg, L21Norm prox, FiniteDifference and projector
+    code executed under the float32 jax.numpy stand-in
+    (tests/golden/make_admm_reference.py): the iterate x after every
+    iteration, the final z and u and every x-update's CG step count are
+    bit-identical, with CG stopped by its tolerance (rho 50) and capped at 10
+    steps (rho 2, lambda 0.005).  The itstat values, which the reference sums
+    in float32 and the oracle in float64, agree to 1e-6."""
+    z = np.load(GOLDEN / "admm_reference_code.npz")
+    for k in range(2):
+        p, n, g, kw = _admm_case(z, k)
+        fwd = lambda v: ctref.xray2d_project(v, g, np.float32)
+        adj = lambda s: ctref.xray2d_back_project(s, g, np.float32)
+        X = z[p + "x"]
+        for it in (1, len(X)):
+            x, hist, zl, ul = ctref.admm_tv(fwd, adj, z[p + "y"], (n, n), maxiter=it, dtype=np.float32, **kw)
+            assert np.array_equal(x, X[it - 1]), (k, it)
+        assert np.array_equal(zl[0], z[p + "z"]) and np.array_equal(ul[0], z[p + "u"]), k
+        assert [h["CG_It"] for h in hist] == list(z[p + "cg_iters"]), k
+        ours = np.array([[h["Objective"], h["Prml_Rsdl"], h["Dual_Rsdl"]] for h in hist])
+        np.testing.assert_allclose(ours, z[p + "itstat"], rtol=1e-6)
 
 
 def test_xray2d_f32_vs_f64():
