@@ -366,6 +366,8 @@ __global__ void __launch_bounds__(NT)
           const float* __restrict__ dz, float* __restrict__ rhs, Shape3 sh, size_t N, TermParams tp,
           double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
           int vec, cudaGraphConditionalHandle dirty, int use_dirty) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (use_dirty && blockIdx.x == 0 && threadIdx.x == 0)
     cudaGraphSetConditional(dirty, slots[S_XCLEAN] == 0.0 ? 1u : 0u);
   ct::KSum ks;  // dual residual
@@ -416,6 +418,8 @@ __global__ void __launch_bounds__(NT)
     k_resid2(const float* __restrict__ sino, const float* __restrict__ y, size_t n,
              double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
              int vec) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (slots[S_XCLEAN] != 0.0) return;  // x unchanged: S_RESID2 is current
   ct::KSum ks;
   if (vec) {
@@ -483,6 +487,8 @@ __device__ __forceinline__ void write_record(const RecParams& rp, double* __rest
 
 // The last record of a call (the statistics epilogue).
 __global__ void k_itstat_final(RecParams rp, double* __restrict__ slots) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   write_record(rp, slots);
   slots[S_HAVE_PREV] = 0.0;
@@ -502,6 +508,8 @@ __global__ void __launch_bounds__(NT)
                  double* __restrict__ cg, double tol, double atol, int maxiter,
                  double* __restrict__ partials, unsigned int* __restrict__ ticket,
                  cudaGraphConditionalHandle cond, int use_cond, int vec, RecParams rp) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (!INIT && cg[CT_CG_DONE] != 0.0) return;
   const bool cached = INIT && slots[S_XCLEAN] != 0.0;
   double acc[2] = {0.0, 0.0};
@@ -739,6 +747,8 @@ __global__ void __launch_bounds__(NT)
          Shape3 sh, size_t N, TermParams tp, double* __restrict__ slots, double* __restrict__ partials,
          unsigned int* __restrict__ ticket, int vec, cudaGraphConditionalHandle loop, int use_loop,
          int maxiter) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   ct::KSum ks[3];  // primal, g21, g1
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
@@ -775,6 +785,8 @@ __global__ void __launch_bounds__(NT)
 }
 
 __global__ void k_reset_call(double* __restrict__ slots) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   slots[S_REC] = 0.0;
   slots[S_HAVE_PREV] = 0.0;
   slots[S_XCLEAN] = 0.0;  // the caller may have changed x between calls
@@ -810,12 +822,16 @@ struct Projector {
   size_t adj_ws_bytes() const { return nd == 2 ? p2.adj_ws_bytes : p3.adj_ws_bytes; }
   int nsplit() const { return nd == 2 ? p2.nsplit : p3.nsplit; }
   ct_status prepare() const { return nd == 2 ? ct::proj2d_prepare(p2) : ct::proj3d_prepare(g3, p3); }
-  ct_status fwd(const float* img, float* sino, void* ws, cudaStream_t s, const double* skip) const {
-    return nd == 2 ? ct::proj2d_fwd_launch(g2, p2, img, sino, 1, static_cast<float*>(ws), s, skip)
+  ct_status fwd(const float* img, float* sino, void* ws, cudaStream_t s, const double* skip,
+                bool dependent = false) const {
+    return nd == 2 ? ct::proj2d_fwd_launch(g2, p2, img, sino, 1, static_cast<float*>(ws), s, skip, dependent)
                    : ct::proj3d_fwd_launch(g3, p3, img, sino, ws, s, skip);
   }
-  ct_status adj(const float* sino, float* out, float* part, cudaStream_t s, const double* skip) const {
-    return nd == 2 ? ct::proj2d_adj_launch(g2, p2, sino, out, part, 1, s, skip)
+  // dependent: the 2D adjoint may be launched as the dependent of its stream
+  // predecessor, one of this library's kernels
+  ct_status adj(const float* sino, float* out, float* part, cudaStream_t s, const double* skip,
+                bool dependent = false) const {
+    return nd == 2 ? ct::proj2d_adj_launch(g2, p2, sino, out, part, 1, s, skip, dependent)
                    : ct::proj3d_adj_launch(g3, p3, sino, out, part, s, skip);
   }
 };
@@ -956,16 +972,19 @@ struct Ctx {
       kernel<3><<<(grid), (block), 0, (stream)>>>(__VA_ARGS__);            \
   } while (0)
 
+// Inside a solve every kernel follows one of this library's kernels: the
+// solver's launches are dependent ones (launch_k in common.cuh).
 ct_status project(const Ctx& c, const float* img, float* sino, cudaStream_t s, const double* skip) {
-  return c.P.proj.fwd(img, sino, c.at<float>(c.L.off_fwd), s, skip);
+  return c.P.proj.fwd(img, sino, c.at<float>(c.L.off_fwd), s, skip, true);
 }
 
 // A^T of a sinogram into the adjoint buffer (or its view splits); returns
 // the buffer to read.
-const float* backproject(const Ctx& c, const float* sino, cudaStream_t s, const double* skip, ct_status& st) {
+const float* backproject(const Ctx& c, const float* sino, cudaStream_t s, const double* skip, ct_status& st,
+                         bool dependent = false) {
   float* adj = c.at<float>(c.L.off_adj);
   float* part = c.at<float>(c.L.off_adjpart);
-  st = c.P.proj.adj(sino, adj, part, s, skip);
+  st = c.P.proj.adj(sino, adj, part, s, skip, dependent);
   return c.P.proj.nsplit() > 1 ? part : adj;
 }
 
@@ -984,20 +1003,24 @@ RecParams rec_params(const Ctx& c) {
 //   CG    enqueue_cg_step per step
 //   post  k_zu (with loop/use_loop: ends the graph's iteration)
 ct_status enqueue_rhs(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle dirty, int use_dirty) {
-  CT_LAUNCH_ND(c.P.nd, k_rhs, NB, NT, s, c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
-               c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N, c.tp,
-               c.slots(), c.partials(), c.ticket(), c.vi, dirty, use_dirty);
-  return ct::launch_check("k_rhs");
+  auto k = c.P.nd == 2 ? k_rhs<2> : k_rhs<3>;
+  return ct::cuda_check(ct::launch_k(k, dim3(NB), dim3(NT), 0, s, true, (const float*)c.at<float>(c.L.off_atyc),
+                                     (const float*)c.at<float>(c.L.off_z), (const float*)c.at<float>(c.L.off_u),
+                                     (const float*)c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N,
+                                     c.tp, c.slots(), c.partials(), c.ticket(), c.vi, dirty, use_dirty),
+                        "k_rhs");
 }
 
 ct_status enqueue_proj(const Ctx& c, cudaStream_t s) {
   float* sinox = c.at<float>(c.L.off_sinox);
   const double* clean = c.slots() + S_XCLEAN;
   CT_TRY(project(c, c.x, sinox, s, clean));
-  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket(), c.vs);
-  CT_TRY(ct::launch_check("k_resid2"));
+  // resid2 and the adjoint follow kernels of this library: dependent launches
+  CT_TRY(ct::cuda_check(ct::launch_k(k_resid2, dim3(NB), dim3(NT), 0, s, true, (const float*)sinox, c.y, c.P.S,
+                                     c.slots(), c.partials(), c.ticket(), c.vs),
+                        "k_resid2"));
   ct_status st;
-  backproject(c, sinox, s, clean, st);
+  backproject(c, sinox, s, clean, st, true);
   return st;
 }
 
@@ -1007,17 +1030,12 @@ ct_status enqueue_init(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle 
   float* r = c.at<float>(c.L.off_r);
   float* p = c.at<float>(c.L.off_p);
   float* rhs = c.at<float>(c.L.off_rhs);
-  if (c.P.nd == 2)
-    k_lhs_finish<2, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
-                                            c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
-                                            c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
-                                            cond, use_cond, c.vi, rec_params(c));
-  else
-    k_lhs_finish<3, true><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), c.x, c.P.sh, N, c.tp, r, rhs, p,
-                                            c.at<float>(c.L.off_lhsx), c.slots(), c.cg(), c.P.prm.cg_tol,
-                                            c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(), c.ticket(),
-                                            cond, use_cond, c.vi, rec_params(c));
-  return ct::launch_check("k_lhs_finish<init>");
+  auto k = c.P.nd == 2 ? k_lhs_finish<2, true> : k_lhs_finish<3, true>;
+  return ct::cuda_check(ct::launch_k(k, dim3(NB), dim3(NT), 0, s, true, adj, c.P.proj.nsplit(), (const float*)c.x,
+                                     c.P.sh, N, c.tp, r, (const float*)rhs, p, c.at<float>(c.L.off_lhsx), c.slots(),
+                                     c.cg(), c.P.prm.cg_tol, c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.partials(),
+                                     c.ticket(), cond, use_cond, c.vi, rec_params(c)),
+                        "k_lhs_finish<init>");
 }
 
 ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle cond, int use_cond) {
@@ -1028,29 +1046,29 @@ ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHand
   float* sino = c.at<float>(c.L.off_sino);
   const double* done = c.cg() + CT_CG_DONE;
   CT_TRY(project(c, p, sino, s, done));
+  // every kernel after the forward's first follows a kernel of this library:
+  // dependent launches (launch_k in common.cuh)
   ct_status st;
-  const float* adj = backproject(c, sino, s, done, st);
+  const float* adj = backproject(c, sino, s, done, st, true);
   CT_TRY(st);
-  if (c.P.nd == 2)
-    k_lhs_finish<2, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
-                                             nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
-                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi,
-                                             RecParams{});
-  else
-    k_lhs_finish<3, false><<<NB, NT, 0, s>>>(adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, nullptr,
-                                             nullptr, nullptr, c.slots(), c.cg(), 0.0, 0.0,
-                                             c.P.prm.cg_maxiter, c.partials(), c.ticket(), 0, 0, c.vi,
-                                             RecParams{});
-  CT_TRY(ct::launch_check("k_lhs_finish<pap>"));
-  CT_TRY(ct::cg_update_launch(c.x, r, p, ap, N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond));
-  return ct::cg_direction_launch(p, r, N, c.cg(), c.ws + c.L.off_red, s);
+  float* nf = nullptr;
+  const float* ncf = nullptr;
+  auto lhs = c.P.nd == 2 ? k_lhs_finish<2, false> : k_lhs_finish<3, false>;
+  CT_TRY(ct::cuda_check(ct::launch_k(lhs, dim3(NB), dim3(NT), 0, s, true, adj, c.P.proj.nsplit(), (const float*)p,
+                                     c.P.sh, N, c.tp, ap, ncf, nf, nf, c.slots(), c.cg(), 0.0, 0.0,
+                                     c.P.prm.cg_maxiter, c.partials(), c.ticket(), (cudaGraphConditionalHandle)0, 0,
+                                     c.vi, RecParams{}),
+                        "k_lhs_finish<pap>"));
+  CT_TRY(ct::cg_update_launch(c.x, r, p, ap, N, c.cg(), c.ws + c.L.off_red, s, cond, use_cond, true));
+  return ct::cg_direction_launch(p, r, N, c.cg(), c.ws + c.L.off_red, s, true);
 }
 
 ct_status enqueue_post(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle loop, int use_loop) {
-  CT_LAUNCH_ND(c.P.nd, k_zu, NB, NT, s, c.x, c.at<float>(c.L.off_z), c.at<float>(c.L.off_u),
-               c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp, c.slots(), c.partials(), c.ticket(), c.vi, loop,
-               use_loop, c.P.prm.maxiter);
-  return ct::launch_check("k_zu");
+  auto k = c.P.nd == 2 ? k_zu<2> : k_zu<3>;
+  return ct::cuda_check(ct::launch_k(k, dim3(NB), dim3(NT), 0, s, true, (const float*)c.x, c.at<float>(c.L.off_z),
+                                     c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.P.sh, c.P.N, c.tp,
+                                     c.slots(), c.partials(), c.ticket(), c.vi, loop, use_loop, c.P.prm.maxiter),
+                        "k_zu");
 }
 
 // One iteration as plain launches (no graph): cg_maxiter CG steps that turn
@@ -1068,10 +1086,11 @@ ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
   float* sinox = c.at<float>(c.L.off_sinox);
   CT_TRY(enqueue_rhs(c, s, 0, 0));
   CT_TRY(project(c, c.x, sinox, s, c.slots() + S_XCLEAN));
-  k_resid2<<<NB, NT, 0, s>>>(sinox, c.y, c.P.S, c.slots(), c.partials(), c.ticket(), c.vs);
-  CT_TRY(ct::launch_check("k_resid2"));
-  k_itstat_final<<<1, 32, 0, s>>>(rec_params(c), c.slots());
-  return ct::launch_check("k_itstat_final");
+  CT_TRY(ct::cuda_check(ct::launch_k(k_resid2, dim3(NB), dim3(NT), 0, s, true, (const float*)sinox, c.y, c.P.S,
+                                     c.slots(), c.partials(), c.ticket(), c.vs),
+                        "k_resid2"));
+  return ct::cuda_check(ct::launch_k(k_itstat_final, dim3(1), dim3(32), 0, s, true, rec_params(c), c.slots()),
+                        "k_itstat_final");
 }
 
 // Executable iteration graphs, one per problem (key: dimension, descriptor

@@ -2,6 +2,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "common.cuh"
@@ -24,6 +25,14 @@ ct_status cuda_check(cudaError_t e, const char* what) {
 }
 
 ct_status launch_check(const char* what) { return cuda_check(cudaGetLastError(), what); }
+
+bool dependent_launch_enabled() {
+  static const bool on = [] {
+    const char* v = getenv("CTGPU_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
 
 int sm_count() {
   static int cached[64] = {0};

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "ctgpu.h"
 
 namespace ct {
@@ -19,6 +21,54 @@ ct_status launch_check(const char* what);
 int sm_count();
 
 inline cudaStream_t as_stream(ct_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch.  A kernel launched by launch_k with
+// dependent = true may be scheduled while its stream predecessor -- always
+// one of this library's kernels -- is still finishing, which hides the host
+// launch latency between the back-to-back kernels of a CG step (the 512^2 /
+// 360-view solve with plain launches: 34.4 -> 21.1 ms).  Every kernel that
+// can be launched that way calls grid_dep_wait() before it touches global
+// memory: it returns once the predecessor grid has completed and its writes
+// are visible (at once for a normal launch), so the kernel sees exactly what
+// stream order would give it.  grid_dep_trigger() then lets the kernel's own
+// successor be scheduled.  While the stream is being captured into a CUDA
+// graph the launch is a normal one: graph kernel nodes already follow one
+// another without the host gap, and dependent edges measured no faster there
+// (the same solve as one graph: 9.55 ms either way).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Dependent launches are on unless the environment sets CTGPU_PDL=0
+// (read once per process).
+bool dependent_launch_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                            bool dependent, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  bool dep = dependent && dependent_launch_enabled();
+  if (dep) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+      (void)cudaGetLastError();  // not an error of the launch: launch normally
+      dep = false;
+    } else if (cs != cudaStreamCaptureStatusNone) {
+      dep = false;
+    }
+  }
+  cfg.attrs = attr;
+  cfg.numAttrs = dep ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 __host__ __device__ inline bool aligned(const void* p, size_t a) {
   return (reinterpret_cast<uintptr_t>(p) % a) == 0;

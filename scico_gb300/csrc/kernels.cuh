@@ -38,13 +38,19 @@ ct_status proj2d_prepare(const Proj2dPlan& p);
 
 // sino = A img.  `skip` (device, may be null): when *skip != 0 the kernels
 // return immediately (used to freeze converged CG iterations in a graph).
+// dependent: the stream predecessor is one of this library's kernels, so the
+// first kernel may be launched as its dependent (launch_k in common.cuh).
 ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* img, float* sino,
-                            int batch, float* part, cudaStream_t s, const double* skip);
+                            int batch, float* part, cudaStream_t s, const double* skip,
+                            bool dependent = false);
 
 // A^T sino.  With p.nsplit == 1 the result goes to `out`; otherwise split k
 // of the views goes to part + k * batch*rows*cols and the caller sums them.
+// dependent: the stream predecessor is one of this library's kernels, so the
+// adjoint may be launched as its dependent (launch_k in common.cuh).
 ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* sino, float* out,
-                            float* part, int batch, cudaStream_t s, const double* skip);
+                            float* part, int batch, cudaStream_t s, const double* skip,
+                            bool dependent = false);
 
 // ---- 3D projector (proj3d.cu) ---------------------------------------------
 struct Proj3dPlan {
@@ -83,11 +89,13 @@ ct_status proj3d_adj_launch(const ct_geom3d* g, const Proj3dPlan& p, const float
 // ---- CG vector steps (vec.cu) ----------------------------------------------
 // cond/use_cond: in a graph with a conditional WHILE CG loop, the update sets
 // the loop condition to "not converged".
+// dependent: launched as the dependent of the stream predecessor, which
+// must be one of this library's kernels (launch_k in common.cuh).
 ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, size_t n,
                            double* scalars, void* red_ws, cudaStream_t s,
-                           cudaGraphConditionalHandle cond = 0, int use_cond = 0);
+                           cudaGraphConditionalHandle cond = 0, int use_cond = 0, bool dependent = false);
 ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, void* red_ws,
-                              cudaStream_t s);
+                              cudaStream_t s, bool dependent = false);
 
 // ---- generic N-way float64 grid sum (see grid_reduce_last in common.cuh) ----
 template <int NT, int K>

@@ -338,6 +338,8 @@ __device__ __forceinline__ void fwd_view_params(const FwdArgs& a, FwdViewSmem* v
 template <int LSC>
 __global__ void __launch_bounds__(kFW * 32, 3)
     k_proj2d_fwd_strips(const FwdArgs a, const __grid_constant__ CUtensorMap tmap) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   const int LS = LSC ? LSC : a.LS;
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -528,6 +530,8 @@ __global__ void __launch_bounds__(128)
     k_proj2d_fwd_gather(const float* __restrict__ part, float* __restrict__ sino,
                         const float* __restrict__ views, int nv, int det, int cspan, int n_chunks,
                         int n_strips, const double* __restrict__ skip) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (skip && *skip != 0.0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int v = blockIdx.x, b = blockIdx.z;
@@ -654,6 +658,8 @@ __device__ __forceinline__ void adj_view_gen(const float4 pv, float width, int b
 // (ty, tx) owns rows ty + 16 r (r < kAR) at columns tx + 16 q (q < kAPX) of
 // the 64 x 64 tile.
 __global__ void __launch_bounds__(kAdjThreads) k_proj2d_adj(const AdjArgs a) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (a.skip && *a.skip != 0.0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* sy = reinterpret_cast<float2*>(smem_raw);          // [kAVC][W]
@@ -946,7 +952,7 @@ ct_status proj2d_prepare(const Proj2dPlan& p) {
 }
 
 ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* img, float* sino,
-                            int batch, float* part, cudaStream_t s, const double* skip) {
+                            int batch, float* part, cudaStream_t s, const double* skip, bool dependent) {
   FwdArgs a;
   a.img = img;
   a.part = part;
@@ -967,20 +973,20 @@ ct_status proj2d_fwd_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   a.skip = skip;
   if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
   dim3 g1(p.n_strips, p.fwd_groups, batch);
-  if (p.LS == kLSDefault)
-    k_proj2d_fwd_strips<kLSDefault><<<g1, kFW * 32, p.fwd_smem, s>>>(a, tmap);
-  else
-    k_proj2d_fwd_strips<0><<<g1, kFW * 32, p.fwd_smem, s>>>(a, tmap);
-  ct_status st = launch_check("k_proj2d_fwd_strips");
+  auto strips = p.LS == kLSDefault ? k_proj2d_fwd_strips<kLSDefault> : k_proj2d_fwd_strips<0>;
+  ct_status st = cuda_check(launch_k(strips, g1, dim3(kFW * 32), p.fwd_smem, s, dependent, a, tmap),
+                            "k_proj2d_fwd_strips");
   if (st != CT_OK) return st;
+  // the gather follows the strips kernel: a dependent launch
   dim3 g2(g->n_views, (g->det_count + 255) / 256, batch);
-  k_proj2d_fwd_gather<<<g2, 128, 0, s>>>(
-      part, sino, g->views, g->n_views, g->det_count, p.cspan, p.n_chunks, p.n_strips, skip);
-  return launch_check("k_proj2d_fwd_gather");
+  return cuda_check(launch_k(k_proj2d_fwd_gather, g2, dim3(128), 0, s, true, (const float*)part, sino,
+                             (const float*)g->views, (int)g->n_views, (int)g->det_count, p.cspan, p.n_chunks,
+                             p.n_strips, skip),
+                    "k_proj2d_fwd_gather");
 }
 
 ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float* sino, float* out,
-                            float* part, int batch, cudaStream_t s, const double* skip) {
+                            float* part, int batch, cudaStream_t s, const double* skip, bool dependent) {
   AdjArgs a;
   a.sino = sino;
   a.out = p.nsplit > 1 ? part : out;
@@ -997,8 +1003,8 @@ ct_status proj2d_adj_launch(const ct_geom2d* g, const Proj2dPlan& p, const float
   a.skip = skip;
   if (!a.errflag) return fail(CT_ERR_CUDA, "proj2d: error-word address unavailable");
   dim3 grid(p.adj_gx, p.adj_gy, batch * p.nsplit);
-  k_proj2d_adj<<<grid, kAdjThreads, p.adj_smem, s>>>(a);
-  return launch_check("k_proj2d_adj");
+  return cuda_check(launch_k(k_proj2d_adj, grid, dim3(kAdjThreads), p.adj_smem, s, dependent, a),
+                    "k_proj2d_adj");
 }
 
 }  // namespace ct

@@ -135,6 +135,8 @@ __global__ void __launch_bounds__(NT)
                 const float* __restrict__ Ap, size_t n, double* __restrict__ s,
                 double* __restrict__ partials, unsigned int* __restrict__ ticket,
                 cudaGraphConditionalHandle cond, int use_cond, int vec) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (s[CT_CG_DONE] != 0.0) {  // uniform over the grid
     if (use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
     return;
@@ -204,6 +206,8 @@ __global__ void __launch_bounds__(NT)
 // word of the reduction workspace) clears it, after all blocks have read it.
 __global__ void k_cg_direction(float* __restrict__ p, const float* __restrict__ r, size_t n,
                                double* __restrict__ s, unsigned int* __restrict__ ticket, int vec) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
   if (s[CT_CG_RAN] == 0.0) return;  // uniform over the grid
   const float bf = (float)s[CT_CG_BETA];
   if (vec) {
@@ -300,19 +304,20 @@ namespace ct {
 
 ct_status cg_update_launch(float* x, float* r, const float* p, const float* Ap, size_t n,
                            double* scalars, void* red_ws, cudaStream_t s, cudaGraphConditionalHandle cond,
-                           int use_cond) {
+                           int use_cond, bool dependent) {
   unsigned int* ticket = static_cast<unsigned int*>(red_ws);
   double* partials = reinterpret_cast<double*>(static_cast<char*>(red_ws) + 256);
-  k_cg_update<<<kReduceBlocks, NT, 0, s>>>(x, r, p, Ap, n, scalars, partials, ticket, cond, use_cond,
-                                           quad_ok(n, x, r, p, Ap));
-  return launch_check("k_cg_update");
+  return cuda_check(launch_k(k_cg_update, dim3(kReduceBlocks), dim3(NT), 0, s, dependent, x, r, p, Ap, n, scalars,
+                             partials, ticket, cond, use_cond, quad_ok(n, x, r, p, Ap)),
+                    "k_cg_update");
 }
 
 ct_status cg_direction_launch(float* p, const float* r, size_t n, double* scalars, void* red_ws,
-                              cudaStream_t s) {
+                              cudaStream_t s, bool dependent) {
   unsigned int* ticket2 = static_cast<unsigned int*>(red_ws) + 1;
-  k_cg_direction<<<kReduceBlocks, NT, 0, s>>>(p, r, n, scalars, ticket2, quad_ok(n, p, r));
-  return launch_check("k_cg_direction");
+  return cuda_check(launch_k(k_cg_direction, dim3(kReduceBlocks), dim3(NT), 0, s, dependent, p, r, n, scalars,
+                             ticket2, quad_ok(n, p, r)),
+                    "k_cg_direction");
 }
 
 }  // namespace ct
