@@ -147,6 +147,8 @@ ct_status ct_proj2d_adj(const ct_geom2d* g, const float* sino, float* img,
  * tests use it to exercise the timeout path without a hung GPU.
  */
 ct_status ct_proj2d_check(ct_stream_t stream);
+/* (bit 3 of the word: a grid barrier wait of the solver's fast-forward
+ * kernel ran out -- ct_set_solver_fast_forward; reported as CT_ERR_TIMEOUT) */
 int ct_proj2d_errflag(void);
 int ct_proj3d_errflag(void);
 void ct_set_wait_poll_limit(uint32_t polls);
@@ -497,6 +499,25 @@ ct_status ct_admm_tv_solve_batch(const ct_admm_tv_desc* descs, int32_t n,
                                  void* const* workspace,
                                  const size_t* workspace_bytes,
                                  int32_t n_streams, ct_stream_t stream);
+
+/*
+ * Fast-forward CG start of the solve graphs (ct_admm_tv_solve and
+ * ct_admm_tv3d_solve with use_graph = 1; not the batch).  Once CG's
+ * stopping test passes at its first step, x stops moving and an iteration
+ * is only the z/u update, the next right-hand side and the CG start.  The
+ * CG start is then one cooperative launch that runs such iterations back
+ * to back, its blocks meeting at bounded grid barriers, and returns when CG
+ * has a step to run or the call's iterations are done.  Results are
+ * bit-identical with it on or off (same passes, same sums in the same
+ * order).  A barrier wait that runs out (poll limit: the smaller of
+ * ct_wait_poll_limit and 2^21) sets bit 3 of the device error word
+ * (ct_proj2d_check reports CT_ERR_TIMEOUT).  On by default unless the
+ * environment sets CTGPU_FFWD=0; used only where the device supports
+ * cooperative launches and the kernel's 304 blocks fit at once.  The setting
+ * is read when a solve graph is built (graphs are cached per setting).
+ */
+void ct_set_solver_fast_forward(int32_t on);
+int32_t ct_solver_fast_forward(void);
 
 /*
  * The same solver for 3D parallel-beam CT (XRayTransform3D,

@@ -197,6 +197,8 @@ _SIGNATURES = {
     "ct_proj2d_errflag": (ctypes.c_int, []),
     "ct_proj3d_errflag": (ctypes.c_int, []),
     "ct_set_wait_poll_limit": (None, [ctypes.c_uint32]),
+    "ct_set_solver_fast_forward": (None, [ctypes.c_int32]),
+    "ct_solver_fast_forward": (ctypes.c_int32, []),
     "ct_wait_poll_limit": (ctypes.c_uint32, []),
     "ct_proj2d_autotune": (ctypes.c_int, [P, c_int32, P, P, P, c_size_t, c_int32, P, P]),
     "ct_proj2d_schedule_get": (ctypes.c_int, [P, c_int32, P]),

@@ -43,9 +43,11 @@
 // next iteration's first projection of the same x (an epilogue covers the
 // last iteration).
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -67,6 +69,7 @@ enum Slot {
   S_REC = 6,      // records written in this call
   S_XCLEAN = 7,   // 1 while lhs(x) and A x in the workspace belong to the current x
   S_ITER = 8,     // ADMM iterations run in this call (the graph's device-side loop)
+  S_ZU_DONE = 9,  // 1: the fast-forward kernel ran the last iteration's z/u update
   S_CG = 16,      // CT_CG_NSCALARS doubles
   S_COUNT = 32
 };
@@ -84,6 +87,20 @@ struct TermParams {
 // slices, 3 for volumes.
 struct Shape3 {
   int n[3];
+};
+
+// Loads of the state arrays in the fused passes.  LdPlain: ordinary loads
+// (the separate kernels read only what earlier kernels wrote).  LdL2: loads
+// through L2 only (ld.global.cg) for the cooperative fast-forward kernel,
+// whose blocks read, after a grid barrier, elements that other blocks wrote
+// earlier in the same launch.  The arithmetic is the same either way.
+struct LdPlain {
+  static __device__ __forceinline__ float4 q(const float* p) { return *reinterpret_cast<const float4*>(p); }
+  static __device__ __forceinline__ float s(const float* p) { return *p; }
+};
+struct LdL2 {
+  static __device__ __forceinline__ float4 q(const float* p) { return __ldcg(reinterpret_cast<const float4*>(p)); }
+  static __device__ __forceinline__ float s(const float* p) { return __ldcg(p); }
 };
 
 template <int ND>
@@ -110,12 +127,12 @@ __device__ __forceinline__ size_t axis_stride(const Shape3& sh, int k) {
 // D^T applied at element e to a stacked (ND, *shape) field f = a - b (b may
 // be null): sum over axes of (f_k[e - st_k] - f_k[e]) with the append=0
 // boundaries, axes added in order (linop/_stack.py:71-72).
-template <int ND>
-__device__ __forceinline__ float dT_at(const float* __restrict__ a, const float* __restrict__ b,
-                                       const int (&c)[ND], size_t e, const Shape3& sh, size_t N) {
+template <int ND, class LD = LdPlain>
+__device__ __forceinline__ float dT_at(const float* a, const float* b, const int (&c)[ND], size_t e,
+                                       const Shape3& sh, size_t N) {
   auto f = [&](int comp, size_t idx) -> float {
-    const float av = a[comp * N + idx];
-    return b ? ct::fsub(av, b[comp * N + idx]) : av;
+    const float av = LD::s(a + comp * N + idx);
+    return b ? ct::fsub(av, LD::s(b + comp * N + idx)) : av;
   };
   float tot = 0.0f;
 #pragma unroll
@@ -180,22 +197,21 @@ __device__ __forceinline__ void unpack4(const float4 a, float (&v)[4]) {
 }
 
 // dT_at for the quad at e0 (coordinates c of e0).
-template <int ND>
-__device__ __forceinline__ void dT_at4(const float* __restrict__ a, const float* __restrict__ b,
-                                       const int (&c)[ND], size_t e0, const Shape3& sh, size_t N,
-                                       float (&tot)[4]) {
+template <int ND, class LD = LdPlain>
+__device__ __forceinline__ void dT_at4(const float* a, const float* b, const int (&c)[ND], size_t e0,
+                                       const Shape3& sh, size_t N, float (&tot)[4]) {
   auto f4 = [&](int comp, size_t idx, float (&v)[4]) {
-    unpack4(ld4(a + comp * N, idx), v);
+    unpack4(LD::q(a + comp * N + idx), v);
     if (b) {
       float w[4];
-      unpack4(ld4(b + comp * N, idx), w);
+      unpack4(LD::q(b + comp * N + idx), w);
 #pragma unroll
       for (int j = 0; j < 4; ++j) v[j] = ct::fsub(v[j], w[j]);
     }
   };
   auto f1 = [&](int comp, size_t idx) -> float {
-    const float av = a[comp * N + idx];
-    return b ? ct::fsub(av, b[comp * N + idx]) : av;
+    const float av = LD::s(a + comp * N + idx);
+    return b ? ct::fsub(av, LD::s(b + comp * N + idx)) : av;
   };
 #pragma unroll
   for (int k = 0; k < ND; ++k) {
@@ -357,31 +373,24 @@ __global__ void __launch_bounds__(NT) k_scale_splits(const float* __restrict__ s
   }
 }
 
-// In the solve graph (use_dirty != 0) k_rhs also sets the condition of the
-// iteration's projection node (a conditional IF node): run the projections of
-// x only when CG moved x since lhs(x) and A x were last computed.
-template <int ND>
-__global__ void __launch_bounds__(NT)
-    k_rhs(const float* __restrict__ atyc, const float* __restrict__ z, const float* __restrict__ u,
-          const float* __restrict__ dz, float* __restrict__ rhs, Shape3 sh, size_t N, TermParams tp,
-          double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
-          int vec, cudaGraphConditionalHandle dirty, int use_dirty) {
-  ct::grid_dep_wait();  // before any global access (dependent launch)
-  ct::grid_dep_trigger();
-  if (use_dirty && blockIdx.x == 0 && threadIdx.x == 0)
-    cudaGraphSetConditional(dirty, slots[S_XCLEAN] == 0.0 ? 1u : 0u);
+// k_rhs's pass over the elements: rhs = c A^T y + sum_i rho D^T (z_i - u_i)
+// and this thread's share of the dual residual ||sum_i rho D^T dz_i||^2.
+template <int ND, class LD>
+__device__ __forceinline__ ct::KSum rhs_pass(const float* atyc, const float* z, const float* u, const float* dz,
+                                            float* rhs, const Shape3& sh, size_t N, const TermParams& tp,
+                                            int vec) {
   ct::KSum ks;  // dual residual
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
       int c[ND];
       coords<ND>(e0, sh, c);
       float val[4], dv[4];
-      unpack4(ld4(atyc, e0), val);
+      unpack4(LD::q(atyc + e0), val);
       for (int t = 0; t < tp.ng; ++t) {
         const size_t o = (size_t)t * ND * N;
         float g[4], h[4];
-        dT_at4<ND>(z + o, u + o, c, e0, sh, N, g);
-        dT_at4<ND>(dz + o, nullptr, c, e0, sh, N, h);
+        dT_at4<ND, LD>(z + o, u + o, c, e0, sh, N, g);
+        dT_at4<ND, LD>(dz + o, nullptr, c, e0, sh, N, h);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           val[j] = ct::fadd(val[j], ct::fmul(tp.rho, g[j]));
@@ -397,18 +406,37 @@ __global__ void __launch_bounds__(NT)
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     int c[ND];
     coords<ND>(e, sh, c);
-    float val = atyc[e];
+    float val = LD::s(atyc + e);
     float dv = 0.0f;
     for (int t = 0; t < tp.ng; ++t) {
       const size_t o = (size_t)t * ND * N;
-      val = ct::fadd(val, ct::fmul(tp.rho, dT_at<ND>(z + o, u + o, c, e, sh, N)));
-      const float w = ct::fmul(tp.rho, dT_at<ND>(dz + o, nullptr, c, e, sh, N));
+      val = ct::fadd(val, ct::fmul(tp.rho, dT_at<ND, LD>(z + o, u + o, c, e, sh, N)));
+      const float w = ct::fmul(tp.rho, dT_at<ND, LD>(dz + o, nullptr, c, e, sh, N));
       dv = (t == 0) ? w : ct::fadd(dv, w);
     }
     rhs[e] = val;
     ks.add(ct::fmul(dv, dv));
   }
   }
+  return ks;
+}
+
+// In the solve graph (use_dirty != 0) k_rhs also sets the condition of the
+// iteration's projection node (a conditional IF node): run the projections of
+// x only when CG moved x since lhs(x) and A x were last computed.
+template <int ND>
+__global__ void __launch_bounds__(NT)
+    k_rhs(const float* __restrict__ atyc, const float* __restrict__ z, const float* __restrict__ u,
+          const float* __restrict__ dz, float* __restrict__ rhs, Shape3 sh, size_t N, TermParams tp,
+          double* __restrict__ slots, double* __restrict__ partials, unsigned int* __restrict__ ticket,
+          int vec, cudaGraphConditionalHandle dirty, int use_dirty, unsigned int* __restrict__ bar_reset) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (use_dirty) cudaGraphSetConditional(dirty, slots[S_XCLEAN] == 0.0 ? 1u : 0u);
+    if (bar_reset) *bar_reset = 0u;  // the grid barrier counter of this iteration's fast-forward kernel
+  }
+  ct::KSum ks = rhs_pass<ND, LdPlain>(atyc, z, u, dz, rhs, sh, N, tp, vec);
   double acc[1] = {ks.value()};
   double tot[1];
   if (ct::grid_sumk_last<NT, 1>(acc, partials, ticket, tot)) slots[S_DUAL2] = tot[0];
@@ -494,35 +522,22 @@ __global__ void k_itstat_final(RecParams rp, double* __restrict__ slots) {
   slots[S_HAVE_PREV] = 0.0;
 }
 
-// lhs(q) = sum_i rho D^T D q + c A^T A q, from the adjoint output (or its
-// view splits).  INIT (q = x): r = rhs - lhs(x), p = r and the CG start
-// scalars; lhs(x) is stored in lhsx, or read from it while x is unchanged
-// (slots[S_XCLEAN]); before the CG scalars are reset the last block writes
-// the previous iteration's itstat record.  PAP: Ap = lhs(q) and <q, Ap>.  In
-// a graph with a conditional CG loop, INIT sets the loop condition.
-template <int ND, bool INIT>
-__global__ void __launch_bounds__(NT)
-    k_lhs_finish(const float* __restrict__ adj, int nsplit, const float* __restrict__ q, Shape3 sh,
-                 size_t N, TermParams tp, float* __restrict__ out, const float* __restrict__ rhs,
-                 float* __restrict__ p, float* __restrict__ lhsx, double* __restrict__ slots,
-                 double* __restrict__ cg, double tol, double atol, int maxiter,
-                 double* __restrict__ partials, unsigned int* __restrict__ ticket,
-                 cudaGraphConditionalHandle cond, int use_cond, int vec, RecParams rp) {
-  ct::grid_dep_wait();  // before any global access (dependent launch)
-  ct::grid_dep_trigger();
-  if (!INIT && cg[CT_CG_DONE] != 0.0) return;
-  const bool cached = INIT && slots[S_XCLEAN] != 0.0;
-  double acc[2] = {0.0, 0.0};
+// k_lhs_finish's pass over the elements (see there); acc: this thread's
+// shares of ||r||^2, ||rhs||^2 (INIT) or <q, Ap> (acc[0]).
+template <int ND, bool INIT, class LD>
+__device__ __forceinline__ void lhs_pass(const float* adj, int nsplit, const float* q, const Shape3& sh, size_t N,
+                                         const TermParams& tp, float* out, const float* rhs, float* p, float* lhsx,
+                                         bool cached, int vec, double (&acc)[2]) {
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
       float v[4], qc[4];
-      if (!INIT || !cached) unpack4(ld4(q, e0), qc);
+      if (!INIT || !cached) unpack4(LD::q(q + e0), qc);
       if (cached) {
-        unpack4(ld4(lhsx, e0), v);
+        unpack4(LD::q(lhsx + e0), v);
       } else {
-        float4 a4 = ld4(adj, e0);
+        float4 a4 = LD::q(adj + e0);
         for (int k = 1; k < nsplit; ++k) {
-          const float4 w = ld4(adj + (size_t)k * N, e0);
+          const float4 w = LD::q(adj + (size_t)k * N + e0);
           a4 = make_float4(ct::fadd(a4.x, w.x), ct::fadd(a4.y, w.y), ct::fadd(a4.z, w.z), ct::fadd(a4.w, w.w));
         }
         float a[4];
@@ -541,7 +556,7 @@ __global__ void __launch_bounds__(NT)
       }
       if (INIT) {
         float b[4], re[4];
-        unpack4(ld4(rhs, e0), b);
+        unpack4(LD::q(rhs + e0), b);
 #pragma unroll
         for (int j = 0; j < 4; ++j) re[j] = ct::fsub(b[j], v[j]);
         st4(out, e0, re);  // r
@@ -561,10 +576,10 @@ __global__ void __launch_bounds__(NT)
   for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
     float v;
     if (cached) {
-      v = lhsx[e];
+      v = LD::s(lhsx + e);
     } else {
-      float a = adj[e];
-      for (int k = 1; k < nsplit; ++k) a = ct::fadd(a, adj[(size_t)k * N + e]);
+      float a = LD::s(adj + e);
+      for (int k = 1; k < nsplit; ++k) a = ct::fadd(a, LD::s(adj + (size_t)k * N + e));
       int c[ND];
       coords<ND>(e, sh, c);
       const float g = dtd_at<ND>(q, c, e, sh);
@@ -574,7 +589,7 @@ __global__ void __launch_bounds__(NT)
       if (INIT) lhsx[e] = v;
     }
     if (INIT) {
-      const float b = rhs[e];
+      const float b = LD::s(rhs + e);
       const float re = ct::fsub(b, v);
       out[e] = re;  // r
       p[e] = re;
@@ -582,10 +597,32 @@ __global__ void __launch_bounds__(NT)
       acc[1] += (double)b * (double)b;
     } else {
       out[e] = v;  // Ap
-      acc[0] += (double)q[e] * (double)v;
+      acc[0] += (double)LD::s(q + e) * (double)v;
     }
   }
   }
+}
+
+// lhs(q) = sum_i rho D^T D q + c A^T A q, from the adjoint output (or its
+// view splits).  INIT (q = x): r = rhs - lhs(x), p = r and the CG start
+// scalars; lhs(x) is stored in lhsx, or read from it while x is unchanged
+// (slots[S_XCLEAN]); before the CG scalars are reset the last block writes
+// the previous iteration's itstat record.  PAP: Ap = lhs(q) and <q, Ap>.  In
+// a graph with a conditional CG loop, INIT sets the loop condition.
+template <int ND, bool INIT>
+__global__ void __launch_bounds__(NT)
+    k_lhs_finish(const float* __restrict__ adj, int nsplit, const float* __restrict__ q, Shape3 sh,
+                 size_t N, TermParams tp, float* __restrict__ out, const float* __restrict__ rhs,
+                 float* __restrict__ p, float* __restrict__ lhsx, double* __restrict__ slots,
+                 double* __restrict__ cg, double tol, double atol, int maxiter,
+                 double* __restrict__ partials, unsigned int* __restrict__ ticket,
+                 cudaGraphConditionalHandle cond, int use_cond, int vec, RecParams rp) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
+  if (!INIT && cg[CT_CG_DONE] != 0.0) return;
+  const bool cached = INIT && slots[S_XCLEAN] != 0.0;
+  double acc[2] = {0.0, 0.0};
+  lhs_pass<ND, INIT, LdPlain>(adj, nsplit, q, sh, N, tp, out, rhs, p, lhsx, cached, vec, acc);
   double tot[2];
   if (ct::grid_sumk_last<NT, 2>(acc, partials, ticket, tot)) {
     if (INIT) {
@@ -637,22 +674,21 @@ __device__ __forceinline__ void prox_nd(int kind, float thr, const float (&v)[ND
 }
 
 // z/u update of one element from its differences d (k_zu's body).
-template <int ND>
-__device__ __forceinline__ void zu_el(const float (&d)[ND], float* __restrict__ z, float* __restrict__ u,
-                                      float* __restrict__ dz, size_t e, size_t N, const TermParams& tp,
-                                      ct::KSum (&acc)[3]) {
+template <int ND, class LD = LdPlain>
+__device__ __forceinline__ void zu_el(const float (&d)[ND], float* z, float* u, float* dz, size_t e, size_t N,
+                                      const TermParams& tp, ct::KSum (&acc)[3]) {
   for (int t = 0; t < tp.ng; ++t) {
     const size_t o = (size_t)t * ND * N;
     float zo[ND], v[ND], zn[ND];
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
-      zo[k] = z[o + k * N + e];
+      zo[k] = LD::s(z + o + k * N + e);
       float ck = d[k];
       if (tp.alpha != 1.0f) {
         const float om = ct::fsub(1.0f, tp.alpha);
         ck = ct::fadd(ct::fmul(tp.alpha, d[k]), ct::fmul(om, zo[k]));
       }
-      v[k] = ct::fadd(ck, u[o + k * N + e]);
+      v[k] = ct::fadd(ck, LD::s(u + o + k * N + e));
     }
     prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
     float pr = 0.0f;
@@ -681,17 +717,16 @@ __device__ __forceinline__ void zu_el(const float (&d)[ND], float* __restrict__ 
 
 // z/u update of the quad at e0: the state arrays move in 128-bit loads and
 // stores, the arithmetic is zu_el's per element, elements in order.
-template <int ND>
-__device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* __restrict__ z, float* __restrict__ u,
-                                        float* __restrict__ dz, size_t e0, size_t N, const TermParams& tp,
-                                        ct::KSum (&acc)[3]) {
+template <int ND, class LD = LdPlain>
+__device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* z, float* u, float* dz, size_t e0,
+                                        size_t N, const TermParams& tp, ct::KSum (&acc)[3]) {
   for (int t = 0; t < tp.ng; ++t) {
     const size_t o = (size_t)t * ND * N;
     float zo[ND][4], uo[ND][4];
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
-      unpack4(ld4(z + o + k * N, e0), zo[k]);
-      unpack4(ld4(u + o + k * N, e0), uo[k]);
+      unpack4(LD::q(z + o + k * N + e0), zo[k]);
+      unpack4(LD::q(u + o + k * N + e0), uo[k]);
     }
     float zn4[ND][4], un4[ND][4], dz4[ND][4];
 #pragma unroll
@@ -738,6 +773,32 @@ __device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* __restri
   }
 }
 
+// k_zu's pass over the elements: z, u (and dz = z - z_old) of every term
+// from D x; ks: this thread's shares of the primal residual and the g norms.
+// x is not written while the pass runs.
+template <int ND, class LD>
+__device__ __forceinline__ void zu_pass(const float* __restrict__ x, float* z, float* u, float* dz, const Shape3& sh,
+                                        size_t N, const TermParams& tp, int vec, ct::KSum (&ks)[3]) {
+  if (vec) {
+    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e0, sh, c);
+      float xc[4], d[ND][4];
+      unpack4(ld4(x, e0), xc);
+      d_at4<ND>(x, xc, c, e0, sh, d);
+      zu_quad<ND, LD>(d, z, u, dz, e0, N, tp, ks);
+    }
+  } else {
+    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
+      int c[ND];
+      coords<ND>(e, sh, c);
+      float d[ND];
+      d_at<ND>(x, c, e, sh, d);
+      zu_el<ND, LD>(d, z, u, dz, e, N, tp, ks);
+    }
+  }
+}
+
 // In the solve graph (use_loop != 0) the last block also ends the iteration:
 // it counts it and keeps the graph's iteration loop (a conditional WHILE
 // node) running while fewer than maxiter iterations have run.
@@ -749,25 +810,12 @@ __global__ void __launch_bounds__(NT)
          int maxiter) {
   ct::grid_dep_wait();  // before any global access (dependent launch)
   ct::grid_dep_trigger();
-  ct::KSum ks[3];  // primal, g21, g1
-  if (vec) {
-    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
-      int c[ND];
-      coords<ND>(e0, sh, c);
-      float xc[4], d[ND][4];
-      unpack4(ld4(x, e0), xc);
-      d_at4<ND>(x, xc, c, e0, sh, d);
-      zu_quad<ND>(d, z, u, dz, e0, N, tp, ks);
-    }
-  } else {
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
-      int c[ND];
-      coords<ND>(e, sh, c);
-      float d[ND];
-      d_at<ND>(x, c, e, sh, d);
-      zu_el<ND>(d, z, u, dz, e, N, tp, ks);
-    }
+  if (slots[S_ZU_DONE] != 0.0) {  // uniform: the iterations of this call are complete
+    if (use_loop && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(loop, 0u);
+    return;
   }
+  ct::KSum ks[3];  // primal, g21, g1
+  zu_pass<ND, LdPlain>(x, z, u, dz, sh, N, tp, vec, ks);
   double acc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
   double tot[3];
   if (ct::grid_sumk_last<NT, 3>(acc, partials, ticket, tot)) {
@@ -791,6 +839,115 @@ __global__ void k_reset_call(double* __restrict__ slots) {
   slots[S_HAVE_PREV] = 0.0;
   slots[S_XCLEAN] = 0.0;  // the caller may have changed x between calls
   slots[S_ITER] = 0.0;
+  slots[S_ZU_DONE] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Fast-forward CG start.  At C2 the CG stopping test passes at the first
+// step from about the 12th iteration on: x stops moving and each remaining
+// iteration is only the z/u update, the next right-hand side and the CG
+// start -- three reducing passes of microseconds each, which as separate
+// graph nodes cost more in launches and reduction tails than in work.
+// k_init_ffwd replaces k_lhs_finish<INIT> in the solve graph: a cooperative
+// launch (every block resident) that does the CG start and, for as long as
+// CG would run no step, the iteration's z/u update, the next rhs and the
+// next CG start in the same launch, the blocks meeting at bounded grid
+// barriers.  Each pass is the separate kernel's own pass (the same per-
+// thread elements, the same per-block partials, the same partial sums in
+// the same order), so the iterates, the CG step counts and the itstat
+// records are bit-identical to the separate kernels'.  It returns when CG
+// has a step to run (the CG loop's condition set) or when the call's last
+// iteration is done (S_ZU_DONE: the z/u kernel that follows in the graph
+// then only ends the loop).
+// ---------------------------------------------------------------------------
+constexpr int kErrBarrier = 8;  // projector error-word bit: a grid barrier wait ran out
+// Partials of the fast-forward kernel (doubles, per block): CG start (2
+// sums), dual residual (1), z/u statistics (3).
+constexpr int kFfInit = 0, kFfDual = 2 * NB, kFfZu = 3 * NB, kFfDoubles = 6 * NB;
+
+template <int ND>
+__global__ void __launch_bounds__(NT, 2)
+    k_init_ffwd(const float* adj, int nsplit, const float* __restrict__ x, Shape3 sh, size_t N, TermParams tp,
+                float* r, float* rhs, float* p, float* lhsx, const float* __restrict__ atyc, float* z, float* u,
+                float* dz, double* slots, double* cg, double tol, double atol, int cg_maxiter, int maxiter,
+                double* fpart, unsigned int* bar, cudaGraphConditionalHandle cond, int vec, RecParams rp,
+                uint32_t max_polls, int* errflag) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
+  __shared__ double dec_s[2];
+  // read by every block before the first barrier; block 0 writes both only after it
+  bool cached = slots[S_XCLEAN] != 0.0;
+  int iter = (int)slots[S_ITER];
+  bool have_dual = false;  // dual-residual partials of a rhs pass of this launch are pending
+  unsigned int nbar = 0;
+  for (;;) {
+    // ---- CG start of iteration `iter` (k_lhs_finish<INIT>)
+    double acc[2] = {0.0, 0.0};
+    lhs_pass<ND, true, LdL2>(adj, nsplit, x, sh, N, tp, r, rhs, p, lhsx, cached, vec, acc);
+    ct::block_partials<NT, 2>(acc, fpart + kFfInit);
+    if (!ct::grid_barrier(bar, ++nbar * gridDim.x, max_polls, errflag, kErrBarrier)) return;
+    double tot[2];
+    ct::sum_partials<NT, 2>(fpart + kFfInit, gridDim.x, tot);
+    if (threadIdx.x == 0) {
+      dec_s[0] = tot[0];
+      dec_s[1] = tot[1];
+    }
+    __syncthreads();
+    const double bn = sqrt(dec_s[1]);
+    const double thr = fmax(tol * bn, atol);
+    const bool done = cg_maxiter <= 0 || !(dec_s[0] > thr * thr);
+    if (blockIdx.x == 0) {
+      if (have_dual) {  // k_rhs's total, before the record that reads it
+        double d[1];
+        ct::sum_partials<NT, 1>(fpart + kFfDual, gridDim.x, d);
+        if (threadIdx.x == 0) slots[S_DUAL2] = d[0];
+      }
+      if (threadIdx.x == 0) {
+        write_record(rp, slots);
+        cg[CT_CG_NUM] = dec_s[0];
+        cg[CT_CG_PAP] = 0.0;
+        cg[CT_CG_ALPHA] = 0.0;
+        cg[CT_CG_BETA] = 0.0;
+        cg[CT_CG_BNORM] = bn;
+        cg[CT_CG_TOL2] = thr * thr;
+        cg[CT_CG_ITERS] = 0.0;
+        cg[CT_CG_MAXITER] = (double)cg_maxiter;
+        cg[CT_CG_RAN] = 0.0;
+        cg[CT_CG_DONE] = done ? 1.0 : 0.0;
+        slots[S_XCLEAN] = 1.0;
+        if (!done) cudaGraphSetConditional(cond, 1u);
+      }
+    }
+    if (!done) return;  // uniform: CG runs this iteration's steps in the graph
+    cached = true;
+    // ---- z/u update of iteration `iter`, x unchanged (k_zu)
+    ct::KSum ks[3];
+    zu_pass<ND, LdL2>(x, z, u, dz, sh, N, tp, vec, ks);
+    double zacc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
+    ct::block_partials<NT, 3>(zacc, fpart + kFfZu);
+    if (!ct::grid_barrier(bar, ++nbar * gridDim.x, max_polls, errflag, kErrBarrier)) return;
+    ++iter;
+    if (blockIdx.x == 0) {
+      double zt[3];
+      ct::sum_partials<NT, 3>(fpart + kFfZu, gridDim.x, zt);
+      if (threadIdx.x == 0) {
+        slots[S_PRIMAL2] = zt[0];
+        slots[S_G21] = zt[1];
+        slots[S_G1] = zt[2];
+        slots[S_HAVE_PREV] = 1.0;
+        slots[S_ITER] = (double)iter;
+        if (iter >= maxiter) slots[S_ZU_DONE] = 1.0;
+      }
+    }
+    if (iter >= maxiter) return;
+    // ---- rhs of the next iteration (k_rhs): reads the neighbours' z and u,
+    // which the barrier above made visible; its CG start follows in the same
+    // threads (rhs at their own elements)
+    ct::KSum kd = rhs_pass<ND, LdL2>(atyc, z, u, dz, rhs, sh, N, tp, vec);
+    double dacc[1] = {kd.value()};
+    ct::block_partials<NT, 1>(dacc, fpart + kFfDual);
+    have_dual = true;
+  }
 }
 
 
@@ -883,7 +1040,7 @@ Problem problem_of(const ct_admm_tv3d_desc* d) {
 struct Layout {
   int ng;
   size_t off_slots, off_red, off_atyc, off_rhs, off_r, off_p, off_ap, off_adj, off_sino, off_z, off_u,
-      off_dz, off_fwd, off_adjpart, off_lhsx, off_sinox, total;
+      off_dz, off_fwd, off_adjpart, off_lhsx, off_sinox, off_ff, total;
 };
 
 Layout layout(const Problem& P) {
@@ -912,6 +1069,7 @@ Layout layout(const Problem& P) {
   L.off_adjpart = take(P.proj.adj_ws_bytes() > 0 ? P.proj.adj_ws_bytes() : 256);
   L.off_lhsx = take(P.N * 4);
   L.off_sinox = take(P.S * 4);
+  L.off_ff = take(256 + sizeof(double) * kFfDoubles);  // barrier counter, then the partials
   L.total = o;
   return L;
 }
@@ -955,6 +1113,9 @@ struct Ctx {
   double* cg() const { return slots() + S_CG; }
   unsigned int* ticket() const { return at<unsigned int>(L.off_red); }
   double* partials() const { return reinterpret_cast<double*>(ws + L.off_red + 256); }
+  unsigned int* ff_bar() const { return at<unsigned int>(L.off_ff); }
+  double* ff_part() const { return reinterpret_cast<double*>(ws + L.off_ff + 256); }
+  bool ffwd = false;  // the solve graph's CG start is k_init_ffwd
 };
 
 #define CT_TRY(expr)                 \
@@ -1007,7 +1168,8 @@ ct_status enqueue_rhs(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle d
   return ct::cuda_check(ct::launch_k(k, dim3(NB), dim3(NT), 0, s, true, (const float*)c.at<float>(c.L.off_atyc),
                                      (const float*)c.at<float>(c.L.off_z), (const float*)c.at<float>(c.L.off_u),
                                      (const float*)c.at<float>(c.L.off_dz), c.at<float>(c.L.off_rhs), c.P.sh, c.P.N,
-                                     c.tp, c.slots(), c.partials(), c.ticket(), c.vi, dirty, use_dirty),
+                                     c.tp, c.slots(), c.partials(), c.ticket(), c.vi, dirty, use_dirty,
+                                     (c.ffwd && use_dirty) ? c.ff_bar() : (unsigned int*)nullptr),
                         "k_rhs");
 }
 
@@ -1030,6 +1192,29 @@ ct_status enqueue_init(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle 
   float* r = c.at<float>(c.L.off_r);
   float* p = c.at<float>(c.L.off_p);
   float* rhs = c.at<float>(c.L.off_rhs);
+  if (c.ffwd && use_cond) {
+    // the fast-forward CG start: a cooperative launch (all NB blocks resident)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(NB);
+    cfg.blockDim = dim3(NT);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const uint32_t polls = std::min<uint32_t>(ct::proj2d_wait_polls(), 1u << 21);
+    int* err = ct::proj2d_errflag_ptr();
+    if (!err) return ct::fail(CT_ERR_CUDA, "k_init_ffwd: error-word address unavailable");
+    auto kf = c.P.nd == 2 ? k_init_ffwd<2> : k_init_ffwd<3>;
+    return ct::cuda_check(
+        cudaLaunchKernelEx(&cfg, kf, adj, c.P.proj.nsplit(), (const float*)c.x, c.P.sh, N, c.tp, r, rhs, p,
+                           c.at<float>(c.L.off_lhsx), (const float*)c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
+                           c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.slots(), c.cg(), c.P.prm.cg_tol,
+                           c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.P.prm.maxiter, c.ff_part(), c.ff_bar(), cond, c.vi,
+                           rec_params(c), polls, err),
+        "k_init_ffwd");
+  }
   auto k = c.P.nd == 2 ? k_lhs_finish<2, true> : k_lhs_finish<3, true>;
   return ct::cuda_check(ct::launch_k(k, dim3(NB), dim3(NT), 0, s, true, adj, c.P.proj.nsplit(), (const float*)c.x,
                                      c.P.sh, N, c.tp, r, (const float*)rhs, p, c.at<float>(c.L.off_lhsx), c.slots(),
@@ -1093,6 +1278,35 @@ ct_status enqueue_epilogue(const Ctx& c, cudaStream_t s) {
                         "k_itstat_final");
 }
 
+// The fast-forward CG start (k_init_ffwd): on unless CTGPU_FFWD=0 or
+// ct_set_solver_fast_forward(0); used where the device runs cooperative
+// launches and all NB blocks of it fit at once.
+std::atomic<int> g_ffwd{-1};
+
+bool ffwd_enabled() {
+  int v = g_ffwd.load(std::memory_order_relaxed);
+  if (v < 0) {
+    const char* e = getenv("CTGPU_FFWD");
+    v = (e && e[0] == '0') ? 0 : 1;
+    g_ffwd.store(v, std::memory_order_relaxed);
+  }
+  return v != 0;
+}
+
+bool ffwd_usable(int nd) {
+  if (!ffwd_enabled()) return false;
+  int dev = 0, coop = 0, nb = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
+  const cudaError_t e = nd == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_init_ffwd<2>, NT, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_init_ffwd<3>, NT, 0);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return nb * ct::sm_count() >= NB;
+}
+
 // Executable iteration graphs, one per problem (key: dimension, descriptor
 // bytes and the state/data pointers), least recently used evicted.  One
 // capture stream per device; graphs are launched on the solve's stream.
@@ -1122,12 +1336,14 @@ void make_key(const Ctx& c, int32_t iter0, std::vector<unsigned char>& key) {
   put(&c.P.nd, sizeof(c.P.nd));
   put(&fresh, sizeof(fresh));
   put(c.P.desc, c.P.desc_size);
-  if (c.P.nd == 2) {  // the projector's schedule (the autotuner may record a new one) and wait limit
+  if (c.P.nd == 2) {  // the projector's schedule (the autotuner may record a new one)
     put(&c.P.proj.p2.vpc, sizeof(int));
     put(&c.P.proj.p2.nsplit, sizeof(int));
-    const uint32_t polls = ct::proj2d_wait_polls();
-    put(&polls, sizeof(polls));
   }
+  const uint32_t polls = ct::proj2d_wait_polls();  // the wait limits captured in the graph
+  put(&polls, sizeof(polls));
+  const int ff = c.ffwd ? 1 : 0;
+  put(&ff, sizeof(ff));
   put(&c.ws, sizeof(c.ws));
   put(&c.y, sizeof(c.y));
   put(&c.x, sizeof(c.x));
@@ -1239,10 +1455,14 @@ ct_status graph_for(const Ctx* cs, int n, int32_t iter0, cudaGraphExec_t& exec) 
   if (!g_cache.capture[dev])
     CT_TRY(ct::cuda_check(cudaStreamCreateWithFlags(&g_cache.capture[dev], cudaStreamNonBlocking),
                           "capture stream"));
+  // the fast-forward CG start only in a single solve's graph: cooperative
+  // kernels of concurrent branches could not all be resident at once
+  std::vector<Ctx> cx(cs, cs + n);
+  for (Ctx& c : cx) c.ffwd = n == 1 && ffwd_usable(c.P.nd);
   std::vector<unsigned char> key;
   key.insert(key.end(), reinterpret_cast<const unsigned char*>(&n),
              reinterpret_cast<const unsigned char*>(&n) + sizeof(n));
-  for (int k = 0; k < n; ++k) make_key(cs[k], iter0, key);
+  for (int k = 0; k < n; ++k) make_key(cx[k], iter0, key);
   GraphEntry* slot = nullptr;
   for (GraphEntry& e : g_cache.e) {
     if (e.exec && e.device == dev && e.key == key) {
@@ -1259,7 +1479,7 @@ ct_status graph_for(const Ctx* cs, int n, int32_t iter0, cudaGraphExec_t& exec) 
   cudaGraph_t graph = nullptr;
   CT_TRY(ct::cuda_check(cudaGraphCreate(&graph, 0), "graph create"));
   ct_status st = CT_OK;
-  for (int k = 0; k < n && st == CT_OK; ++k) st = append_solve(cs[k], iter0, g_cache.capture[dev], graph);
+  for (int k = 0; k < n && st == CT_OK; ++k) st = append_solve(cx[k], iter0, g_cache.capture[dev], graph);
   if (st != CT_OK) {
     cudaGraphDestroy(graph);
     return st;
@@ -1395,6 +1615,10 @@ ct_status state_of(const D* d, const char* who, size_t* z_offset, size_t* u_offs
 }  // namespace
 
 extern "C" {
+
+void ct_set_solver_fast_forward(int32_t on) { g_ffwd.store(on ? 1 : 0, std::memory_order_relaxed); }
+
+int32_t ct_solver_fast_forward(void) { return ffwd_enabled() ? 1 : 0; }
 
 ct_status ct_admm_tv_workspace(const ct_admm_tv_desc* d, size_t* bytes) {
   return workspace_of(d, "ct_admm_tv_workspace", bytes);

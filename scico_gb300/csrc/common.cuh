@@ -161,15 +161,42 @@ __device__ __forceinline__ void block_reduce(double (&v)[K], double (*red)[NT / 
   __syncthreads();
 }
 
+// The two halves of the grid reduction.  block_partials: the block's K
+// partials (thread 0 writes them).  sum_partials: the K totals over the
+// grid's partials, summed with all threads of one block in a fixed pattern;
+// valid in thread 0.  The partials are read through L2 (other blocks wrote
+// them).
 template <int NT, int K>
-__device__ __forceinline__ bool grid_reduce_last(double (&v)[K], double* partials, unsigned int* ticket,
-                                                 double (&out)[K]) {
+__device__ __forceinline__ void block_partials(double (&v)[K], double* partials) {
   __shared__ double red[K][NT / 32];
-  __shared__ bool is_last;
   block_reduce<NT, K>(v, red);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) partials[(size_t)K * blockIdx.x + k] = v[k];
+  }
+}
+
+template <int NT, int K>
+__device__ __forceinline__ void sum_partials(const double* partials, unsigned int nblocks, double (&out)[K]) {
+  __shared__ double red[K][NT / 32];
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (unsigned int b = threadIdx.x; b < nblocks; b += NT) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] += __ldcg(partials + (size_t)K * b + k);
+  }
+  block_reduce<NT, K>(acc, red);
+#pragma unroll
+  for (int k = 0; k < K; ++k) out[k] = acc[k];
+}
+
+template <int NT, int K>
+__device__ __forceinline__ bool grid_reduce_last(double (&v)[K], double* partials, unsigned int* ticket,
+                                                 double (&out)[K]) {
+  __shared__ bool is_last;
+  block_partials<NT, K>(v, partials);
+  if (threadIdx.x == 0) {
     __threadfence();
     is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
   }
@@ -177,18 +204,46 @@ __device__ __forceinline__ bool grid_reduce_last(double (&v)[K], double* partial
   if (!is_last) return false;
   __threadfence();
   double acc[K];
-#pragma unroll
-  for (int k = 0; k < K; ++k) acc[k] = 0.0;
-  for (unsigned int b = threadIdx.x; b < gridDim.x; b += NT) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] += __ldcg(partials + (size_t)K * b + k);
-  }
-  block_reduce<NT, K>(acc, red);
+  sum_partials<NT, K>(partials, gridDim.x, acc);
   if (threadIdx.x != 0) return false;
 #pragma unroll
   for (int k = 0; k < K; ++k) out[k] = acc[k];
   *ticket = 0u;
   return true;
+}
+
+// Grid barrier of a cooperative launch (all blocks resident).  `count` is a
+// counter that only grows during the launch (reset to 0 before it); the
+// k-th barrier of the launch waits until it reaches k * gridDim.x.  The wait
+// is bounded: after max_polls polls the block sets bit `err_bit` of *err and
+// the barrier returns false, so a block that is never joined ends instead of
+// hanging (the launch's results are then void and reported).
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, uint32_t max_polls, int* err,
+                                             int err_bit) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+    uint32_t polls = 0;
+    while (ld_acquire_gpu(count) < target) {
+      if (++polls > max_polls) {
+        ok = 0;
+        atomicOr(err, err_bit);
+        break;
+      }
+    }
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
 }
 
 // Fixed grid size for reductions (independent of the device, so results are

@@ -30,6 +30,8 @@ Proj2dPlan proj2d_plan(const ct_geom2d* g, int batch);  // recorded schedule, el
 Proj2dPlan proj2d_plan_sched(const ct_geom2d* g, int batch, Sched2d s);
 // Current poll limit of the forward's strip-copy wait (ct_set_wait_poll_limit).
 uint32_t proj2d_wait_polls();
+// Device address of the library's device error word (ct_proj2d_check).
+int* proj2d_errflag_ptr();
 // out[e] = sum over the adjoint's view splits (in split order) of part[k n + e].
 ct_status proj2d_sum_splits(const float* part, float* out, size_t n, int nsplit, cudaStream_t s);
 // One-time per-process function attributes (large dynamic shared memory);

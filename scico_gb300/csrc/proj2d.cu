@@ -755,8 +755,9 @@ __global__ void k_sum_splits(const float* __restrict__ part, float* __restrict__
   }
 }
 
-// Device error word of the projector's internal checks (bit 0: forward tile
-// span, bit 1: strip copy wait, bit 2: adjoint window span).
+// Device error word of the library's device checks (bit 0: forward tile
+// span, bit 1: strip copy wait, bit 2: adjoint window span, bit 3: a grid
+// barrier wait of the solver's fast-forward kernel).
 __device__ int g_proj2d_err = 0;
 
 int* errflag_ptr() {
@@ -823,6 +824,8 @@ size_t adj_smem_bytes(int W) {
 #include "kernels.cuh"
 
 namespace ct {
+
+int* proj2d_errflag_ptr() { return errflag_ptr(); }
 
 ct_status proj2d_check(const ct_geom2d* g, const char* who) {
   if (!g) return fail(CT_ERR_INVALID_ARG, "%s: null geometry", who);
@@ -1274,6 +1277,9 @@ ct_status ct_proj2d_check(ct_stream_t stream) {
   const int zero = 0;
   st = ct::cuda_check(cudaMemcpyToSymbol(g_proj2d_err, &zero, sizeof(int)), "ct_proj2d_check: clear");
   if (st != CT_OK) return st;
+  if (v & 8)
+    return ct::fail(CT_ERR_TIMEOUT, "ct_proj2d_check: a solver grid barrier wait ran out (error word 0x%x); "
+                    "the solve's results are void", v);
   if (v & 2)
     return ct::fail(CT_ERR_TIMEOUT, "ct_proj2d_check: a forward strip copy wait ran out (error word 0x%x); "
                     "the CTAs concerned skipped their work and wrote zeros", v);
