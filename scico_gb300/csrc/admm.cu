@@ -674,21 +674,23 @@ __device__ __forceinline__ void prox_nd(int kind, float thr, const float (&v)[ND
 }
 
 // z/u update of one element from its differences d (k_zu's body).
+// zi, ui: the state read; z, u, dz: where the new state goes (the same
+// arrays for the in-place update).
 template <int ND, class LD = LdPlain>
-__device__ __forceinline__ void zu_el(const float (&d)[ND], float* z, float* u, float* dz, size_t e, size_t N,
-                                      const TermParams& tp, ct::KSum (&acc)[3]) {
+__device__ __forceinline__ void zu_el(const float (&d)[ND], const float* zi, const float* ui, float* z, float* u,
+                                      float* dz, size_t e, size_t N, const TermParams& tp, ct::KSum (&acc)[3]) {
   for (int t = 0; t < tp.ng; ++t) {
     const size_t o = (size_t)t * ND * N;
     float zo[ND], v[ND], zn[ND];
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
-      zo[k] = LD::s(z + o + k * N + e);
+      zo[k] = LD::s(zi + o + k * N + e);
       float ck = d[k];
       if (tp.alpha != 1.0f) {
         const float om = ct::fsub(1.0f, tp.alpha);
         ck = ct::fadd(ct::fmul(tp.alpha, d[k]), ct::fmul(om, zo[k]));
       }
-      v[k] = ct::fadd(ck, LD::s(u + o + k * N + e));
+      v[k] = ct::fadd(ck, LD::s(ui + o + k * N + e));
     }
     prox_nd<ND>(tp.kind[t], tp.thr[t], v, zn);
     float pr = 0.0f;
@@ -718,15 +720,16 @@ __device__ __forceinline__ void zu_el(const float (&d)[ND], float* z, float* u, 
 // z/u update of the quad at e0: the state arrays move in 128-bit loads and
 // stores, the arithmetic is zu_el's per element, elements in order.
 template <int ND, class LD = LdPlain>
-__device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* z, float* u, float* dz, size_t e0,
-                                        size_t N, const TermParams& tp, ct::KSum (&acc)[3]) {
+__device__ __forceinline__ void zu_quad(const float (&d)[ND][4], const float* zi, const float* ui, float* z,
+                                        float* u, float* dz, size_t e0, size_t N, const TermParams& tp,
+                                        ct::KSum (&acc)[3]) {
   for (int t = 0; t < tp.ng; ++t) {
     const size_t o = (size_t)t * ND * N;
     float zo[ND][4], uo[ND][4];
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
-      unpack4(LD::q(z + o + k * N + e0), zo[k]);
-      unpack4(LD::q(u + o + k * N + e0), uo[k]);
+      unpack4(LD::q(zi + o + k * N + e0), zo[k]);
+      unpack4(LD::q(ui + o + k * N + e0), uo[k]);
     }
     float zn4[ND][4], un4[ND][4], dz4[ND][4];
 #pragma unroll
@@ -777,8 +780,9 @@ __device__ __forceinline__ void zu_quad(const float (&d)[ND][4], float* z, float
 // from D x; ks: this thread's shares of the primal residual and the g norms.
 // x is not written while the pass runs.
 template <int ND, class LD>
-__device__ __forceinline__ void zu_pass(const float* __restrict__ x, float* z, float* u, float* dz, const Shape3& sh,
-                                        size_t N, const TermParams& tp, int vec, ct::KSum (&ks)[3]) {
+__device__ __forceinline__ void zu_pass(const float* __restrict__ x, const float* zi, const float* ui, float* z,
+                                        float* u, float* dz, const Shape3& sh, size_t N, const TermParams& tp,
+                                        int vec, ct::KSum (&ks)[3]) {
   if (vec) {
     for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT) {
       int c[ND];
@@ -786,7 +790,7 @@ __device__ __forceinline__ void zu_pass(const float* __restrict__ x, float* z, f
       float xc[4], d[ND][4];
       unpack4(ld4(x, e0), xc);
       d_at4<ND>(x, xc, c, e0, sh, d);
-      zu_quad<ND, LD>(d, z, u, dz, e0, N, tp, ks);
+      zu_quad<ND, LD>(d, zi, ui, z, u, dz, e0, N, tp, ks);
     }
   } else {
     for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT) {
@@ -794,7 +798,7 @@ __device__ __forceinline__ void zu_pass(const float* __restrict__ x, float* z, f
       coords<ND>(e, sh, c);
       float d[ND];
       d_at<ND>(x, c, e, sh, d);
-      zu_el<ND, LD>(d, z, u, dz, e, N, tp, ks);
+      zu_el<ND, LD>(d, zi, ui, z, u, dz, e, N, tp, ks);
     }
   }
 }
@@ -815,7 +819,7 @@ __global__ void __launch_bounds__(NT)
     return;
   }
   ct::KSum ks[3];  // primal, g21, g1
-  zu_pass<ND, LdPlain>(x, z, u, dz, sh, N, tp, vec, ks);
+  zu_pass<ND, LdPlain>(x, z, u, z, u, dz, sh, N, tp, vec, ks);
   double acc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
   double tot[3];
   if (ct::grid_sumk_last<NT, 3>(acc, partials, ticket, tot)) {
@@ -849,45 +853,89 @@ __global__ void k_reset_call(double* __restrict__ slots) {
 // start -- three reducing passes of microseconds each, which as separate
 // graph nodes cost more in launches and reduction tails than in work.
 // k_init_ffwd replaces k_lhs_finish<INIT> in the solve graph: a cooperative
-// launch (every block resident) that does the CG start and, for as long as
-// CG would run no step, the iteration's z/u update, the next rhs and the
-// next CG start in the same launch, the blocks meeting at bounded grid
-// barriers.  Each pass is the separate kernel's own pass (the same per-
-// thread elements, the same per-block partials, the same partial sums in
-// the same order), so the iterates, the CG step counts and the itstat
-// records are bit-identical to the separate kernels'.  It returns when CG
-// has a step to run (the CG loop's condition set) or when the call's last
-// iteration is done (S_ZU_DONE: the z/u kernel that follows in the graph
-// then only ends the loop).
+// launch (every block resident) that runs the CG start and, for as long as
+// CG would run no step, the following iterations, one grid barrier per
+// iteration.  In one phase each thread computes, for its own elements, the
+// iteration's rhs (from the neighbours' z, u, dz, made visible by the last
+// barrier), the CG start, and the z/u update speculatively into the other
+// of two state buffers; after the barrier every block reads the CG start's
+// sums: if CG has a step to run, the speculative update is dropped and the
+// kernel returns (the CG loop's condition set); otherwise it is committed
+// (its statistics written) and the next phase reads the other buffer.  At
+// exit the current state is copied back into the primary buffers if it is
+// in the second.  Each pass is the separate kernel's own pass (the same
+// per-thread elements, per-block partials and partial sums in the same
+// order), so the iterates, the CG step counts and the itstat records are
+// bit-identical to the separate kernels'.  It returns when CG has a step to
+// run or when the call's last iteration is done (S_ZU_DONE: the z/u kernel
+// that follows in the graph then only ends the loop).
 // ---------------------------------------------------------------------------
-constexpr int kErrBarrier = 8;  // projector error-word bit: a grid barrier wait ran out
-// Partials of the fast-forward kernel (doubles, per block): CG start (2
-// sums), dual residual (1), z/u statistics (3).
-constexpr int kFfInit = 0, kFfDual = 2 * NB, kFfZu = 3 * NB, kFfDoubles = 6 * NB;
+constexpr int kErrBarrier = 8;  // error-word bit: a grid barrier wait ran out
+// Partials of the fast-forward kernel (doubles), two sets alternating by
+// phase: CG start (2 sums per block), dual residual (1), z/u statistics (3).
+constexpr int kFfInit = 0, kFfDual = 2 * NB, kFfZu = 3 * NB, kFfSet = 6 * NB, kFfDoubles = 2 * kFfSet;
+
+// The state arrays (every term's z, u and dz) of this thread's elements,
+// copied from the second buffers to the primary ones.
+template <int ND>
+__device__ __forceinline__ void copy_state(const float* z2, const float* u2, const float* dz2, float* z, float* u,
+                                           float* dz, size_t N, int ng, int vec) {
+  const float* src[3] = {z2, u2, dz2};
+  float* dst[3] = {z, u, dz};
+  for (int a = 0; a < 3; ++a) {
+    for (int comp = 0; comp < ng * ND; ++comp) {
+      const size_t o = (size_t)comp * N;
+      if (vec) {
+        for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < N; e0 += 4 * (size_t)gridDim.x * NT)
+          *reinterpret_cast<float4*>(dst[a] + o + e0) = LdL2::q(src[a] + o + e0);
+      } else {
+        for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < N; e += (size_t)gridDim.x * NT)
+          dst[a][o + e] = LdL2::s(src[a] + o + e);
+      }
+    }
+  }
+}
 
 template <int ND>
 __global__ void __launch_bounds__(NT, 2)
     k_init_ffwd(const float* adj, int nsplit, const float* __restrict__ x, Shape3 sh, size_t N, TermParams tp,
                 float* r, float* rhs, float* p, float* lhsx, const float* __restrict__ atyc, float* z, float* u,
-                float* dz, double* slots, double* cg, double tol, double atol, int cg_maxiter, int maxiter,
-                double* fpart, unsigned int* bar, cudaGraphConditionalHandle cond, int vec, RecParams rp,
-                uint32_t max_polls, int* errflag) {
+                float* dz, float* z2, float* u2, float* dz2, double* slots, double* cg, double tol, double atol,
+                int cg_maxiter, int maxiter, double* fpart, unsigned int* bar, cudaGraphConditionalHandle cond,
+                int vec, RecParams rp, uint32_t max_polls, int* errflag) {
   ct::grid_dep_wait();  // before any global access (dependent launch)
   ct::grid_dep_trigger();
   __shared__ double dec_s[2];
-  // read by every block before the first barrier; block 0 writes both only after it
+  // read by every block before the first barrier; blocks write them only after it
   bool cached = slots[S_XCLEAN] != 0.0;
   int iter = (int)slots[S_ITER];
-  bool have_dual = false;  // dual-residual partials of a rhs pass of this launch are pending
-  unsigned int nbar = 0;
-  for (;;) {
-    // ---- CG start of iteration `iter` (k_lhs_finish<INIT>)
+  const unsigned int last = gridDim.x - 1;
+  int cur = 0;  // the current iteration's z, u, dz: 0 = primary buffers, 1 = second buffers
+  for (unsigned int phase = 0;; ++phase) {
+    double* fp = fpart + (phase & 1u) * kFfSet;
+    const float* zc = cur ? z2 : z;
+    const float* uc = cur ? u2 : u;
+    const float* dzc = cur ? dz2 : dz;
+    float* zn = cur ? z : z2;
+    float* un = cur ? u : u2;
+    float* dzn = cur ? dz : dz2;
+    if (phase > 0) {  // the rhs (k_rhs); the first phase's came from the graph's k_rhs
+      ct::KSum kd = rhs_pass<ND, LdL2>(atyc, zc, uc, dzc, rhs, sh, N, tp, vec);
+      double dacc[1] = {kd.value()};
+      ct::block_partials<NT, 1>(dacc, fp + kFfDual);
+    }
+    // the CG start (k_lhs_finish<INIT>); rhs at the thread's own elements
     double acc[2] = {0.0, 0.0};
     lhs_pass<ND, true, LdL2>(adj, nsplit, x, sh, N, tp, r, rhs, p, lhsx, cached, vec, acc);
-    ct::block_partials<NT, 2>(acc, fpart + kFfInit);
-    if (!ct::grid_barrier(bar, ++nbar * gridDim.x, max_polls, errflag, kErrBarrier)) return;
+    ct::block_partials<NT, 2>(acc, fp + kFfInit);
+    // the z/u update (k_zu, x unchanged), valid if CG runs no step
+    ct::KSum ks[3];
+    zu_pass<ND, LdL2>(x, zc, uc, zn, un, dzn, sh, N, tp, vec, ks);
+    double zacc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
+    ct::block_partials<NT, 3>(zacc, fp + kFfZu);
+    if (!ct::grid_barrier(bar, (phase + 1) * gridDim.x, max_polls, errflag, kErrBarrier)) return;
     double tot[2];
-    ct::sum_partials<NT, 2>(fpart + kFfInit, gridDim.x, tot);
+    ct::sum_partials<NT, 2>(fp + kFfInit, gridDim.x, tot);
     if (threadIdx.x == 0) {
       dec_s[0] = tot[0];
       dec_s[1] = tot[1];
@@ -897,9 +945,9 @@ __global__ void __launch_bounds__(NT, 2)
     const double thr = fmax(tol * bn, atol);
     const bool done = cg_maxiter <= 0 || !(dec_s[0] > thr * thr);
     if (blockIdx.x == 0) {
-      if (have_dual) {  // k_rhs's total, before the record that reads it
+      if (phase > 0) {  // k_rhs's total, before the record that reads it
         double d[1];
-        ct::sum_partials<NT, 1>(fpart + kFfDual, gridDim.x, d);
+        ct::sum_partials<NT, 1>(fp + kFfDual, gridDim.x, d);
         if (threadIdx.x == 0) slots[S_DUAL2] = d[0];
       }
       if (threadIdx.x == 0) {
@@ -918,18 +966,14 @@ __global__ void __launch_bounds__(NT, 2)
         if (!done) cudaGraphSetConditional(cond, 1u);
       }
     }
-    if (!done) return;  // uniform: CG runs this iteration's steps in the graph
-    cached = true;
-    // ---- z/u update of iteration `iter`, x unchanged (k_zu)
-    ct::KSum ks[3];
-    zu_pass<ND, LdL2>(x, z, u, dz, sh, N, tp, vec, ks);
-    double zacc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
-    ct::block_partials<NT, 3>(zacc, fpart + kFfZu);
-    if (!ct::grid_barrier(bar, ++nbar * gridDim.x, max_polls, errflag, kErrBarrier)) return;
-    ++iter;
-    if (blockIdx.x == 0) {
+    if (!done) {  // uniform: CG runs this iteration's steps in the graph; the update is dropped
+      if (cur) copy_state<ND>(z2, u2, dz2, z, u, dz, N, tp.ng, vec);
+      return;
+    }
+    ++iter;  // the update is committed (k_zu's last block)
+    if (blockIdx.x == last) {
       double zt[3];
-      ct::sum_partials<NT, 3>(fpart + kFfZu, gridDim.x, zt);
+      ct::sum_partials<NT, 3>(fp + kFfZu, gridDim.x, zt);
       if (threadIdx.x == 0) {
         slots[S_PRIMAL2] = zt[0];
         slots[S_G21] = zt[1];
@@ -939,17 +983,14 @@ __global__ void __launch_bounds__(NT, 2)
         if (iter >= maxiter) slots[S_ZU_DONE] = 1.0;
       }
     }
-    if (iter >= maxiter) return;
-    // ---- rhs of the next iteration (k_rhs): reads the neighbours' z and u,
-    // which the barrier above made visible; its CG start follows in the same
-    // threads (rhs at their own elements)
-    ct::KSum kd = rhs_pass<ND, LdL2>(atyc, z, u, dz, rhs, sh, N, tp, vec);
-    double dacc[1] = {kd.value()};
-    ct::block_partials<NT, 1>(dacc, fpart + kFfDual);
-    have_dual = true;
+    cur ^= 1;
+    cached = true;
+    if (iter >= maxiter) {
+      if (cur) copy_state<ND>(z2, u2, dz2, z, u, dz, N, tp.ng, vec);
+      return;
+    }
   }
 }
-
 
 // ---------------------------------------------------------------------------
 
@@ -1040,7 +1081,7 @@ Problem problem_of(const ct_admm_tv3d_desc* d) {
 struct Layout {
   int ng;
   size_t off_slots, off_red, off_atyc, off_rhs, off_r, off_p, off_ap, off_adj, off_sino, off_z, off_u,
-      off_dz, off_fwd, off_adjpart, off_lhsx, off_sinox, off_ff, total;
+      off_dz, off_fwd, off_adjpart, off_lhsx, off_sinox, off_ff, off_z2, off_u2, off_dz2, total;
 };
 
 Layout layout(const Problem& P) {
@@ -1070,6 +1111,9 @@ Layout layout(const Problem& P) {
   L.off_lhsx = take(P.N * 4);
   L.off_sinox = take(P.S * 4);
   L.off_ff = take(256 + sizeof(double) * kFfDoubles);  // barrier counter, then the partials
+  L.off_z2 = take(zbytes);  // the fast-forward kernel's second state buffers
+  L.off_u2 = take(zbytes);
+  L.off_dz2 = take(zbytes);
   L.total = o;
   return L;
 }
@@ -1210,7 +1254,8 @@ ct_status enqueue_init(const Ctx& c, cudaStream_t s, cudaGraphConditionalHandle 
     return ct::cuda_check(
         cudaLaunchKernelEx(&cfg, kf, adj, c.P.proj.nsplit(), (const float*)c.x, c.P.sh, N, c.tp, r, rhs, p,
                            c.at<float>(c.L.off_lhsx), (const float*)c.at<float>(c.L.off_atyc), c.at<float>(c.L.off_z),
-                           c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.slots(), c.cg(), c.P.prm.cg_tol,
+                           c.at<float>(c.L.off_u), c.at<float>(c.L.off_dz), c.at<float>(c.L.off_z2),
+                           c.at<float>(c.L.off_u2), c.at<float>(c.L.off_dz2), c.slots(), c.cg(), c.P.prm.cg_tol,
                            c.P.prm.cg_atol, c.P.prm.cg_maxiter, c.P.prm.maxiter, c.ff_part(), c.ff_bar(), cond, c.vi,
                            rec_params(c), polls, err),
         "k_init_ffwd");
