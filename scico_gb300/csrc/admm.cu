@@ -51,6 +51,7 @@
 #include <mutex>
 #include <vector>
 
+#include "cgpass.cuh"
 #include "kernels.cuh"
 
 namespace {
@@ -434,7 +435,11 @@ __global__ void __launch_bounds__(NT)
   ct::grid_dep_trigger();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     if (use_dirty) cudaGraphSetConditional(dirty, slots[S_XCLEAN] == 0.0 ? 1u : 0u);
-    if (bar_reset) *bar_reset = 0u;  // the grid barrier counter of this iteration's fast-forward kernel
+    if (bar_reset) {  // the grid barrier counters of this iteration's cooperative kernels
+      bar_reset[0] = 0u;  // k_init_ffwd
+      bar_reset[1] = 0u;  // k_cg_step: counter and the next launch's base
+      bar_reset[2] = 0u;
+    }
   }
   ct::KSum ks = rhs_pass<ND, LdPlain>(atyc, z, u, dz, rhs, sh, N, tp, vec);
   double acc[1] = {ks.value()};
@@ -871,9 +876,13 @@ __global__ void k_reset_call(double* __restrict__ slots) {
 // that follows in the graph then only ends the loop).
 // ---------------------------------------------------------------------------
 constexpr int kErrBarrier = 8;  // error-word bit: a grid barrier wait ran out
-// Partials of the fast-forward kernel (doubles), two sets alternating by
-// phase: CG start (2 sums per block), dual residual (1), z/u statistics (3).
-constexpr int kFfInit = 0, kFfDual = 2 * NB, kFfZu = 3 * NB, kFfSet = 6 * NB, kFfDoubles = 2 * kFfSet;
+// Partials of the fast-forward kernel: per block and phase the six sums
+// [CG start ||r||^2, ||rhs||^2, dual residual, z/u primal, g21, g1], reduced
+// over the block in one pass (each sum by the same tree as alone); two sets
+// alternating by phase.
+constexpr int kFfK = 6, kFfInit = 0, kFfDual = 2, kFfZu = 3, kFfSet = kFfK * NB;
+// ... and those of the fused CG step (k_cg_step): <p, Ap> and <r, r> phases.
+constexpr int kCgPart = 2 * kFfSet, kFfDoubles = kCgPart + 4 * NB;
 
 // The state arrays (every term's z, u and dz) of this thread's elements,
 // copied from the second buffers to the primary ones.
@@ -919,23 +928,25 @@ __global__ void __launch_bounds__(NT, 2)
     float* zn = cur ? z : z2;
     float* un = cur ? u : u2;
     float* dzn = cur ? dz : dz2;
+    double v6[kFfK];
+    v6[kFfDual] = 0.0;
     if (phase > 0) {  // the rhs (k_rhs); the first phase's came from the graph's k_rhs
       ct::KSum kd = rhs_pass<ND, LdL2>(atyc, zc, uc, dzc, rhs, sh, N, tp, vec);
-      double dacc[1] = {kd.value()};
-      ct::block_partials<NT, 1>(dacc, fp + kFfDual);
+      v6[kFfDual] = kd.value();
     }
     // the CG start (k_lhs_finish<INIT>); rhs at the thread's own elements
     double acc[2] = {0.0, 0.0};
     lhs_pass<ND, true, LdL2>(adj, nsplit, x, sh, N, tp, r, rhs, p, lhsx, cached, vec, acc);
-    ct::block_partials<NT, 2>(acc, fp + kFfInit);
+    v6[kFfInit] = acc[0];
+    v6[kFfInit + 1] = acc[1];
     // the z/u update (k_zu, x unchanged), valid if CG runs no step
     ct::KSum ks[3];
     zu_pass<ND, LdL2>(x, zc, uc, zn, un, dzn, sh, N, tp, vec, ks);
-    double zacc[3] = {ks[0].value(), ks[1].value(), ks[2].value()};
-    ct::block_partials<NT, 3>(zacc, fp + kFfZu);
+    for (int k = 0; k < 3; ++k) v6[kFfZu + k] = ks[k].value();
+    ct::block_partials<NT, kFfK>(v6, fp);
     if (!ct::grid_barrier(bar, (phase + 1) * gridDim.x, max_polls, errflag, kErrBarrier)) return;
     double tot[2];
-    ct::sum_partials<NT, 2>(fp + kFfInit, gridDim.x, tot);
+    ct::sum_partials<NT, 2>(fp + kFfInit, gridDim.x, tot, kFfK);
     if (threadIdx.x == 0) {
       dec_s[0] = tot[0];
       dec_s[1] = tot[1];
@@ -947,7 +958,7 @@ __global__ void __launch_bounds__(NT, 2)
     if (blockIdx.x == 0) {
       if (phase > 0) {  // k_rhs's total, before the record that reads it
         double d[1];
-        ct::sum_partials<NT, 1>(fp + kFfDual, gridDim.x, d);
+        ct::sum_partials<NT, 1>(fp + kFfDual, gridDim.x, d, kFfK);
         if (threadIdx.x == 0) slots[S_DUAL2] = d[0];
       }
       if (threadIdx.x == 0) {
@@ -973,7 +984,7 @@ __global__ void __launch_bounds__(NT, 2)
     ++iter;  // the update is committed (k_zu's last block)
     if (blockIdx.x == last) {
       double zt[3];
-      ct::sum_partials<NT, 3>(fp + kFfZu, gridDim.x, zt);
+      ct::sum_partials<NT, 3>(fp + kFfZu, gridDim.x, zt, kFfK);
       if (threadIdx.x == 0) {
         slots[S_PRIMAL2] = zt[0];
         slots[S_G21] = zt[1];
@@ -990,6 +1001,73 @@ __global__ void __launch_bounds__(NT, 2)
       return;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Fused CG step of the solve graph: k_lhs_finish<PAP>, k_cg_update and
+// k_cg_direction as one cooperative launch with two bounded grid barriers
+// (after <p, Ap> and after <r, r>), the projections of p staying separate
+// kernels before it.  vec / vec_update / vec_dir: each pass's quad flag as
+// its separate kernel takes it (the stencil pass needs the last axis in
+// quads, the vector passes only the flat length and alignment).  Each thread updates only its own elements in the
+// three passes (the same element mapping in all three), so the barriers
+// carry only the two sums; the passes and sums are the separate kernels'
+// own, so the iterates are bit-identical.  The barrier counter grows by two
+// grids per launch from 0 (reset by the iteration's k_rhs); bar[2] holds the
+// next launch's base.
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(NT, 2)
+    k_cg_step(const float* adj, int nsplit, float* p, Shape3 sh, size_t N, TermParams tp, float* ap, float* x,
+              float* r, double* cg, double* part, unsigned int* bar, cudaGraphConditionalHandle cond, int vec,
+              int vec_update, int vec_dir, uint32_t max_polls, int* errflag) {
+  ct::grid_dep_wait();  // before any global access (dependent launch)
+  ct::grid_dep_trigger();
+  __shared__ double sum_s;
+  // read by every block before the first barrier; block 0 writes them only after the second
+  const double num = cg[CT_CG_NUM], it0 = cg[CT_CG_ITERS];
+  const double tol2 = cg[CT_CG_TOL2], maxit = cg[CT_CG_MAXITER];
+  const unsigned int base = bar[2];
+  if (cg[CT_CG_DONE] != 0.0) {  // uniform (the graph's CG loop only runs while not done)
+    if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
+  // Ap = lhs(p) and <p, Ap> (k_lhs_finish<PAP>)
+  double acc[2] = {0.0, 0.0};
+  lhs_pass<ND, false, LdPlain>(adj, nsplit, p, sh, N, tp, ap, nullptr, nullptr, nullptr, false, vec, acc);
+  ct::block_partials<NT, 2>(acc, part);
+  if (!ct::grid_barrier(bar + 1, base + gridDim.x, max_polls, errflag, kErrBarrier)) return;
+  double t[2];
+  ct::sum_partials<NT, 2>(part, gridDim.x, t);
+  if (threadIdx.x == 0) sum_s = t[0];
+  __syncthreads();
+  const double pap = sum_s;
+  const double alpha = num / pap;
+  // x += alpha p; r -= alpha Ap; <r, r> (k_cg_update)
+  double v2[2] = {ct::cg_update_pass(x, r, p, ap, N, (float)alpha, vec_update), 0.0};
+  ct::block_partials<NT, 2>(v2, part + 2 * NB);
+  if (!ct::grid_barrier(bar + 1, base + 2 * gridDim.x, max_polls, errflag, kErrBarrier)) return;
+  ct::sum_partials<NT, 2>(part + 2 * NB, gridDim.x, t);
+  if (threadIdx.x == 0) sum_s = t[0];
+  __syncthreads();
+  const double trr = sum_s;
+  const double beta = trr / num;
+  const double it = it0 + 1.0;
+  const bool done = !(trr > tol2) || it >= maxit;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cg[CT_CG_PAP] = pap;
+    cg[CT_CG_ALPHA] = alpha;
+    cg[CT_CG_NUM] = trr;
+    cg[CT_CG_BETA] = beta;
+    cg[CT_CG_ITERS] = it;
+    cg[CT_CG_RAN] = 0.0;  // the direction update runs in this launch
+    if (done) cg[CT_CG_DONE] = 1.0;
+    bar[2] = base + 2 * gridDim.x;
+    cudaGraphSetConditional(cond, done ? 0u : 1u);
+  }
+  // p = r + beta p (k_cg_direction): the direction update still runs in the
+  // step that finds CG done (reference order)
+  ct::cg_direction_pass(p, r, N, (float)beta, vec_dir);
 }
 
 // ---------------------------------------------------------------------------
@@ -1281,6 +1359,25 @@ ct_status enqueue_cg_step(const Ctx& c, cudaStream_t s, cudaGraphConditionalHand
   ct_status st;
   const float* adj = backproject(c, sino, s, done, st, true);
   CT_TRY(st);
+  if (c.ffwd && use_cond) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(NB);
+    cfg.blockDim = dim3(NT);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const uint32_t polls = std::min<uint32_t>(ct::proj2d_wait_polls(), 1u << 21);
+    int* err = ct::proj2d_errflag_ptr();
+    if (!err) return ct::fail(CT_ERR_CUDA, "k_cg_step: error-word address unavailable");
+    auto kf = c.P.nd == 2 ? k_cg_step<2> : k_cg_step<3>;
+    return ct::cuda_check(cudaLaunchKernelEx(&cfg, kf, adj, c.P.proj.nsplit(), p, c.P.sh, N, c.tp, ap, c.x, r,
+                                             c.cg(), c.ff_part() + kCgPart, c.ff_bar(), cond, c.vi,
+                                             ct::quad_ok(N, c.x, r, p, ap), ct::quad_ok(N, p, r), polls, err),
+                          "k_cg_step");
+  }
   float* nf = nullptr;
   const float* ncf = nullptr;
   auto lhs = c.P.nd == 2 ? k_lhs_finish<2, false> : k_lhs_finish<3, false>;
@@ -1343,13 +1440,16 @@ bool ffwd_usable(int nd) {
   int dev = 0, coop = 0, nb = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
+  int nc = 0;
   const cudaError_t e = nd == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_init_ffwd<2>, NT, 0)
                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_init_ffwd<3>, NT, 0);
-  if (e != cudaSuccess) {
+  const cudaError_t e2 = nd == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nc, k_cg_step<2>, NT, 0)
+                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nc, k_cg_step<3>, NT, 0);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
   }
-  return nb * ct::sm_count() >= NB;
+  return std::min(nb, nc) * ct::sm_count() >= NB;
 }
 
 // Executable iteration graphs, one per problem (key: dimension, descriptor

@@ -176,15 +176,18 @@ __device__ __forceinline__ void block_partials(double (&v)[K], double* partials)
   }
 }
 
+// stride: doubles per block in `partials` (K when the block's partials are
+// exactly these K sums; larger when they are K of a wider set).
 template <int NT, int K>
-__device__ __forceinline__ void sum_partials(const double* partials, unsigned int nblocks, double (&out)[K]) {
+__device__ __forceinline__ void sum_partials(const double* partials, unsigned int nblocks, double (&out)[K],
+                                             unsigned int stride = K) {
   __shared__ double red[K][NT / 32];
   double acc[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) acc[k] = 0.0;
   for (unsigned int b = threadIdx.x; b < nblocks; b += NT) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] += __ldcg(partials + (size_t)K * b + k);
+    for (int k = 0; k < K; ++k) acc[k] += __ldcg(partials + (size_t)stride * b + k);
   }
   block_reduce<NT, K>(acc, red);
 #pragma unroll

@@ -1,6 +1,7 @@
 // Deterministic float64 reductions and the CG vector steps of
 // scico.solver.cg (scico/solver.py:378-400), with the stopping test kept on
 // the device so that a fixed launch sequence reproduces the early exit.
+#include "cgpass.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -148,42 +149,7 @@ __global__ void __launch_bounds__(NT)
   __syncthreads();
   const double alpha = alpha_s;
   const float af = (float)alpha;
-  double rr = 0.0;
-  if (vec) {
-    const size_t stride = 4 * (size_t)gridDim.x * NT;
-    auto quad = [&](size_t e0, float4 x4, float4 r4, float4 p4, float4 a4) {
-      float xv[4], rv[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        xv[j] = ct::fadd(at4(x4, j), ct::fmul(af, at4(p4, j)));
-        rv[j] = ct::fsub(at4(r4, j), ct::fmul(af, at4(a4, j)));
-        rr += (double)rv[j] * (double)rv[j];
-      }
-      st4(x, e0, make_float4(xv[0], xv[1], xv[2], xv[3]));
-      st4(r, e0, make_float4(rv[0], rv[1], rv[2], rv[3]));
-    };
-    for (size_t e0 = 4 * ((size_t)blockIdx.x * NT + threadIdx.x); e0 < n; e0 += 2 * stride) {
-      const bool two = e0 + stride < n;
-      const float4 x0 = ld4(x, e0), r0 = ld4(r, e0), p0 = ld4(p, e0), a0 = ld4(Ap, e0);
-      float4 x1 = x0, r1 = r0, p1 = p0, a1 = a0;
-      if (two) {
-        x1 = ld4(x, e0 + stride);
-        r1 = ld4(r, e0 + stride);
-        p1 = ld4(p, e0 + stride);
-        a1 = ld4(Ap, e0 + stride);
-      }
-      quad(e0, x0, r0, p0, a0);
-      if (two) quad(e0 + stride, x1, r1, p1, a1);
-    }
-  } else {
-    for (size_t e = (size_t)blockIdx.x * NT + threadIdx.x; e < n; e += (size_t)gridDim.x * NT) {
-      const float pe = p[e];
-      x[e] = ct::fadd(x[e], ct::fmul(af, pe));
-      const float re = ct::fsub(r[e], ct::fmul(af, Ap[e]));
-      r[e] = re;
-      rr += (double)re * (double)re;
-    }
-  }
+  const double rr = ct::cg_update_pass(x, r, p, Ap, n, af, vec);
   double trr, t1;
   if (grid_sum2_last<NT>(rr, 0.0, partials, ticket, trr, t1)) {
     const double num_old = s[CT_CG_NUM];
@@ -210,28 +176,7 @@ __global__ void k_cg_direction(float* __restrict__ p, const float* __restrict__ 
   ct::grid_dep_trigger();
   if (s[CT_CG_RAN] == 0.0) return;  // uniform over the grid
   const float bf = (float)s[CT_CG_BETA];
-  if (vec) {
-    const size_t stride = 4 * (size_t)gridDim.x * blockDim.x;
-    auto quad = [&](size_t e0, float4 r4, float4 p4) {
-      st4(p, e0, make_float4(ct::fadd(r4.x, ct::fmul(bf, p4.x)), ct::fadd(r4.y, ct::fmul(bf, p4.y)),
-                             ct::fadd(r4.z, ct::fmul(bf, p4.z)), ct::fadd(r4.w, ct::fmul(bf, p4.w))));
-    };
-    for (size_t e0 = 4 * ((size_t)blockIdx.x * blockDim.x + threadIdx.x); e0 < n; e0 += 2 * stride) {
-      const bool two = e0 + stride < n;
-      const float4 r0 = ld4(r, e0), p0 = ld4(p, e0);
-      float4 r1 = r0, p1 = p0;
-      if (two) {
-        r1 = ld4(r, e0 + stride);
-        p1 = ld4(p, e0 + stride);
-      }
-      quad(e0, r0, p0);
-      if (two) quad(e0 + stride, r1, p1);
-    }
-  } else {
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-         e += (size_t)gridDim.x * blockDim.x)
-      p[e] = ct::fadd(r[e], ct::fmul(bf, p[e]));
-  }
+  ct::cg_direction_pass(p, r, n, bf, vec);
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
