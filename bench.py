@@ -78,21 +78,41 @@ def solve_projections(cg_its):
     return n
 
 
-def solve_launches(cg_its):
+def solve_launches(cg_its, fast_forward=True):
     """Kernel launches of one fused solve whose iterations ran cg_its CG
-    steps: A^T y, its split sum, z/u init and the call reset (4); per
-    iteration k_rhs, the projections of x when CG moved x in the previous
-    iteration or it is the first (forward strips and gather, residual,
-    adjoint: the graph's conditional IF node), the CG start, the CG loop body
-    (the graph's WHILE node runs it exactly CG_It times: forward strips and
-    gather, adjoint, lhs, CG update, direction = 6) and the z/u update; the
-    itstat epilogue (rhs, forward strips and gather, residual, record = 5).
-    CG_It comes from the solve's own itstat records."""
+    steps (CG_It from the solve's own itstat records).  Set-up: A^T y, its
+    split sum, z/u init and the call reset (4); the itstat epilogue: rhs,
+    forward strips and gather, residual, record (5).
+
+    With the cooperative fast-forward kernels (the default on a GPU that
+    runs cooperative launches; ct_solver_fast_forward): the graph's loop body
+    starts at iteration 0 and after every iteration whose CG ran -- k_rhs,
+    the projections of x (forward strips and gather, residual, adjoint: 4),
+    the fast-forward CG start (1), which runs every following CG-free
+    iteration inside its own launch, the CG steps of the iteration it hands
+    back (forward strips and gather, adjoint, fused CG step = 4 each) and
+    the z/u update (1).  Without them: per iteration k_rhs, the projections
+    of x when CG moved x in the previous iteration or it is the first, the
+    CG start, 6 launches per CG step (forward 2, adjoint, lhs, update,
+    direction) and the z/u update."""
     n = 4 + 5
-    for i, k in enumerate(cg_its):
-        dirty = i == 0 or cg_its[i - 1] > 0
-        n += 1 + (4 if dirty else 0) + 1 + 6 * k + 1
+    m = len(cg_its)
+    if not fast_forward:
+        for i, k in enumerate(cg_its):
+            dirty = i == 0 or cg_its[i - 1] > 0
+            n += 1 + (4 if dirty else 0) + 1 + 6 * k + 1
+        return n
+    i = 0
+    while i < m:
+        n += 1 + 4 + 1 + 1
+        j = i
+        while j < m and cg_its[j] == 0:
+            j += 1
+        if j < m:
+            n += 4 * cg_its[j]
+        i = j + 1
     return n
+
 
 def _args():
     ap = argparse.ArgumentParser()
@@ -505,7 +525,7 @@ def run_gpu(args):
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
     cg_its = [int(v) for v in itstat[:, _lib.CT_ITSTAT_CG_ITERS].cpu().numpy()]
-    launches_per_step = solve_launches(cg_its)
+    launches_per_step = solve_launches(cg_its, bool(_lib.load().ct_solver_fast_forward()))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -733,7 +753,8 @@ def run_gpu_3d(args):
                              f"to {k:.1f} + 2 pairs per ADMM iteration ({per_iter:.1f} s per iteration)"}
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
-    launches_per_step = solve_launches(cg_its)  # as the 2D solver: forward 2 kernels, adjoint 1
+    # as the 2D solver (the 3D forward is also 2 kernels, the adjoint 1)
+    launches_per_step = solve_launches(cg_its, bool(_lib.load().ct_solver_fast_forward()))
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -513,8 +513,12 @@ ct_status ct_admm_tv_solve_batch(const ct_admm_tv_desc* descs, int32_t n,
  * ct_wait_poll_limit and 2^21) sets bit 3 of the device error word
  * (ct_proj2d_check reports CT_ERR_TIMEOUT).  On by default unless the
  * environment sets CTGPU_FFWD=0; used only where the device supports
- * cooperative launches and the kernel's 304 blocks fit at once.  The setting
- * is read when a solve graph is built (graphs are cached per setting).
+ * cooperative launches and the kernels' 304 blocks fit at once.  The
+ * setting is read when a solve graph is built (graphs are cached per
+ * setting).  In the same graphs each CG step's vector work (lhs, update,
+ * direction) is one cooperative launch with two bounded grid barriers.
+ * ct_solver_fast_forward returns 1 when the setting is on and the current
+ * device runs the kernels.
  */
 void ct_set_solver_fast_forward(int32_t on);
 int32_t ct_solver_fast_forward(void);

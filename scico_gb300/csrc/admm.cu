@@ -1763,7 +1763,7 @@ extern "C" {
 
 void ct_set_solver_fast_forward(int32_t on) { g_ffwd.store(on ? 1 : 0, std::memory_order_relaxed); }
 
-int32_t ct_solver_fast_forward(void) { return ffwd_enabled() ? 1 : 0; }
+int32_t ct_solver_fast_forward(void) { return ffwd_usable(2) ? 1 : 0; }
 
 ct_status ct_admm_tv_workspace(const ct_admm_tv_desc* d, size_t* bytes) {
   return workspace_of(d, "ct_admm_tv_workspace", bytes);
