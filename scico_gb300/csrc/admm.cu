@@ -914,6 +914,7 @@ __global__ void __launch_bounds__(NT, 2)
                 int vec, RecParams rp, uint32_t max_polls, int* errflag) {
   ct::grid_dep_wait();  // before any global access (dependent launch)
   ct::grid_dep_trigger();
+  using LDS = LdL2;  // state written by other blocks earlier in this launch
   __shared__ double dec_s[2];
   // read by every block before the first barrier; blocks write them only after it
   bool cached = slots[S_XCLEAN] != 0.0;
@@ -931,17 +932,17 @@ __global__ void __launch_bounds__(NT, 2)
     double v6[kFfK];
     v6[kFfDual] = 0.0;
     if (phase > 0) {  // the rhs (k_rhs); the first phase's came from the graph's k_rhs
-      ct::KSum kd = rhs_pass<ND, LdL2>(atyc, zc, uc, dzc, rhs, sh, N, tp, vec);
+      ct::KSum kd = rhs_pass<ND, LDS>(atyc, zc, uc, dzc, rhs, sh, N, tp, vec);
       v6[kFfDual] = kd.value();
     }
     // the CG start (k_lhs_finish<INIT>); rhs at the thread's own elements
     double acc[2] = {0.0, 0.0};
-    lhs_pass<ND, true, LdL2>(adj, nsplit, x, sh, N, tp, r, rhs, p, lhsx, cached, vec, acc);
+    lhs_pass<ND, true, LDS>(adj, nsplit, x, sh, N, tp, r, rhs, p, lhsx, cached, vec, acc);
     v6[kFfInit] = acc[0];
     v6[kFfInit + 1] = acc[1];
     // the z/u update (k_zu, x unchanged), valid if CG runs no step
     ct::KSum ks[3];
-    zu_pass<ND, LdL2>(x, zc, uc, zn, un, dzn, sh, N, tp, vec, ks);
+    zu_pass<ND, LDS>(x, zc, uc, zn, un, dzn, sh, N, tp, vec, ks);
     for (int k = 0; k < 3; ++k) v6[kFfZu + k] = ks[k].value();
     ct::block_partials<NT, kFfK>(v6, fp);
     if (!ct::grid_barrier(bar, (phase + 1) * gridDim.x, max_polls, errflag, kErrBarrier)) return;

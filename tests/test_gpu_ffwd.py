@@ -164,3 +164,67 @@ def test_barrier_timeout_reports_and_recovers(cuda):
     x_again = solve()  # the default limit: clean and exact again
     assert lib.ct_proj2d_errflag() == 0
     assert torch.equal(x_again, x_ref)
+
+
+@pytest.mark.parametrize("n", [64, 45])
+def test_plain_launches_match_the_graph(cuda, n):
+    """ct_admm_tv_solve with use_graph = 0 (every kernel a plain launch, each
+    after the first of the call a programmatic dependent launch) against the
+    solve graph (with its cooperative kernels): the same x and itstat
+    records, bit for bit; n = 45 takes the kernels' scalar paths."""
+    x_gt = workloads.random_ellipses(64, 6, 9)[:n, :n].copy()
+    A = linop.XRayTransform2D((n, n), np.linspace(0, np.pi, 40, endpoint=False))
+    y = A(torch.from_numpy(x_gt).to(cuda)).contiguous()
+    g = A.geometry()
+    out = []
+    for use_graph in (0, 1):
+        desc = _lib.AdmmTvDesc(g, 25, 10, 1e-4, 0.0, 0.01, 0.0, 2.0, 0.5, 1.0, use_graph)
+        nb = _lib.c_size_t()
+        _lib.call("ct_admm_tv_workspace", _lib.ctypes.addressof(desc), _lib.ctypes.addressof(nb))
+        ws = torch.empty(nb.value, dtype=torch.uint8, device=cuda)
+        x = torch.zeros((n, n), device=cuda)
+        it = torch.zeros((25, _lib.CT_ITSTAT_FIELDS), dtype=torch.float64, device=cuda)
+        _lib.call("ct_admm_tv_solve", _lib.ctypes.addressof(desc), y.data_ptr(), x.data_ptr(), it.data_ptr(), 0,
+                  ws.data_ptr(), ws.numel(), torch.cuda.current_stream().cuda_stream)
+        _lib.check_device(torch.cuda.current_stream().cuda_stream)
+        out.append((x.clone(), it.cpu()))
+    assert torch.equal(out[0][0], out[1][0])
+    assert torch.equal(out[0][1], out[1][1])
+    assert int((out[1][1][:, _lib.CT_ITSTAT_CG_ITERS] == 0).sum()) >= 1  # CG-free iterations in both
+
+
+def test_fast_forward_c2_size(cuda):
+    """The benchmark's workload (512^2, 360 views, 725 bins, lambda 0.005,
+    rho 2, 100 iterations, CG <= 10): one quad per thread of the 304 x 256
+    grid; the same bits with the cooperative kernels on and off."""
+    c = workloads.C2
+    A = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
+    y0 = A(torch.from_numpy(c.phantom()).to(cuda)).cpu().numpy()
+    y = torch.from_numpy(workloads.noisy(y0, c.noise, c.noise_seed)).to(cuda)
+
+    def go():
+        return _run(_admm(A, y, (c.n, c.n), c.lam, 0.0, c.rho, c.maxiter, c.cg_tol, c.cg_maxiter), calls=1)
+
+    off, on = _both(go)
+    _same(off, on)
+    assert [r[3] for r in on[3]].count(0) >= 50
+
+
+def test_fast_forward_3d_several_quads_per_thread(cuda):
+    """A 64^3 volume: 65,536 quads, so the grid-stride passes give most
+    threads several quads (the 3D path of the passes at size)."""
+    shape, det, nv = (64, 64, 64), (64, 91), 48
+    ang = np.linspace(0, np.pi, nv, endpoint=False)[:, None]
+    M = linop.XRayTransform3D.matrices_from_euler_angles(shape, det, "X", ang).astype(np.float32)
+    A = linop.XRayTransform3D(shape, M, det)
+    x_gt = np.zeros(shape, np.float32)
+    x_gt[10:40, 20:50, 15:45] = 1.0
+    x_gt[30:55, 5:25, 30:60] += 0.5
+    y = A(torch.from_numpy(x_gt).to(cuda))
+
+    def go():
+        return _run(_admm(A, y, shape, 0.01, 0.01, 1.0, 20, 1e-3, 8), calls=1)
+
+    off, on = _both(go)
+    _same(off, on)
+    assert [r[3] for r in on[3]].count(0) >= 1
