@@ -1033,11 +1033,21 @@ __global__ void __launch_bounds__(NT, 2)
     if (blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(cond, 0u);
     return;
   }
+  // A block whose barrier wait runs out ends the graph's CG loop (the error
+  // bit is set): the loop then cannot run on with a condition that no block
+  // of this launch cleared.  The loop continues only where block 0 passed
+  // both barriers, which also counts the step, so it ends by cg_maxiter.
+  auto give_up = [&]() {
+    if (threadIdx.x == 0) {
+      cg[CT_CG_DONE] = 1.0;
+      cudaGraphSetConditional(cond, 0u);
+    }
+  };
   // Ap = lhs(p) and <p, Ap> (k_lhs_finish<PAP>)
   double acc[2] = {0.0, 0.0};
   lhs_pass<ND, false, LdPlain>(adj, nsplit, p, sh, N, tp, ap, nullptr, nullptr, nullptr, false, vec, acc);
   ct::block_partials<NT, 2>(acc, part);
-  if (!ct::grid_barrier(bar + 1, base + gridDim.x, max_polls, errflag, kErrBarrier)) return;
+  if (!ct::grid_barrier(bar + 1, base + gridDim.x, max_polls, errflag, kErrBarrier)) return give_up();
   double t[2];
   ct::sum_partials<NT, 2>(part, gridDim.x, t);
   if (threadIdx.x == 0) sum_s = t[0];
@@ -1047,7 +1057,7 @@ __global__ void __launch_bounds__(NT, 2)
   // x += alpha p; r -= alpha Ap; <r, r> (k_cg_update)
   double v2[2] = {ct::cg_update_pass(x, r, p, ap, N, (float)alpha, vec_update), 0.0};
   ct::block_partials<NT, 2>(v2, part + 2 * NB);
-  if (!ct::grid_barrier(bar + 1, base + 2 * gridDim.x, max_polls, errflag, kErrBarrier)) return;
+  if (!ct::grid_barrier(bar + 1, base + 2 * gridDim.x, max_polls, errflag, kErrBarrier)) return give_up();
   ct::sum_partials<NT, 2>(part + 2 * NB, gridDim.x, t);
   if (threadIdx.x == 0) sum_s = t[0];
   __syncthreads();
