@@ -916,6 +916,13 @@ __global__ void __launch_bounds__(NT, 2)
   ct::grid_dep_trigger();
   using LDS = LdL2;  // state written by other blocks earlier in this launch
   __shared__ double dec_s[2];
+  // A block whose barrier wait runs out hands over to the graph's CG loop
+  // and returns: the solve's results are void (the error word says so), and
+  // the fused CG step then ends the loop on its own failed barrier, so every
+  // failure path of the solve graph runs in the poll-limit test.
+  auto give_up = [&]() {
+    if (threadIdx.x == 0) cudaGraphSetConditional(cond, 1u);
+  };
   // read by every block before the first barrier; blocks write them only after it
   bool cached = slots[S_XCLEAN] != 0.0;
   int iter = (int)slots[S_ITER];
@@ -945,7 +952,7 @@ __global__ void __launch_bounds__(NT, 2)
     zu_pass<ND, LDS>(x, zc, uc, zn, un, dzn, sh, N, tp, vec, ks);
     for (int k = 0; k < 3; ++k) v6[kFfZu + k] = ks[k].value();
     ct::block_partials<NT, kFfK>(v6, fp);
-    if (!ct::grid_barrier(bar, (phase + 1) * gridDim.x, max_polls, errflag, kErrBarrier)) return;
+    if (!ct::grid_barrier(bar, (phase + 1) * gridDim.x, max_polls, errflag, kErrBarrier)) return give_up();
     double tot[2];
     ct::sum_partials<NT, 2>(fp + kFfInit, gridDim.x, tot, kFfK);
     if (threadIdx.x == 0) {
