@@ -137,3 +137,31 @@ def test_modl_native_matches_autograd(cuda):
     num = sum(((a.double() - c.double()) ** 2).sum() for a, c in zip(out[0][1], out[1][1])).sqrt()
     den = sum((c.double() ** 2).sum() for c in out[1][1]).sqrt()
     assert (num / den).item() <= 1e-4
+
+
+def test_cg_block_reference_code_vectors(cuda):
+    """Against scico.flax's own cg_solver run under the float32 jax.numpy
+    stand-in (tests/golden/modl_cg_reference_code.npz).  The block keeps its
+    dot products in float64, the stand-in in float32: the bar is 3x the
+    distance of the oracle's recurrence with float64 dots from the vectors,
+    plus 1e-5 (at lambda 0.1 / 10 steps that distance is 6e-4, at 0.5 / 6
+    steps 1e-4)."""
+    from pathlib import Path
+
+    z = np.load(Path(__file__).resolve().parent / "golden" / "modl_cg_reference_code.npz")
+    for k in range(2):
+        p = f"c{k}_"
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        ang = np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32)
+        H = linop.XRayTransform2D((n, n), ang)
+        g = ctref.xray2d_defaults((n, n), ang)
+        lm = float(z[p + "lmbda"])
+        A = lambda v: ctref.xray2d_back_project(ctref.xray2d_project(v, g, np.float32), g, np.float32) + \
+            np.float32(lm) * v
+        floor = ctref.rel_l2(ctref.cg_fixed(A, z[p + "b"], maxiter=int(z[p + "maxiter"]), dot_dtype=np.float64),
+                             z[p + "x"])
+        b = torch.from_numpy(z[p + "b"]).to(cuda)[None]
+        lam = torch.full((1,), lm, device=cuda)
+        x = inverse.cg_block(H, b, lam, maxiter=int(z[p + "maxiter"]))[0].cpu().numpy()
+        assert ctref.rel_l2(x, z[p + "x"]) <= 3 * floor + 1e-5, (k, ctref.rel_l2(x, z[p + "x"]), floor)
+

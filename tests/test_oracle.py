@@ -251,6 +251,26 @@ def test_admm_oracle_is_the_reference_code():
         np.testing.assert_allclose(ours, z[p + "itstat"], rtol=1e-6)
 
 
+def test_modl_cg_oracle_is_the_reference_code():
+    """The oracle's fixed-iteration CG (cg_fixed) against scico.flax's own
+    cg_solver (flax/inverse.py:113-158) executed under the float32
+    jax.numpy stand-in on MoDLNet's system A^T A + lambda I with the
+    reference projector (tests/golden/make_modl_cg_reference.py): the same
+    iterate bit for bit, at lambda 0.1 / 10 steps and 0.5 / 6 steps."""
+    z = np.load(GOLDEN / "modl_cg_reference_code.npz")
+    for k in range(2):
+        p = f"c{k}_"
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        g = ctref.xray2d_defaults((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
+        lm = np.float32(float(z[p + "lmbda"]))
+
+        def A(v):
+            return ctref.xray2d_back_project(ctref.xray2d_project(v, g, np.float32), g, np.float32) + lm * v
+
+        x = ctref.cg_fixed(A, z[p + "b"], maxiter=int(z[p + "maxiter"]))
+        assert np.array_equal(x, z[p + "x"]), k
+
+
 def test_xray2d_f32_vs_f64():
     rng = np.random.default_rng(4)
     im = rng.random((20, 20)).astype(np.float32)
