@@ -136,3 +136,29 @@ def test_padmm_fused_continuation(cuda):
     assert torch.equal(xa, xb)
     assert len(b.history()) == 20
     assert [r.Prml_Rsdl for r in a.history()] == [r.Prml_Rsdl for r in b.history()]
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_padmm_reference_code_vectors(cuda, fused):
+    """Against scico's own ProximalADMM.step and prox code run under the
+    float32 jax.numpy stand-in (tests/golden/padmm_reference_code.npz), with
+    the vectors' mu and nu: x within 1e-4 after the last iteration, through
+    the fused solver and the generic composition."""
+    from pathlib import Path
+
+    z = np.load(Path(__file__).resolve().parent / "golden" / "padmm_reference_code.npz")
+    for k in range(2):
+        p = f"c{k}_"
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        H = linop.XRayTransform2D((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
+        alpha, lam = float(z[p + "alpha"]), float(z[p + "lam"])
+        D = linop.FiniteDifference((n, n), append=0)
+        A = linop.VerticalStack((H, alpha * D))
+        g = functional.SeparableFunctional((loss.SquaredL2Loss(y=torch.from_numpy(z[p + "y"]).to(cuda)),
+                                            (lam / alpha) * functional.L21Norm()))
+        X = z[p + "x"]
+        s = ProximalADMM(f=functional.ZeroFunctional(), g=g, A=A, rho=float(z[p + "rho"]), mu=float(z[p + "mu"]),
+                         nu=float(z[p + "nu"]), maxiter=len(X), fused=fused)
+        x = s.solve().cpu().numpy()
+        assert ctref.rel_l2(x, X[-1]) <= 1e-4, (k, ctref.rel_l2(x, X[-1]))
+

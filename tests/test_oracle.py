@@ -271,6 +271,28 @@ def test_modl_cg_oracle_is_the_reference_code():
         assert np.array_equal(x, z[p + "x"]), k
 
 
+def test_padmm_oracle_is_the_reference_code():
+    """The oracle's proximal ADMM (padmm_tv, float32) against scico's own
+    ProximalADMM.step, SeparableFunctional / ZeroFunctional / SquaredL2Loss /
+    L21Norm prox, FiniteDifference and projector code executed under the
+    float32 jax.numpy stand-in on the ct_3d_tv_padmm split with a 2D
+    projector (tests/golden/make_padmm_reference.py): x after every
+    iteration bit for bit."""
+    z = np.load(GOLDEN / "padmm_reference_code.npz")
+    for k in range(2):
+        p = f"c{k}_"
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        g = ctref.xray2d_defaults((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
+        fwd = lambda v: ctref.xray2d_project(v, g, np.float32)
+        adj = lambda s: ctref.xray2d_back_project(s, g, np.float32)
+        X = z[p + "x"]
+        for it in (1, len(X)):
+            x, _ = ctref.padmm_tv(fwd, adj, z[p + "y"], (n, n), lam=float(z[p + "lam"]), alpha=float(z[p + "alpha"]),
+                                  rho=float(z[p + "rho"]), mu=float(z[p + "mu"]), nu=float(z[p + "nu"]), maxiter=it,
+                                  dtype=np.float32)
+            assert np.array_equal(x, X[it - 1]), (k, it)
+
+
 def test_xray2d_f32_vs_f64():
     rng = np.random.default_rng(4)
     im = rng.random((20, 20)).astype(np.float32)
