@@ -231,7 +231,8 @@ class ResNet(torch.nn.Module):
             if isinstance(m, torch.nn.Conv2d):
                 torch.nn.init.xavier_normal_(m.weight)
         # NHWC (channels-last) activations and filters: cuDNN's convolution
-        # and batch-norm kernels for this layout run the C4 training step in
+        # and batch-norm kernels for this layout run the MoDL training step
+        # (16 x 256^2 images, 32 filters) in
         # 0.82x the time of NCHW (float32 throughout, same arithmetic up to
         # the kernels' summation order)
         self.body.to(memory_format=torch.channels_last)
