@@ -114,3 +114,23 @@ def test_reference_arm_nonzero_rank_exits_quietly():
     r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "0"], capture_output=True, text=True, env=env, timeout=300)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_launch_and_projection_accounting():
+    """bench.solve_launches / solve_projections from a solve's CG step
+    counts: set-up 4 + epilogue 5; with the cooperative kernels a pass of the
+    graph's loop body (iteration 0 and every iteration after one whose CG
+    ran) is k_rhs, 4 projection launches, the fast-forward CG start and the
+    z/u update, plus 4 launches per CG step of the iteration it hands back
+    (the CG-free iterations in between run inside the fast-forward launch);
+    without them every iteration launches its own kernels, 6 per CG step."""
+    import bench
+
+    cg = [10, 10, 7, 0, 0, 5, 0, 0]
+    assert bench.solve_launches(cg, True) == 9 + (7 + 40) + (7 + 40) + (7 + 28) + (7 + 20) + 7
+    per_iter = [1 + (4 if i == 0 or cg[i - 1] > 0 else 0) + 1 + 6 * k + 1 for i, k in enumerate(cg)]
+    assert bench.solve_launches(cg, False) == 9 + sum(per_iter)
+    assert bench.solve_launches([0, 0, 0], True) == 9 + 7  # one pass: the CG start runs all three
+    # A^T y, the epilogue's A x (the last CG moved x), a pair per CG step and
+    # per iteration after a CG step
+    assert bench.solve_projections([3, 0, 2]) == 1 + 1 + (2 + 6) + (2 + 0) + (0 + 4)
