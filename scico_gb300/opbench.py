@@ -37,6 +37,9 @@ def main(argv=None):
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     ap.add_argument("--views", type=int, default=0, help="proj3d: first N views of the workload (0 = all)")
     ap.add_argument("--recompute", action="store_true", help="modl: recompute CG steps in the backward pass")
+    ap.add_argument("--cudnn-search", type=int, default=1, choices=[0, 1],
+                    help="modl: 1 = cuDNN picks convolution algorithms by measuring them (as XLA autotunes its "
+                         "convolutions), 0 = cuDNN's heuristics")
     ap.add_argument("--streams", type=int, default=0, help="c3: internal streams of the batch solve (0 = auto)")
     ap.add_argument("--autotune", action="store_true",
                     help="c3, modl: measure and record projector schedules (ct_proj2d_autotune) before timing")
@@ -60,7 +63,7 @@ def main(argv=None):
     if a.op == "padmm3d":
         return print(json.dumps(padmm3d(dev, a.iters, a.warmup, a.reps)))
     if a.op == "modl":
-        return print(json.dumps(modl(dev, a.warmup, a.reps, a.recompute, a.autotune)))
+        return print(json.dumps(modl(dev, a.warmup, a.reps, a.recompute, a.autotune, bool(a.cudnn_search))))
     if a.op == "c3":
         return print(json.dumps(c3(dev, a.iters, a.warmup, a.reps, a.streams, a.autotune, a.plain)))
     c = {"c1": workloads.C1, "c2": workloads.C2}[a.config]
@@ -229,7 +232,7 @@ def padmm3d(dev, iters=20, warmup=1, reps=2, generic=True):
     return out
 
 
-def modl(dev, warmup=3, reps=20, recompute=False, autotune=False):
+def modl(dev, warmup=3, reps=20, recompute=False, autotune=False, cudnn_search=True):
     """One MoDL training step on the C4 batch (16 x 256^2, 180 views; 5
     blocks of CG(10) on A^T A + lmbda I, 3-layer 32-filter ResNet): forward
     with the MSE loss, then backward, each timed with CUDA events.
@@ -238,6 +241,9 @@ def modl(dev, warmup=3, reps=20, recompute=False, autotune=False):
 
     torch.backends.cudnn.allow_tf32 = False
     torch.backends.cuda.matmul.allow_tf32 = False
+    # cuDNN's measured algorithm choice (the counterpart of XLA's convolution
+    # autotuning); its heuristics pick FFT-tiled backward convolutions here
+    torch.backends.cudnn.benchmark = cudnn_search
     c = workloads.C4
     H = linop.XRayTransform2D((c.n, c.n), c.angles, det_count=c.det_count)
     schedule = H.autotune(batch=c.batch, reps=5) if autotune else H.schedule(batch=c.batch)
@@ -267,7 +273,7 @@ def modl(dev, warmup=3, reps=20, recompute=False, autotune=False):
             "forward_s": tf, "backward_s": tb, "backward_over_forward": tb / tf,
             "images_per_s_train": c.batch / (tf + tb), "projector_applications_forward": n_proj,
             "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9, "loss": float(loss.detach()),
-            "projector_schedule": schedule}
+            "projector_schedule": schedule, "cudnn_search": cudnn_search}
 
 
 def c3(dev, iters=50, warmup=3, reps=20, streams=0, autotune=False, plain=False):
