@@ -10,7 +10,9 @@ Configuration keys follow the reference's ConfigDict
 ``warmup_epochs``, ``lr_schedule``, ``criterion``, ``steps_per_eval``,
 ``steps_per_checkpoint``, ``log_every_steps``, ``log``, ``workdir``,
 ``checkpointing``, ``return_state``, ``post_lst`` (and ``device``, default
-the CUDA device).  Data sets are dicts with
+the CUDA device; ``cudnn_search``, default True: cuDNN picks convolution
+algorithms by measuring them, as XLA autotunes the reference's
+convolutions).  Data sets are dicts with
 ``"image"`` (the network input: projections ``(N, *A.output_shape)``, an
 optional trailing channel axis of 1) and ``"label"`` (the images).
 
@@ -177,6 +179,8 @@ class BasicTrainer:
         # (dense, CPU) operators may name its device
         self.dev = torch.device(config["device"]) if "device" in config else _device.require_cuda()
         self.model = model.to(self.dev)
+        if self.dev.type == "cuda":
+            torch.backends.cudnn.benchmark = bool(config.get("cudnn_search", True))
         seed = int(config.get("seed", 0))
         torch.manual_seed(seed)
         bs = int(config.get("batch_size", 2))
