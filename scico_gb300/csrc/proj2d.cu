@@ -1291,8 +1291,10 @@ ct_status ct_proj2d_check(ct_stream_t stream) {
 int ct_proj2d_errflag(void) {
   int v = 0;
   if (cudaMemcpyFromSymbol(&v, g_proj2d_err, sizeof(int)) != cudaSuccess) return -1;
-  const int zero = 0;
-  cudaMemcpyToSymbol(g_proj2d_err, &zero, sizeof(int));
+  if (v != 0) {  // clear only a set word (no copy on the common path)
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_proj2d_err, &zero, sizeof(int));
+  }
   return v;
 }
 

@@ -1128,8 +1128,10 @@ void ct_proj3d_schedule_clear(void) {
 int ct_proj3d_errflag(void) {
   int v = 0;
   if (cudaMemcpyFromSymbol(&v, ct::g_proj3d_err, sizeof(int)) != cudaSuccess) return -1;
-  const int zero = 0;
-  cudaMemcpyToSymbol(ct::g_proj3d_err, &zero, sizeof(int));
+  if (v != 0) {  // clear only a set word (no copy on the common path)
+    const int zero = 0;
+    cudaMemcpyToSymbol(ct::g_proj3d_err, &zero, sizeof(int));
+  }
   return v;
 }
 
