@@ -348,6 +348,21 @@ ct_status ct_fd_fwd(const ct_fd_desc* d, const float* x, float* out,
 ct_status ct_fd_adj(const ct_fd_desc* d, const float* dx, float* x,
                     int32_t batch, ct_stream_t stream);
 
+/* w = HaarTransform(x): the single-level shift-invariant Haar transform of
+ * the TV norms' prox over d->axes (HaarTransform / SingleAxisHaarTransform,
+ * scico/functional/_tvnorm.py:458-538): for axis k, w[k][0] =
+ * r (x + roll(x, -1)) and w[k][1] = r (roll(x, -1) - x), r = float32(1/sqrt 2),
+ * w of shape (naxes, 2, *shape) per batch item.  Only d's ndim, shape, naxes
+ * and axes are read. */
+ct_status ct_haar_fwd(const ct_fd_desc* d, const float* x, float* w,
+                      int32_t batch, ct_stream_t stream);
+
+/* x = its adjoint: the sum over axes, in order, of r (lo + roll(lo, 1)) +
+ * r (roll(hi, 1) - hi) (the transpose jax builds for the reference's
+ * FiniteSum / circular FiniteDifference, summed per VerticalStack block). */
+ct_status ct_haar_adj(const ct_fd_desc* d, const float* w, float* x,
+                      int32_t batch, ct_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Proximal operators and norms (scico/functional/_norm.py)                 */
 /* ------------------------------------------------------------------------ */

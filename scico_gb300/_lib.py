@@ -214,6 +214,8 @@ _SIGNATURES = {
     "ct_fd_out_count": (ctypes.c_int, [P, P]),
     "ct_fd_fwd": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_fd_adj": (ctypes.c_int, [P, P, P, c_int32, P]),
+    "ct_haar_fwd": (ctypes.c_int, [P, P, P, c_int32, P]),
+    "ct_haar_adj": (ctypes.c_int, [P, P, P, c_int32, P]),
     "ct_l21_prox": (ctypes.c_int, [P, P, c_int32, c_int64, c_float, P]),
     "ct_l1_prox": (ctypes.c_int, [P, P, c_int64, c_float, P]),
     "ct_l21_norm": (ctypes.c_int, [P, c_int32, c_int64, P, P, c_size_t, P]),

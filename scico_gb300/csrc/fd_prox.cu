@@ -1,5 +1,7 @@
 // Finite differences (scico FiniteDifference), their adjoint, and the
 // L2,1 / L1 proximal operators and norms (scico/functional/_norm.py).
+#include <math.h>
+
 #include <algorithm>
 
 #include "common.cuh"
@@ -160,6 +162,68 @@ __global__ void k_fd_adj(const float* __restrict__ d, float* __restrict__ x, FdP
   }
 }
 
+// Single-level shift-invariant Haar transform over the descriptor's axes
+// (HaarTransform / SingleAxisHaarTransform, scico/functional/_tvnorm.py:
+// 458-538), output (naxes, 2, *shape) per batch item: for axis k,
+// w[k][0] = r (x + x[next]) and w[k][1] = r (x[next] - x), x[next] the
+// circularly next sample along the axis, r = float32(1/sqrt 2); every sum and
+// product rounded on its own (the reference's separate float32 operations).
+__global__ void k_haar_fwd(const float* __restrict__ x, float* __restrict__ w, FdParams p, float r,
+                           int batch) {
+  const size_t per = 2 * (size_t)p.nblocks * p.in_count;
+  const size_t total = per * batch;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t bi = e / per;
+    size_t rem = e - bi * per;
+    const int k = (int)(rem / (2 * p.in_count));
+    rem -= (size_t)k * 2 * p.in_count;
+    const int comp = (int)(rem / p.in_count);
+    const size_t idx = rem - (size_t)comp * p.in_count;
+    const int ax = p.blk[k].axis;
+    const int c2 = (int)(idx % p.n[2]);
+    const size_t r1 = idx / p.n[2];
+    const int c[3] = {(int)(r1 / p.n[1]), (int)(r1 % p.n[1]), c2};
+    size_t stride = 1;
+    for (int q = 2; q > ax; --q) stride *= p.n[q];
+    const float* xb = x + bi * p.in_count;
+    const float xc = __ldg(xb + idx);
+    const size_t in = c[ax] + 1 == p.n[ax] ? idx - (size_t)c[ax] * stride : idx + stride;
+    const float xn = __ldg(xb + in);
+    w[e] = comp == 0 ? ct::fmul(r, ct::fadd(xc, xn)) : ct::fmul(r, ct::fsub(xn, xc));
+  }
+}
+
+// Its adjoint: x = sum over axes, in axis order, of
+// r (lo + lo[prev]) + r (hi[prev] - hi), [prev] the circularly previous
+// sample along the axis.
+__global__ void k_haar_adj(const float* __restrict__ w, float* __restrict__ x, FdParams p, float r,
+                           int batch) {
+  const size_t total = p.in_count * batch;
+  const size_t per = 2 * (size_t)p.nblocks * p.in_count;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t bi = e / p.in_count;
+    const size_t idx = e - bi * p.in_count;
+    const int c2 = (int)(idx % p.n[2]);
+    const size_t r1 = idx / p.n[2];
+    const int c[3] = {(int)(r1 / p.n[1]), (int)(r1 % p.n[1]), c2};
+    float acc = 0.0f;
+    for (int k = 0; k < p.nblocks; ++k) {
+      const int ax = p.blk[k].axis;
+      size_t stride = 1;
+      for (int q = 2; q > ax; --q) stride *= p.n[q];
+      const size_t ip = c[ax] == 0 ? idx + (size_t)(p.n[ax] - 1) * stride : idx - stride;
+      const float* lo = w + bi * per + (size_t)k * 2 * p.in_count;
+      const float* hi = lo + p.in_count;
+      const float t = ct::fadd(ct::fmul(r, ct::fadd(__ldg(lo + idx), __ldg(lo + ip))),
+                               ct::fmul(r, ct::fsub(__ldg(hi + ip), __ldg(hi + idx))));
+      acc = k == 0 ? t : ct::fadd(acc, t);
+    }
+    x[e] = acc;
+  }
+}
+
 int grid_for(size_t n, int threads) {
   const size_t want = (n + threads - 1) / threads;
   const size_t cap = (size_t)ct::sm_count() * 16;
@@ -262,6 +326,28 @@ ct_status ct_fd_adj(const ct_fd_desc* d, const float* dx, float* x, int32_t batc
   const size_t total = p.in_count * batch;
   k_fd_adj<<<grid_for(total, 256), 256, 0, ct::as_stream(stream)>>>(dx, x, p, batch);
   return ct::launch_check("k_fd_adj");
+}
+
+ct_status ct_haar_fwd(const ct_fd_desc* d, const float* x, float* w, int32_t batch, ct_stream_t stream) {
+  FdParams p{};
+  ct_status st = make_fd(d, p, "ct_haar_fwd");
+  if (st != CT_OK) return st;
+  if (!x || !w) return ct::fail(CT_ERR_INVALID_ARG, "ct_haar_fwd: null array");
+  if (batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_haar_fwd: batch=%d", batch);
+  const size_t total = 2 * (size_t)p.nblocks * p.in_count * batch;
+  k_haar_fwd<<<grid_for(total, 256), 256, 0, ct::as_stream(stream)>>>(x, w, p, (float)(1.0 / sqrt(2.0)), batch);
+  return ct::launch_check("k_haar_fwd");
+}
+
+ct_status ct_haar_adj(const ct_fd_desc* d, const float* w, float* x, int32_t batch, ct_stream_t stream) {
+  FdParams p{};
+  ct_status st = make_fd(d, p, "ct_haar_adj");
+  if (st != CT_OK) return st;
+  if (!x || !w) return ct::fail(CT_ERR_INVALID_ARG, "ct_haar_adj: null array");
+  if (batch <= 0) return ct::fail(CT_ERR_INVALID_ARG, "ct_haar_adj: batch=%d", batch);
+  const size_t total = p.in_count * batch;
+  k_haar_adj<<<grid_for(total, 256), 256, 0, ct::as_stream(stream)>>>(w, x, p, (float)(1.0 / sqrt(2.0)), batch);
+  return ct::launch_check("k_haar_adj");
 }
 
 ct_status ct_l21_prox(const float* v, float* out, int32_t ncomp, int64_t n, float lam,

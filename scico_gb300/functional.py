@@ -17,6 +17,7 @@ proxes run in the ctgpu kernels.
 
 from __future__ import annotations
 
+import ctypes
 import math
 from typing import Tuple, Union
 
@@ -193,29 +194,33 @@ class L1Norm(Functional):
 # TV norms (scico/functional/_tvnorm.py)
 # ---------------------------------------------------------------------------
 
-_R2 = 1.0 / math.sqrt(2.0)
+def _haar_desc(shape, axes):
+    from .linop import _fd_desc
+
+    return _fd_desc(tuple(shape), tuple(axes), None, None, True)
 
 
 def _haar_fwd(x: torch.Tensor, axes) -> torch.Tensor:
     """Single-level shift-invariant Haar transform (HaarTransform,
-    _tvnorm.py:458-538): per axis a lowpass (x + x shifted by one, circular)
-    and highpass (x shifted by one - x) component, each / sqrt(2), stacked
-    to (naxes, 2, *shape)."""
-    out = []
-    for a in axes:
-        xs = torch.roll(x, -1, dims=a)
-        out.append(torch.stack((_R2 * (x + xs), _R2 * (xs - x))))
-    return torch.stack(out)
+    _tvnorm.py:458-538) by ct_haar_fwd: per axis a lowpass (x + x shifted by
+    one, circular) and highpass (x shifted by one - x) component, each times
+    float32(1/sqrt 2), stacked to (naxes, 2, *shape)."""
+    x = x.contiguous()
+    d = _haar_desc(x.shape, axes)
+    w = _device.empty((len(axes), 2) + tuple(x.shape))
+    _lib.call("ct_haar_fwd", ctypes.addressof(d), x.data_ptr(), w.data_ptr(), 1, _device.stream())
+    return w
 
 
 def _haar_adj(w: torch.Tensor, axes) -> torch.Tensor:
-    """Adjoint of _haar_fwd: sum over axes of the adjoint of each component."""
-    acc = None
-    for k, a in enumerate(axes):
-        lo, hi = w[k, 0], w[k, 1]
-        t = _R2 * (lo + torch.roll(lo, 1, dims=a)) + _R2 * (torch.roll(hi, 1, dims=a) - hi)
-        acc = t if acc is None else acc + t
-    return acc
+    """Adjoint of _haar_fwd (ct_haar_adj): the sum over axes of the adjoint
+    of each component."""
+    w = w.contiguous()
+    shape = tuple(w.shape[2:])
+    d = _haar_desc(shape, axes)
+    x = _device.empty(shape)
+    _lib.call("ct_haar_adj", ctypes.addressof(d), w.data_ptr(), x.data_ptr(), 1, _device.stream())
+    return x
 
 
 def haar_transform(x, axes=None, adjoint: bool = False) -> torch.Tensor:

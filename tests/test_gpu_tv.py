@@ -16,6 +16,20 @@ from scico_gb300.optimize import ADMM, AcceleratedPGM, LinearSubproblemSolver
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("shape,axes", [((17,), (0,)), ((12, 9), (0, 1)), ((12, 9), (1,)), ((5, 6, 7), (0, 1, 2)),
+                                        ((5, 6, 7), (2, 0))])
+def test_haar_kernels_vs_oracle(cuda, shape, axes):
+    """ct_haar_fwd / ct_haar_adj against the oracle's float32 Haar transform
+    and its adjoint (the same float32 operations): bit for bit."""
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(shape).astype(np.float32)
+    w = functional.haar_transform(torch.from_numpy(x).to(cuda), axes=axes)
+    np.testing.assert_array_equal(w.cpu().numpy(), ctref.haar_fwd(x, axes))
+    wr = rng.standard_normal((len(axes), 2) + shape).astype(np.float32)
+    back = functional.haar_transform(torch.from_numpy(wr).to(cuda), axes=axes, adjoint=True)
+    np.testing.assert_array_equal(back.cpu().numpy(), ctref.haar_adj(wr, axes))
+
+
 def test_haar_identities(cuda):
     x = torch.randn((3, 4), generator=torch.Generator().manual_seed(1)).to(cuda)
     for ax in (0, 1):
