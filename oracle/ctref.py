@@ -590,17 +590,21 @@ def tv_prox(v: np.ndarray, lam: float, isotropic: bool, circular: bool, axes=Non
     nd = v.ndim
     axes = tuple(range(nd)) if axes is None else tuple(axes)
     K = 2 * len(axes)
-    thr = math.sqrt(2.0) * K * lam
+    # snp.sqrt(2) * K * lam and (1.0 / K) * ... (_tvnorm.py:203, 206) in the
+    # array dtype, as jax evaluates them on float32 arrays
+    f = np.dtype(dtype).type
+    thr = f(f(np.sqrt(f(2.0))) * f(K)) * f(lam)
+    inv_k = f(1.0 / K)
     prox = (lambda t: l21_prox(t, thr)) if isotropic else (lambda t: l1_prox(t, thr))
     if circular:
         w = haar_fwd(v, axes)
         w[:, 1] = prox(w[:, 1])
-        return haar_adj(w, axes) / K
+        return inv_k * haar_adj(w, axes)
     vp = np.pad(v, [(0, 1) if a in axes else (0, 0) for a in range(nd)], mode="edge")
     w = haar_fwd(vp, axes)
     region = (slice(None), 1) + tuple(slice(0, vp.shape[a] - 1) if a in axes else slice(None) for a in range(nd))
     w[region] = prox(w[region])
-    return (haar_adj(w, axes) / K)[tuple(slice(0, n) for n in v.shape)]
+    return (inv_k * haar_adj(w, axes))[tuple(slice(0, n) for n in v.shape)]
 
 
 def snr(reference: np.ndarray, comparison: np.ndarray) -> float:

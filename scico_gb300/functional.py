@@ -18,7 +18,6 @@ proxes run in the ctgpu kernels.
 from __future__ import annotations
 
 import ctypes
-import math
 from typing import Tuple, Union
 
 import numpy as np
@@ -277,10 +276,14 @@ class TVNorm(Functional):
         nd = v.ndim
         axes = self._axes_of(nd)
         K = 2 * len(axes)
+        # the base norm's prox parameter snp.sqrt(2) * K * lam (_tvnorm.py:203),
+        # evaluated in float32 as jax evaluates it
+        f = np.float32
+        thr = float(f(f(np.sqrt(f(2.0))) * f(K)) * f(lam))
         if self.circular:
             w = _haar_fwd(v, axes)
             hi = w[:, 1].contiguous()
-            w[:, 1] = self.norm.prox(hi, math.sqrt(2.0) * K * lam)
+            w[:, 1] = self.norm.prox(hi, thr)
             return (1.0 / K) * _haar_adj(w, axes)
         # replicate-pad by one at the end of each differenced axis
         vp = v
@@ -294,7 +297,7 @@ class TVNorm(Functional):
             region[2 + a] = slice(0, vp.shape[a] - 1)
         region = tuple(region)
         hi = w[region].contiguous()
-        w[region] = self.norm.prox(hi, math.sqrt(2.0) * K * lam)
+        w[region] = self.norm.prox(hi, thr)
         u = _haar_adj(w, axes)
         crop = tuple(slice(0, v.shape[a]) for a in range(nd))
         return (1.0 / K) * u[crop]
