@@ -10,7 +10,8 @@ under the float32 jax.numpy stand-in of make_xray2d_reference.py:
 * ``LinearSubproblemSolver.compute_rhs`` and ``.solve``
   (scico/optimize/_admmaux.py:231-269);
 * ``scico.solver.cg`` (scico/solver.py:326-405);
-* ``L21Norm._l2norm``, ``._prox``, ``.prox``, ``.__call__``
+* ``L21Norm._l2norm``, ``._prox``, ``.prox``, ``.__call__``, ``L1Norm.prox``,
+  ``.__call__``
   (scico/functional/_norm.py:238-296), ``ScaledFunctional.prox`` and
   ``__call__`` (scico/functional/_functional.py:159-198) and
   ``no_nan_divide`` (scico/numpy/util.py:302-315);
@@ -27,8 +28,10 @@ of jnp.diff's concatenate / slice / subtract), and the operator algebra of
 ``rho * C.adj(C(x)) + 2 * scale * A.adj(W(A(x)))``, scico/loss.py:259).
 
 It writes admm_reference_code.npz: per case the problem, the iterate x after
-every iteration, the final z and u, the CG step count of each x-update and
-the float32 itstat values.  tests/test_oracle.py checks the oracle's
+every iteration, the final z and u of every term, the CG step count of each
+x-update and the float32 itstat values; the cases include L2,1 + L1 on the
+same differences in 2D and on a volume with the reference's 3D projector
+(make_xray3d_reference.py).  tests/test_oracle.py checks the oracle's
 admm_tv against it bit for bit (iterates and step counts; itstat within
 float32 summation rounding) and tests/test_gpu_admm.py the GPU solver.
 
@@ -80,6 +83,11 @@ class _SNP2(_SNP):
     def stack(xs, axis=0):
         return _wrap(np.stack([np.asarray(x) for x in xs], axis=axis))
 
+    class util:
+        @staticmethod
+        def is_complex_dtype(dtype):
+            return np.dtype(dtype).kind == "c"
+
 
 def _source(checkout: Path, rel: str, cls: str | None, names):
     """The named functions (methods of ``cls`` if given) of a reference file,
@@ -128,6 +136,14 @@ def build(checkout: Path):
     for name in ("prox", "__call__"):
         _exec(src[name], ns, f"_norm.py:{name}")
         setattr(L21Norm, name, ns[name])
+
+    class L1Norm:
+        pass
+
+    src = _source(checkout, "scico/functional/_norm.py", "L1Norm", ["prox", "__call__"])
+    for name in ("prox", "__call__"):
+        _exec(src[name], ns, f"_norm.py:L1Norm.{name}")
+        setattr(L1Norm, name, staticmethod(ns[name]))
 
     class ScaledFunctional:
         def __init__(self, functional, scale):
@@ -201,9 +217,18 @@ def build(checkout: Path):
 
         def internal_init(self, admm):
             self.admm = admm
-            f, C, rho = admm.f, admm.C_list[0], admm.rho_list[0]
-            # rho * C.gram_op + f.hessian (operator sum and scalar multiple)
-            self.lhs_op = lambda x: rho * C.adj(C(x)) + 2 * f.scale * f.A.adj(f.W(f.A(x)))
+            f = admm.f
+
+            # reduce(+, [rho_i * C_i.gram_op]) + f.hessian (operator sums and
+            # scalar multiples, _admmaux.py:222-227)
+            def lhs(x):
+                acc = None
+                for rho, C in zip(admm.rho_list, admm.C_list):
+                    t = rho * C.adj(C(x))
+                    acc = t if acc is None else acc + t
+                return acc + 2 * f.scale * f.A.adj(f.W(f.A(x)))
+
+            self.lhs_op = lhs
 
     src = _source(checkout, "scico/optimize/_admmaux.py", "LinearSubproblemSolver", ["compute_rhs", "solve"])
     for name in ("compute_rhs", "solve"):
@@ -227,16 +252,21 @@ def build(checkout: Path):
         _exec(src[name], ns, f"_admm.py:{name}")
         setattr(ADMM, name, ns[name])
 
-    return dict(L21Norm=L21Norm, ScaledFunctional=ScaledFunctional, FiniteDifference=FiniteDifference,
+    return dict(L21Norm=L21Norm, L1Norm=L1Norm, ScaledFunctional=ScaledFunctional, FiniteDifference=FiniteDifference,
                 SquaredL2Loss=SquaredL2Loss, LinearSubproblemSolver=LinearSubproblemSolver, ADMM=ADMM,
                 cg=reference_cg(checkout), X=reference_functions(checkout))
 
 
-# Two regimes: CG stopped by its tolerance in every x-update (rho = 50), and
-# the benchmark-like split (rho = 2, lambda = 0.005, CG capped at 10 steps).
+# Two regimes with one L2,1 term: CG stopped by its tolerance in every
+# x-update (rho = 50), and the benchmark-like split (rho = 2, lambda 0.005,
+# CG capped at 10 steps); then L2,1 and L1 on the same differences, in 2D and
+# on a volume (the 3D workload's two-term pattern, rho 1, CG capped at 8).
 CASES = [
-    dict(n=24, nv=18, lam=0.05, rho=50.0, cg_tol=1e-4, cg_maxiter=100, iters=6, seed=1),
-    dict(n=32, nv=24, lam=0.005, rho=2.0, cg_tol=1e-4, cg_maxiter=10, iters=8, seed=2),
+    dict(kind=2, n=24, nv=18, lam=0.05, lam1=0.0, rho=50.0, cg_tol=1e-4, cg_maxiter=100, iters=6, seed=1),
+    dict(kind=2, n=32, nv=24, lam=0.005, lam1=0.0, rho=2.0, cg_tol=1e-4, cg_maxiter=10, iters=8, seed=2),
+    dict(kind=2, n=28, nv=20, lam=0.01, lam1=0.005, rho=1.0, cg_tol=1e-4, cg_maxiter=10, iters=6, seed=3),
+    dict(kind=3, shape=(10, 12, 12), det=(10, 18), nv=12, lam=0.01, lam1=0.01, rho=1.0, cg_tol=1e-4,
+         cg_maxiter=8, iters=4, seed=4),
 ]
 
 
@@ -244,31 +274,56 @@ def main():
     checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
     R = build(checkout)
     X = R["X"]
+    X3 = None
     out = {}
     for k, c in enumerate(CASES):
-        n, nv = c["n"], c["nv"]
-        ang = np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32)
-        g = ctref.xray2d_defaults((n, n), ang)
-        x0g, dx, y0, ny = _wrap(np.asarray(g["x0"], np.float32)), _wrap(np.asarray(g["dx"], np.float32)), \
-            float(g["y0"]), g["ny"]
-
-        class A:  # the 2D projector as a LinearOperator
-            def __call__(self, v):
-                return X._project(_wrap(np.asarray(v, np.float32)), x0g, dx, y0, ny, _wrap(ang))
-
-            def adj(self, s):
-                return X._back_project(_wrap(np.asarray(s, np.float32)), x0g, dx, (n, n), y0, _wrap(ang))
-
         rng = np.random.default_rng(c["seed"])
-        im = rng.random((n, n)).astype(np.float32)
+        extra = {}
+        if c["kind"] == 2:
+            n, nv = c["n"], c["nv"]
+            shape = (n, n)
+            ang = np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32)
+            g = ctref.xray2d_defaults(shape, ang)
+            x0g, dx, y0, ny = _wrap(np.asarray(g["x0"], np.float32)), _wrap(np.asarray(g["dx"], np.float32)), \
+                float(g["y0"]), g["ny"]
+
+            class A:  # the 2D projector as a LinearOperator
+                def __call__(self, v):
+                    return X._project(_wrap(np.asarray(v, np.float32)), x0g, dx, y0, ny, _wrap(ang))
+
+                def adj(self, s):
+                    return X._back_project(_wrap(np.asarray(s, np.float32)), x0g, dx, shape, y0, _wrap(ang))
+
+            extra = {"n": np.array(n), "nv": np.array(nv)}
+        else:
+            if X3 is None:
+                import make_xray3d_reference as m3
+
+                X3 = m3.reference_functions(checkout)
+            shape, det, nv = tuple(c["shape"]), tuple(c["det"]), c["nv"]
+            ang = np.linspace(0, np.pi, nv, endpoint=False)
+            M = np.asarray(X3.matrices_from_euler_angles(shape, det, "X", ang[:, None]), np.float32)
+
+            class A:  # the 3D projector (rotation about axis 0) as a LinearOperator
+                def __call__(self, v):
+                    return X3._project(_wrap(np.asarray(v, np.float32)), _wrap(M), det)
+
+                def adj(self, s):
+                    return X3._back_project(_wrap(np.asarray(s, np.float32)), _wrap(M), shape)
+
+            extra = {"shape": np.array(shape), "det": np.array(det), "M": M}
+        im = rng.random(shape).astype(np.float32)
         y = np.asarray(A()(im)).astype(np.float32)
         y = (y + rng.normal(0, 0.01 * float(np.abs(y).max()), y.shape)).astype(np.float32)
 
         f = R["SquaredL2Loss"](_wrap(y), A())
-        gfun = R["ScaledFunctional"](R["L21Norm"](), c["lam"])
-        C = R["FiniteDifference"]((n, n), append=0)
+        C = R["FiniteDifference"](shape, append=0)
+        gl, cl = [R["ScaledFunctional"](R["L21Norm"](), c["lam"])], [C]
+        if c["lam1"]:
+            gl.append(R["ScaledFunctional"](R["L1Norm"](), c["lam1"]))
+            cl.append(C)
         sp = R["LinearSubproblemSolver"](R["cg"], {"tol": c["cg_tol"], "maxiter": c["cg_maxiter"]})
-        admm = R["ADMM"](f, [gfun], [C], [c["rho"]], sp, _wrap(np.zeros((n, n), np.float32)))
+        admm = R["ADMM"](f, gl, cl, [c["rho"]] * len(gl), sp, _wrap(np.zeros(shape, np.float32)))
         xs, its, stats = [], [], []
         for _ in range(c["iters"]):
             admm.step()
@@ -277,11 +332,12 @@ def main():
             stats.append([float(np.asarray(admm.objective())), float(np.asarray(admm.norm_primal_residual())),
                           float(np.asarray(admm.norm_dual_residual()))])
         p = f"c{k}_"
-        out.update({p + "n": np.array(n), p + "nv": np.array(nv), p + "lam": np.array(c["lam"]),
+        out.update({p + key: v for key, v in extra.items()})
+        out.update({p + "kind": np.array(c["kind"]), p + "lam": np.array(c["lam"]), p + "lam1": np.array(c["lam1"]),
                     p + "rho": np.array(c["rho"]), p + "cg_tol": np.array(c["cg_tol"]),
                     p + "cg_maxiter": np.array(c["cg_maxiter"]), p + "y": y, p + "x": np.stack(xs),
-                    p + "z": np.asarray(admm.z_list[0]).astype(np.float32),
-                    p + "u": np.asarray(admm.u_list[0]).astype(np.float32),
+                    p + "z": np.stack([np.asarray(z).astype(np.float32) for z in admm.z_list]),
+                    p + "u": np.stack([np.asarray(u).astype(np.float32) for u in admm.u_list]),
                     p + "cg_iters": np.array(its), p + "itstat": np.array(stats)})
         print(k, "CG steps", its, "objective", [s[0] for s in stats])
     np.savez_compressed(HERE / "admm_reference_code.npz", **out)

@@ -76,31 +76,53 @@ def test_golden_admm(cuda):
 @pytest.mark.parametrize("fused", [False, True])
 def test_reference_code_admm(cuda, fused):
     """Against the iterates of scico's own ADMM / LinearSubproblemSolver / cg /
-    L21Norm / FiniteDifference / projector code run under the float32
-    jax.numpy stand-in (tests/golden/admm_reference_code.npz).  Case 0 (CG
-    stopped by its tolerance): x within 1e-4 rel l2 after every iteration
-    and the objective to 1e-4.  Case 1 (CG capped at 10): within 3x the
-    distance at which the same-precision oracle (float32 vectors, float64
+    L21Norm / L1Norm / FiniteDifference / projector code run under the
+    float32 jax.numpy stand-in (tests/golden/admm_reference_code.npz).  Case
+    0 (CG stopped by its tolerance): x within 1e-4 rel l2 after every
+    iteration and the objective to 1e-4.  The capped cases -- one L2,1 term;
+    L2,1 + L1 in 2D; L2,1 + L1 on a volume with the 3D projector: within 3x
+    the distance at which the same-precision oracle (float32 vectors, float64
     dots, as here) ends from the reference code, plus 1e-4."""
     z = np.load(GOLDEN / "admm_reference_code.npz")
-    for k in range(2):
+    for k in range(4):
         p = f"c{k}_"
-        n, nv = int(z[p + "n"]), int(z[p + "nv"])
-        ang = np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32)
         X, its = z[p + "x"], len(z[p + "x"])
-        kw = dict(lam21=float(z[p + "lam"]), rho=float(z[p + "rho"]), cg_tol=float(z[p + "cg_tol"]),
-                  cg_maxiter=int(z[p + "cg_maxiter"]))
+        lam21, lam1, rho = float(z[p + "lam"]), float(z[p + "lam1"]), float(z[p + "rho"])
+        cg_tol, cg_maxiter = float(z[p + "cg_tol"]), int(z[p + "cg_maxiter"])
+        if int(z[p + "kind"]) == 2:
+            n, nv = int(z[p + "n"]), int(z[p + "nv"])
+            shape = (n, n)
+            ang = np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32)
+            A = linop.XRayTransform2D(shape, ang)
+            g = ctref.xray2d_defaults(shape, ang)
+            fwd = lambda v: ctref.xray2d_project(v, g, np.float32)
+            adj = lambda s_: ctref.xray2d_back_project(s_, g, np.float32)
+        else:
+            shape, det, M = tuple(int(v) for v in z[p + "shape"]), tuple(int(v) for v in z[p + "det"]), z[p + "M"]
+            A = linop.XRayTransform3D(shape, M, det)
+            fwd = lambda v: ctref.xray3d_project(v, M, det, np.float32)
+            adj = lambda s_: ctref.xray3d_back_project(s_, M, shape, np.float32)
         obj_ref = z[p + "itstat"][:, 0]
         if k == 0:
             fx = fo = 0.0
         else:
-            g = ctref.xray2d_defaults((n, n), ang)
-            xm, hm, _, _ = _oracle(z[p + "y"], (n, n), g, dtype=np.float32, dot_dtype=np.float64,
-                                   lam_l21=kw["lam21"], rho=kw["rho"], maxiter=its, cg_tol=kw["cg_tol"],
-                                   cg_maxiter=kw["cg_maxiter"])
+            xm, hm, _, _ = ctref.admm_tv(fwd, adj, z[p + "y"], shape, lam_l21=lam21, lam_l1=lam1, rho=rho,
+                                         maxiter=its, cg_tol=cg_tol, cg_maxiter=cg_maxiter, dtype=np.float32,
+                                         dot_dtype=np.float64)
             fx = ctref.rel_l2(xm, X[-1])
             fo = float(np.max(np.abs(np.array([h["Objective"] for h in hm]) / obj_ref - 1)))
-        s = _solver(cuda, ang, z[p + "y"], (n, n), maxiter=its, fused=fused, **kw)
+
+        def solver(maxiter):
+            C = linop.FiniteDifference(shape, append=0)
+            gl, cl = [lam21 * functional.L21Norm()], [C]
+            if lam1:
+                gl.append(lam1 * functional.L1Norm())
+                cl.append(C)
+            return ADMM(f=loss.SquaredL2Loss(y=torch.from_numpy(z[p + "y"]).to(cuda), A=A), g_list=gl, C_list=cl,
+                        rho_list=[rho] * len(gl), maxiter=maxiter, fused=fused,
+                        subproblem_solver=LinearSubproblemSolver(cg_kwargs={"tol": cg_tol, "maxiter": cg_maxiter}))
+
+        s = solver(its)
         x = s.solve().cpu().numpy()
         ex = ctref.rel_l2(x, X[-1])
         eo = float(np.max(np.abs(np.array(s.history(transpose=True).Objective) / obj_ref - 1)))
@@ -108,7 +130,7 @@ def test_reference_code_admm(cuda, fused):
         assert eo <= 3 * fo + 1e-4, (k, eo, fo)
         if k == 0:
             for it in range(1, its):  # every intermediate iterate of the tolerance-stopped case
-                xi = _solver(cuda, ang, z[p + "y"], (n, n), maxiter=it, fused=fused, **kw).solve().cpu().numpy()
+                xi = solver(it).solve().cpu().numpy()
                 assert ctref.rel_l2(xi, X[it - 1]) <= 1e-4, (it, ctref.rel_l2(xi, X[it - 1]))
 
 

@@ -218,34 +218,41 @@ def test_cg_oracle_is_the_reference_code():
         assert info["num_iter"] == int(z[p + "num_iter"]) and info["rel_res"] == float(z[p + "rel_res"]), k
 
 
-def _admm_case(z, k):
-    p = f"c{k}_"
-    n, nv = int(z[p + "n"]), int(z[p + "nv"])
-    g = ctref.xray2d_defaults((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
-    kw = dict(lam_l21=float(z[p + "lam"]), rho=float(z[p + "rho"]), cg_tol=float(z[p + "cg_tol"]),
-              cg_maxiter=int(z[p + "cg_maxiter"]))
-    return p, n, g, kw
+def _admm_operators(z, p):
+    """The case's projector pair (the oracle's float32 2D or 3D projector)
+    and image shape."""
+    if int(z[p + "kind"]) == 2:
+        n, nv = int(z[p + "n"]), int(z[p + "nv"])
+        g = ctref.xray2d_defaults((n, n), np.linspace(0, np.pi, nv, endpoint=False).astype(np.float32))
+        return (lambda v: ctref.xray2d_project(v, g, np.float32),
+                lambda s: ctref.xray2d_back_project(s, g, np.float32), (n, n))
+    shape, det, M = tuple(int(v) for v in z[p + "shape"]), tuple(int(v) for v in z[p + "det"]), z[p + "M"]
+    return (lambda v: ctref.xray3d_project(v, M, det, np.float32),
+            lambda s: ctref.xray3d_back_project(s, M, shape, np.float32), shape)
 
 
 def test_admm_oracle_is_the_reference_code():
     """The oracle's ADMM-TV against scico's own ADMM.step, LinearSubproblemSolver
-    .compute_rhs/.solve, cg, L21Norm prox, FiniteDifference and projector
-    code executed under the float32 jax.numpy stand-in
+    .compute_rhs/.solve, cg, L21Norm / L1Norm prox, FiniteDifference and
+    projector code executed under the float32 jax.numpy stand-in
     (tests/golden/make_admm_reference.py): the iterate x after every
-    iteration, the final z and u and every x-update's CG step count are
-    bit-identical, with CG stopped by its tolerance (rho 50) and capped at 10
-    steps (rho 2, lambda 0.005).  The itstat values, which the reference sums
-    in float32 and the oracle in float64, agree to 1e-6."""
+    iteration, the final z and u of every term and every x-update's CG step
+    count are bit-identical -- CG stopped by its tolerance (rho 50), capped at
+    10 steps (rho 2, lambda 0.005), and L2,1 + L1 on the same differences in
+    2D and on a volume with the 3D projector.  The itstat values, which the
+    reference sums in float32 and the oracle in float64, agree to 1e-6."""
     z = np.load(GOLDEN / "admm_reference_code.npz")
-    for k in range(2):
-        p, n, g, kw = _admm_case(z, k)
-        fwd = lambda v: ctref.xray2d_project(v, g, np.float32)
-        adj = lambda s: ctref.xray2d_back_project(s, g, np.float32)
+    for k in range(4):
+        p = f"c{k}_"
+        fwd, adj, shape = _admm_operators(z, p)
+        kw = dict(lam_l21=float(z[p + "lam"]), lam_l1=float(z[p + "lam1"]), rho=float(z[p + "rho"]),
+                  cg_tol=float(z[p + "cg_tol"]), cg_maxiter=int(z[p + "cg_maxiter"]))
         X = z[p + "x"]
         for it in (1, len(X)):
-            x, hist, zl, ul = ctref.admm_tv(fwd, adj, z[p + "y"], (n, n), maxiter=it, dtype=np.float32, **kw)
+            x, hist, zl, ul = ctref.admm_tv(fwd, adj, z[p + "y"], shape, maxiter=it, dtype=np.float32, **kw)
             assert np.array_equal(x, X[it - 1]), (k, it)
-        assert np.array_equal(zl[0], z[p + "z"]) and np.array_equal(ul[0], z[p + "u"]), k
+        assert all(np.array_equal(a, b) for a, b in zip(zl, z[p + "z"])), k
+        assert all(np.array_equal(a, b) for a, b in zip(ul, z[p + "u"])), k
         assert [h["CG_It"] for h in hist] == list(z[p + "cg_iters"]), k
         ours = np.array([[h["Objective"], h["Prml_Rsdl"], h["Dual_Rsdl"]] for h in hist])
         np.testing.assert_allclose(ours, z[p + "itstat"], rtol=1e-6)
