@@ -47,6 +47,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
+DEFAULT_CHECKOUT = Path("/root/reference")  # the reference checkout read as text
 sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parent.parent))
 
@@ -271,7 +272,7 @@ CASES = [
 
 
 def main():
-    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_CHECKOUT
     R = build(checkout)
     X = R["X"]
     X3 = None

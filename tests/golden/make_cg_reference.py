@@ -21,6 +21,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
+DEFAULT_CHECKOUT = Path("/root/reference")  # the reference checkout read as text
 sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parent.parent))
 
@@ -61,7 +62,7 @@ CASES = [dict(n=24, nv=18, tol=1e-4, maxiter=100, seed=1), dict(n=32, nv=24, tol
 
 
 def main():
-    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_CHECKOUT
     X = reference_functions(checkout)
     cg = reference_cg(checkout)
     out = {}

@@ -24,6 +24,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
+DEFAULT_CHECKOUT = Path("/root/reference")  # the reference checkout read as text
 sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parent.parent))
 
@@ -84,7 +85,7 @@ CASES = [dict(n=24, nv=18, lmbda=0.1, maxiter=10, seed=1), dict(n=32, nv=30, lmb
 
 
 def main():
-    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_CHECKOUT
     X = mx.reference_functions(checkout)
     cg_solver = reference_cg_solver(checkout)
     out = {}

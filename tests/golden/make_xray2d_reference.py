@@ -33,6 +33,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
+DEFAULT_CHECKOUT = Path("/root/reference")  # the reference checkout read as text
 REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO))
 
@@ -236,7 +237,7 @@ CASES = [
 
 
 def main():
-    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_CHECKOUT
     X = reference_functions(checkout)
     out = {}
     for k, c in enumerate(CASES):

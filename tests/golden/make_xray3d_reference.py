@@ -26,6 +26,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
+DEFAULT_CHECKOUT = Path("/root/reference")  # the reference checkout read as text
 sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parent.parent))
 
@@ -87,7 +88,7 @@ def cases(X):
 
 
 def main():
-    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    checkout = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_CHECKOUT
     X = reference_functions(checkout)
     out = {}
     for k, (name, shape, det, M, euler) in enumerate(cases(X)):

@@ -456,3 +456,28 @@ def test_c_f64_build_matches_numpy_f64():
     assert ctref.rel_l2(x, xn) <= 1e-10
     # noise-free data: the data term is a small difference of large sums
     np.testing.assert_allclose(it[:, 0], [h["Objective"] for h in hist], rtol=1e-7)
+
+
+@pytest.mark.parametrize("script", ["make_xray2d_reference", "make_xray3d_reference", "make_cg_reference",
+                                    "make_admm_reference", "make_modl_cg_reference", "make_padmm_reference"])
+def test_reference_code_fixtures_reproduce(script, tmp_path, monkeypatch, capsys):
+    """Each committed reference-code fixture is exactly what its committed
+    script writes from the reference's sources (skipped where the reference
+    checkout is not present)."""
+    import importlib
+    import sys
+
+    monkeypatch.syspath_prepend(str(GOLDEN))
+    m = importlib.import_module(script)
+    if not (m.DEFAULT_CHECKOUT / "scico").is_dir():
+        pytest.skip("the reference checkout is not present here")
+    monkeypatch.setattr(m, "HERE", tmp_path)
+    monkeypatch.setattr(sys, "argv", [script])
+    m.main()
+    outs = sorted(tmp_path.glob("*.npz"))
+    assert outs
+    for o in outs:
+        a, b = np.load(o), np.load(GOLDEN / o.name)
+        assert set(a.files) == set(b.files), o.name
+        for k in a.files:
+            assert np.array_equal(a[k], b[k]), (o.name, k)
